@@ -1,0 +1,155 @@
+/*
+ * msc_gpu.h - C ABI of the GB300 (sm_103a) sorted deferred-shading path tracer.
+ *
+ * The render-loop entry points replace the public interface of the
+ * reference's engine class, msc::Pathtracer (include/core/Pathtracer.h:36-110
+ * of joshbainbridge/msc-project).  Every function returns MSC_OK (0) or a
+ * negative status; msc_last_error() gives the message.  No C++ exception
+ * crosses this boundary.  Pointers are plain host pointers unless a name ends
+ * in _device.  A handle is used by one render thread; msc_terminate() and
+ * msc_image() may be called from another thread.
+ */
+#ifndef MSC_GPU_H_
+#define MSC_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSC_OK 0
+#define MSC_ERR_ARG (-1)       /* bad argument or null handle */
+#define MSC_ERR_SCENE (-2)     /* scene file could not be read or is malformed */
+#define MSC_ERR_CUDA (-3)      /* a CUDA call failed (no device, out of memory, launch error) */
+#define MSC_ERR_DEVICE (-4)    /* a device stage reported an error flag (bin overflow, stack overflow) */
+#define MSC_ERR_BUSY (-5)      /* the handle is rendering on another thread */
+
+typedef struct msc_handle msc_handle;
+
+/* Pathtracer::Pathtracer(const std::string&) - include/core/Pathtracer.h:44,
+ * src/core/Pathtracer.cpp:369-379.  Loads the two-document YAML scene (and the
+ * OBJ files it names), builds the device BVH and allocates the render buffers
+ * on the current CUDA device. */
+int msc_create(const char* yaml_path, msc_handle** out);
+
+/* Pathtracer::~Pathtracer() - include/core/Pathtracer.h:49, src/core/Pathtracer.cpp:381-392. */
+int msc_destroy(msc_handle* h);
+
+/* int Pathtracer::process() - include/core/Pathtracer.h:82, src/core/Pathtracer.cpp:425-493.
+ * Renders one iteration (every pixel x sample), adds the filtered result to
+ * the accumulated image and copies it to the host mirror.  *iteration gets
+ * the new iteration count, or 0 when msc_terminate() stopped the pass. */
+int msc_process(msc_handle* h, int* iteration);
+
+/* Same as msc_process without the device-to-host copy of the image; the
+ * host mirror is refreshed by the next msc_image() call. */
+int msc_process_device(msc_handle* h, int* iteration);
+
+/* void Pathtracer::image(float**, int*, int*) - include/core/Pathtracer.h:58,
+ * src/core/Pathtracer.cpp:394-400.  Row-major y*W+x, 3 floats per pixel, the
+ * sum over iterations (divide by the iteration count to display).  The
+ * buffer is owned by the handle and valid until the next process/clear/destroy. */
+int msc_image(msc_handle* h, const float** rgb, int* width, int* height);
+
+/* void Pathtracer::clear() - include/core/Pathtracer.h:63, src/core/Pathtracer.cpp:402-413. */
+int msc_clear(msc_handle* h);
+
+/* bool Pathtracer::active() - include/core/Pathtracer.h:70, src/core/Pathtracer.cpp:415-418. */
+int msc_active(msc_handle* h, int* active);
+
+/* void Pathtracer::terminate() - include/core/Pathtracer.h:75, src/core/Pathtracer.cpp:420-423.
+ * Thread-safe; a running msc_process stops at its next batch boundary. */
+int msc_terminate(msc_handle* h);
+
+/* Message of the last failing call on this handle (or of the last failed msc_create when h is NULL). */
+const char* msc_last_error(msc_handle* h);
+
+/* ---- introspection (no reference counterpart beyond the batch loop's stdout progress,
+ *      src/core/Pathtracer.cpp:435-438,453) ---- */
+typedef struct msc_stats {
+  uint64_t closest_queries;   /* closest-hit ray queries in the last process() */
+  uint64_t shadow_queries;    /* occlusion ray queries in the last process() */
+  uint64_t batches;           /* ray batches processed */
+  uint64_t kernel_launches;   /* kernels enqueued by the last process() */
+  double process_ms;          /* device time of the last process(), CUDA events */
+  double stage_ms[12];        /* per-stage device time when profiling is on (see MSC_STAGE_*) */
+  uint64_t stage_launches[12];
+  int width, height, spp, triangles, lights, iteration;
+} msc_stats;
+
+enum {
+  MSC_STAGE_RAYGEN = 0, MSC_STAGE_BINS = 1, MSC_STAGE_RAYKEYS = 2, MSC_STAGE_RAYSORT = 3,
+  MSC_STAGE_GATHER = 4, MSC_STAGE_TRACE = 5, MSC_STAGE_HITSORT = 6, MSC_STAGE_SHADE = 7,
+  MSC_STAGE_SHADOW = 8, MSC_STAGE_FILTER = 9, MSC_STAGE_OTHER = 10, MSC_STAGE_COUNT = 11
+};
+
+int msc_get_stats(msc_handle* h, msc_stats* out);
+/* 1: bracket every stage with CUDA events (adds host syncs; for measurement runs only). */
+int msc_set_profiling(msc_handle* h, int on);
+
+/* Per-sample radiance and film position of the last iteration (Image::samples,
+ * include/core/Image.h:15-19): rgb gets 3*N floats, xy 2*N floats, N = W*H*spp,
+ * in sampleID order x*H*spp + y*spp + i. */
+int msc_get_samples(msc_handle* h, float* rgb, float* xy);
+
+/* ---- stage entry points on host arrays (one call = upload, kernel, download) ---- */
+
+/* Cardinal direction bin of each direction (src/core/Camera.cpp:42-44,
+ * src/core/Integrator.cpp:240-242).  dirs: 3*n floats. */
+int msc_stage_cardinal(const float* dirs, int n, int32_t* bins);
+
+/* Stable partition of rays into the six cardinal bins (DirectionalBins::add,
+ * src/core/DirectionalBins.cpp:37-73).  rays: 12 floats per ray
+ * (org.xyz, lastPdf, dir.xyz, depth-as-int, weight.rgb, sampleID-as-int);
+ * a ray whose depth word is negative is dropped.  out: 6*cap*12 floats,
+ * bin b at [b*cap, (b+1)*cap); counts: 6 ints. */
+int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts);
+
+/* 32-bit ray sort keys in the origin box of the given rays (replaces the
+ * median split of RaySort, src/core/RaySort.cpp:7-118). org, dir: 3*n floats. */
+int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys);
+
+/* Stable LSD radix sort of (keys, vals) on bits [0, bits); sorted in place. */
+int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
+
+/* Device-pointer form of msc_sort_pairs on the given CUDA stream (0 = default).
+ * Scratch is allocated per call. */
+int msc_sort_pairs_device(uint32_t* keys, uint32_t* vals, int n, int bits, void* stream);
+
+/* Closest hit against the handle's scene (rtcIntersect, src/core/RayIntersect.cpp:7-12)
+ * on [0.001, 1e5].  geom/prim are the reference's geomID/primID, -1 for a miss. */
+int msc_trace_closest(msc_handle* h, const float* org, const float* dir, int n, float* t, float* u, float* v,
+                      int32_t* geom, int32_t* prim);
+
+/* Occlusion against non-emitter geometry on (0.001, tmax) (rtcOccluded with mask
+ * 0x0FFFFFFF, src/core/Integrator.cpp:153-174).  occluded[i] = 1 when blocked. */
+int msc_trace_occluded(msc_handle* h, const float* org, const float* dir, const float* tmax, int n,
+                       int32_t* occluded);
+
+/* ---- host-only scene input (no GPU needed) ---- */
+
+/* OBJ reading with tinyobjloader's rules (thirdparty/tinyobjloader/tiny_obj_loader.cpp:309-412,
+ * 643-891, as PolygonObject::construct calls it, src/core/PolygonObject.cpp:7-8).
+ * sizes[0..2] = float count of positions, float count of texcoords, index count;
+ * pass NULL arrays to query the sizes first. */
+int msc_obj_load(const char* path, float* positions, float* texcoords, uint32_t* indices, int64_t* sizes);
+
+/* Parses a scene YAML and its OBJ files on the host only (Pathtracer::construct,
+ * src/core/Pathtracer.cpp:32-275).  info[0..7] = width, height, spp, triangles,
+ * lights, shaders, geometries, camera type.  tri_v (9 floats per triangle, world
+ * space, geomID order) and tri_geom may be NULL. */
+int msc_scene_load_host(const char* yaml_path, int32_t* info, float* tri_v, int32_t* tri_geom);
+
+/* Writes a seeded synthetic scene (YAML + OBJ files) into out_dir.
+ * config 0: the Cornell-style box; config 1: the terrain + icospheres scene;
+ * config 100: a tiny test scene.  scale in (0, 1] shrinks geometry, image and
+ * sample counts for tests.  The YAML path is written to yaml_path (size cap). */
+int msc_generate_scene(int config, uint32_t seed, double scale, const char* out_dir, char* yaml_path, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSC_GPU_H_ */

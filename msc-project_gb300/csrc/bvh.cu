@@ -1,0 +1,259 @@
+// Device LBVH build (Karras, "Maximizing Parallelism in the Construction of
+// BVHs, Octrees, and k-d Trees", HPG 2012), replacing the Embree scene build
+// of the reference (rtcNewTriangleMesh/rtcCommit, src/core/Pathtracer.cpp:171-201,
+// 242-274).  Steps: centroid bounds -> 30-bit Morton codes -> stable radix
+// sort -> one thread per internal node finds its range and split -> one
+// thread per leaf walks to the root, the second arrival at each node
+// forming its box -> pack into the traversal layout of trace.cuh.
+#include "bvh.h"
+#include "dmath.h"
+#include "radix.cuh"
+
+namespace mscg {
+
+namespace {
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// bounds[0..2] = min (ordered ints), bounds[3..5] = max
+__global__ void k_centroid_bounds(const float* __restrict__ v, int n, uint32_t* bounds) {
+  float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      float c = (v[9 * t + a] + v[9 * t + 3 + a] + v[9 * t + 6 + a]) * (1.0f / 3.0f);
+      mn[a] = fminf(mn[a], c);
+      mx[a] = fmaxf(mx[a], c);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&bounds[a], f2ord(mn[a]));
+      atomicMax(&bounds[3 + a], f2ord(mx[a]));
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t morton30(float3 c, float3 lo, float3 sc) {
+  uint32_t x = (uint32_t)min(max((int)floorf((c.x - lo.x) * sc.x), 0), 1023);
+  uint32_t y = (uint32_t)min(max((int)floorf((c.y - lo.y) * sc.y), 0), 1023);
+  uint32_t z = (uint32_t)min(max((int)floorf((c.z - lo.z) * sc.z), 0), 1023);
+  return (spread_bits_3(x) << 2) | (spread_bits_3(y) << 1) | spread_bits_3(z);
+}
+
+__global__ void k_morton(const float* __restrict__ v, int n, const uint32_t* __restrict__ bounds,
+                         uint32_t* __restrict__ codes) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  float3 lo = f3(ord2f(bounds[0]), ord2f(bounds[1]), ord2f(bounds[2]));
+  float3 hi = f3(ord2f(bounds[3]), ord2f(bounds[4]), ord2f(bounds[5]));
+  float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+  float3 sc = f3(ex > 0.f ? 1024.0f / ex : 0.f, ey > 0.f ? 1024.0f / ey : 0.f, ez > 0.f ? 1024.0f / ez : 0.f);
+  float3 c;
+  c.x = (v[9 * t + 0] + v[9 * t + 3] + v[9 * t + 6]) * (1.0f / 3.0f);
+  c.y = (v[9 * t + 1] + v[9 * t + 4] + v[9 * t + 7]) * (1.0f / 3.0f);
+  c.z = (v[9 * t + 2] + v[9 * t + 5] + v[9 * t + 8]) * (1.0f / 3.0f);
+  codes[t] = morton30(c, lo, sc);
+}
+
+__device__ __forceinline__ int lcp(const uint32_t* __restrict__ codes, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  uint32_t a = codes[i], b = codes[j];
+  if (a == b) return 32 + __clz((uint32_t)(i ^ j));
+  return __clz(a ^ b);
+}
+
+// parent[] holds the parents of internal nodes [0, n-1) then of leaves [n-1, 2n-1).
+__global__ void k_karras(const uint32_t* __restrict__ codes, int n, int2* __restrict__ children,
+                         int* __restrict__ parent) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int d = (lcp(codes, n, i, i + 1) - lcp(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = lcp(codes, n, i, i - d);
+  int lmax = 2;
+  while (lcp(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (lcp(codes, n, i, i + (l + t) * d) > dmin) l += t;
+  int j = i + l * d;
+  int dnode = lcp(codes, n, i, j);
+  int s = 0;
+  int t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (lcp(codes, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  int gamma = i + s * d + min(d, 0);
+  int left = (min(i, j) == gamma) ? ~gamma : gamma;
+  int right = (max(i, j) == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  children[i] = make_int2(left, right);
+  parent[left >= 0 ? left : (n - 1) + ~left] = i;
+  parent[right >= 0 ? right : (n - 1) + ~right] = i;
+  if (i == 0) parent[0] = -1;
+}
+
+// Leaf k holds triangle order[k]; writes the traversal triangle record and the leaf box.
+__global__ void k_leaves(const float* __restrict__ v, const int* __restrict__ geom, const uint8_t* __restrict__ is_light,
+                         const uint32_t* __restrict__ order, int n, float4* __restrict__ tris, int* __restrict__ tri_orig,
+                         float4* __restrict__ leaf_box) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int t = (int)order[k];
+  float3 v0 = f3(v[9 * t + 0], v[9 * t + 1], v[9 * t + 2]);
+  float3 v1 = f3(v[9 * t + 3], v[9 * t + 4], v[9 * t + 5]);
+  float3 v2 = f3(v[9 * t + 6], v[9 * t + 7], v[9 * t + 8]);
+  float3 e1 = v_sub(v1, v0), e2 = v_sub(v2, v0);
+  tris[3 * k + 0] = make_float4(v0.x, v0.y, v0.z, __int_as_float(geom[t]));
+  tris[3 * k + 1] = make_float4(e1.x, e1.y, e1.z, __int_as_float((int)is_light[t]));
+  tris[3 * k + 2] = make_float4(e2.x, e2.y, e2.z, __int_as_float(t));
+  tri_orig[k] = t;
+  leaf_box[2 * k + 0] = make_float4(fminf(fminf(v0.x, v1.x), v2.x), fminf(fminf(v0.y, v1.y), v2.y),
+                                    fminf(fminf(v0.z, v1.z), v2.z), 0.f);
+  leaf_box[2 * k + 1] = make_float4(fmaxf(fmaxf(v0.x, v1.x), v2.x), fmaxf(fmaxf(v0.y, v1.y), v2.y),
+                                    fmaxf(fmaxf(v0.z, v1.z), v2.z), 0.f);
+}
+
+__device__ __forceinline__ void load_box(int c, const float4* leaf_box, const float4* node_box, float4* lo, float4* hi) {
+  if (c < 0) {
+    *lo = leaf_box[2 * (~c) + 0];
+    *hi = leaf_box[2 * (~c) + 1];
+  } else {
+    *lo = __ldcg(&node_box[2 * c + 0]);
+    *hi = __ldcg(&node_box[2 * c + 1]);
+  }
+}
+
+// One thread per leaf; the second thread to reach a node builds its box and
+// continues upward.  No thread waits on another.
+__global__ void k_refit(const int2* __restrict__ children, const int* __restrict__ parent, int n,
+                        const float4* __restrict__ leaf_box, float4* node_box, int* flags, int* err) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int p = parent[(n - 1) + k];
+  int level = 0;
+  while (p >= 0) {
+    if (++level > n) {  // a parent chain longer than the tree can only come from a malformed hierarchy
+      atomicOr(err, 1);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(&flags[p], 1) == 0) return;
+    __threadfence();
+    int2 ch = children[p];
+    float4 l0, h0, l1, h1;
+    load_box(ch.x, leaf_box, node_box, &l0, &h0);
+    load_box(ch.y, leaf_box, node_box, &l1, &h1);
+    float4 lo = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f);
+    float4 hi = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f);
+    __stcg(&node_box[2 * p + 0], lo);
+    __stcg(&node_box[2 * p + 1], hi);
+    p = parent[p];
+  }
+}
+
+__global__ void k_pack(const int2* __restrict__ children, int n, const float4* __restrict__ leaf_box,
+                       const float4* __restrict__ node_box, float4* __restrict__ nodes) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int2 ch = children[i];
+  float4 l0, h0, l1, h1;
+  load_box(ch.x, leaf_box, node_box, &l0, &h0);
+  load_box(ch.y, leaf_box, node_box, &l1, &h1);
+  nodes[4 * i + 0] = make_float4(l0.x, h0.x, l0.y, h0.y);
+  nodes[4 * i + 1] = make_float4(l1.x, h1.x, l1.y, h1.y);
+  nodes[4 * i + 2] = make_float4(l0.z, h0.z, l1.z, h1.z);
+  nodes[4 * i + 3] = make_float4(__int_as_float(ch.x), __int_as_float(ch.y), 0.f, 0.f);
+}
+
+// Scene bounds of all vertices (used to place direction-only tests and for stats).
+__global__ void k_scene_bounds(const float4* __restrict__ node_box, float* out) {
+  out[0] = node_box[0].x; out[1] = node_box[0].y; out[2] = node_box[0].z;
+  out[3] = node_box[1].x; out[4] = node_box[1].y; out[5] = node_box[1].z;
+}
+
+size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n, DeviceBvh* out, cudaStream_t stream,
+              std::string* err) {
+  if (n < 2) { *err = "the BVH needs at least two triangles"; return -1; }
+  int launches = 0;
+  out->num_tris = n;
+  out->num_nodes = n - 1;
+  // persistent buffers
+  if (cudaMalloc(&out->nodes, (size_t)(n - 1) * 4 * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&out->tris, (size_t)n * 3 * sizeof(float4)) != cudaSuccess ||
+      cudaMalloc(&out->tri_orig, (size_t)n * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&out->bounds_dev, 8 * sizeof(float)) != cudaSuccess) {
+    *err = "out of device memory for the BVH";
+    return -1;
+  }
+  // build scratch
+  size_t bytes = al(6 * 4) + al((size_t)n * 4) * 2 + al((size_t)(n - 1) * sizeof(int2)) + al((size_t)(2 * n) * 4) +
+                 al((size_t)n * 2 * sizeof(float4)) + al((size_t)(n - 1) * 2 * sizeof(float4)) + al((size_t)n * 4) +
+                 sort_scratch_bytes(n);
+  char* scratch = nullptr;
+  if (cudaMalloc(&scratch, bytes) != cudaSuccess) { *err = "out of device memory for the BVH build"; return -1; }
+  char* p = scratch;
+  uint32_t* bounds = (uint32_t*)p; p += al(6 * 4);
+  uint32_t* codes = (uint32_t*)p; p += al((size_t)n * 4);
+  uint32_t* order = (uint32_t*)p; p += al((size_t)n * 4);
+  int2* children = (int2*)p; p += al((size_t)(n - 1) * sizeof(int2));
+  int* parent = (int*)p; p += al((size_t)(2 * n) * 4);
+  float4* leaf_box = (float4*)p; p += al((size_t)n * 2 * sizeof(float4));
+  float4* node_box = (float4*)p; p += al((size_t)(n - 1) * 2 * sizeof(float4));
+  int* flags = (int*)p; p += al((size_t)n * 4);
+  SortScratch ss;
+  sort_scratch_bind(&ss, p, n);
+
+  cudaMemsetAsync(bounds, 0xff, 12, stream);
+  cudaMemsetAsync(bounds + 3, 0x00, 20, stream);  // max words and the error word bounds[7]
+  cudaMemsetAsync(flags, 0, (size_t)n * 4, stream);
+  const int tb = 256;
+  const int g = (n + tb - 1) / tb;
+  k_centroid_bounds<<<min(g, 1024), tb, 0, stream>>>(d_v, n, bounds);
+  k_morton<<<g, tb, 0, stream>>>(d_v, n, bounds, codes);
+  launches += 2;
+  launches += sort_pairs(codes, nullptr, codes, order, n, 30, ss, stream);
+  k_karras<<<(n - 1 + tb - 1) / tb, tb, 0, stream>>>(codes, n, children, parent);
+  k_leaves<<<g, tb, 0, stream>>>(d_v, d_geom, d_light, order, n, out->tris, out->tri_orig, leaf_box);
+  k_refit<<<g, tb, 0, stream>>>(children, parent, n, leaf_box, node_box, flags, (int*)(bounds + 7));
+  k_pack<<<(n - 1 + tb - 1) / tb, tb, 0, stream>>>(children, n, leaf_box, node_box, out->nodes);
+  k_scene_bounds<<<1, 1, 0, stream>>>(node_box, out->bounds_dev);
+  launches += 5;
+  int refit_err = 0;
+  cudaMemcpyAsync(&refit_err, bounds + 7, 4, cudaMemcpyDeviceToHost, stream);
+  cudaError_t e = cudaStreamSynchronize(stream);
+  cudaFree(scratch);
+  if (e != cudaSuccess) { *err = std::string("BVH build failed: ") + cudaGetErrorString(e); return -1; }
+  if (refit_err != 0) { *err = "BVH build produced a malformed hierarchy"; return -1; }
+  return launches;
+}
+
+void bvh_free(DeviceBvh* b) {
+  if (b->nodes) cudaFree(b->nodes);
+  if (b->tris) cudaFree(b->tris);
+  if (b->tri_orig) cudaFree(b->tri_orig);
+  if (b->bounds_dev) cudaFree(b->bounds_dev);
+  b->bounds_dev = nullptr;
+  b->nodes = nullptr;
+  b->tris = nullptr;
+  b->tri_orig = nullptr;
+}
+
+}  // namespace mscg

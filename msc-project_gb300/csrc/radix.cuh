@@ -1,0 +1,127 @@
+// Tile-local stable ranking and the LSD radix sort of 32-bit key/value pairs.
+//
+// A tile is BLOCK threads x ITEMS items.  Warp w owns the contiguous
+// sub-tile [w*32*ITEMS, (w+1)*32*ITEMS); in round k lane l holds item
+// w*32*ITEMS + k*32 + l.  Within a round, lanes holding the same digit find
+// each other with __match_any_sync; the lowest such lane bumps a per-warp
+// digit counter.  Prefixes over warps then give every item its position in
+// the tile sorted stably by digit, which is used to stage the tile in shared
+// memory so the global scatter writes contiguous runs per digit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mscg {
+
+template <int BLOCK, int RADIX>
+struct RankSmem {
+  int whist[BLOCK / 32][RADIX];
+  int tile_start[RADIX];
+  int tile_count[RADIX];
+  int scan_tmp[BLOCK / 32 + 1];
+};
+
+// Exclusive scan of sm.tile_count[0..RADIX) into sm.tile_start.
+template <int BLOCK, int RADIX>
+__device__ __forceinline__ void tile_digit_scan(RankSmem<BLOCK, RADIX>& sm) {
+  constexpr int PER = (RADIX + BLOCK - 1) / BLOCK;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int vals[PER];
+  int local = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    int d = t * PER + k;
+    vals[k] = d < RADIX ? sm.tile_count[d] : 0;
+    local += vals[k];
+  }
+  int incl = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) sm.scan_tmp[warp] = incl;
+  __syncthreads();
+  if (t == 0) {
+    int run = 0;
+    for (int w = 0; w < BLOCK / 32; ++w) { int c = sm.scan_tmp[w]; sm.scan_tmp[w] = run; run += c; }
+  }
+  __syncthreads();
+  int excl = sm.scan_tmp[warp] + incl - local;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    int d = t * PER + k;
+    if (d < RADIX) sm.tile_start[d] = excl;
+    excl += vals[k];
+  }
+}
+
+// digit[k] < 0 marks an empty slot.  On return pos[k] is the item's index in
+// the tile sorted stably by digit (-1 for empty slots), sm.tile_count holds
+// the tile histogram and sm.tile_start its exclusive scan.
+template <int BLOCK, int ITEMS, int RADIX>
+__device__ __forceinline__ void tile_rank(const int (&digit)[ITEMS], int (&pos)[ITEMS], RankSmem<BLOCK, RADIX>& sm) {
+  constexpr int WARPS = BLOCK / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < WARPS * RADIX; i += BLOCK) (&sm.whist[0][0])[i] = 0;
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+  int rank[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int d = digit[k];
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    int old = 0;
+    if (d >= 0 && lane == leader) {
+      old = sm.whist[warp][d];
+      sm.whist[warp][d] = old + __popc(peers);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rank[k] = old + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < RADIX; d += BLOCK) {
+    int run = 0;
+#pragma unroll
+    for (int w = 0; w < WARPS; ++w) { int c = sm.whist[w][d]; sm.whist[w][d] = run; run += c; }
+    sm.tile_count[d] = run;
+  }
+  __syncthreads();
+  tile_digit_scan<BLOCK, RADIX>(sm);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int d = digit[k];
+    pos[k] = d >= 0 ? sm.tile_start[d] + sm.whist[warp][d] + rank[k] : -1;
+  }
+}
+
+// Single-block exclusive scan of data[0..len) in place; total written to *total if non-null.
+__global__ void k_scan_exclusive(uint32_t* data, int len, uint32_t* total);
+
+struct SortScratch {
+  uint32_t* keys_alt = nullptr;
+  uint32_t* vals_alt = nullptr;
+  uint32_t* counts = nullptr;   // RADIX * max tiles
+  int capacity = 0;
+};
+
+constexpr int kSortBlock = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortBlock * kSortItems;
+constexpr int kSortRadixBits = 8;
+
+size_t sort_scratch_bytes(int capacity);
+// Carves the scratch buffers out of `base` (sort_scratch_bytes(capacity) bytes, 256-aligned).
+void sort_scratch_bind(SortScratch* s, void* base, int capacity);
+
+// Stable LSD sort of (keys_in, vals_in) on bits [0, bits) into (keys_out, vals_out).
+// vals_in == nullptr means vals_in[i] = i.  Input buffers are left unchanged
+// unless they alias the outputs.  Returns the number of kernel launches.
+int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
+               int bits, SortScratch& s, cudaStream_t stream);
+
+}  // namespace mscg

@@ -1,0 +1,613 @@
+// Device stages of one render iteration.  Each kernel cites the reference
+// code whose arithmetic it restates.
+#include "radix.cuh"
+#include "render.h"
+#include "trace.cuh"
+
+namespace mscg {
+
+namespace {
+
+constexpr int TB = 256;
+inline int grid_for(int n, int tb = TB) { return (n + tb - 1) / tb; }
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ float mis_weight(float a, float b, int power) {
+  if (power) {  // power heuristic, beta = 2
+    float a2 = a * a;
+    return a2 / (a2 + b * b);
+  }
+  return a / (a + b);  // misBalance, include/core/Common.h:45-48
+}
+
+// ------------------------------------------------------------------ raygen
+// Camera::operator() (src/core/Camera.cpp:6-59) with StratifiedSampler
+// (src/core/StratifiedSampler.cpp:5-17), IndependentSampler, GridSampler and
+// PinHoleCamera::sample (src/core/PinHoleCamera.cpp:16-32) /
+// ThinLensCamera::sample (src/core/ThinLensCamera.cpp:16-56).
+// sampleID = x*H*spp + y*spp + i (Camera.cpp:28).
+__global__ void __launch_bounds__(TB) k_raygen(DevFrame f, uint32_t first, int n, RayBuf out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const uint32_t sid = first + (uint32_t)t;
+  const uint32_t col = (uint32_t)f.height * (uint32_t)f.spp;
+  const uint32_t x = sid / col;
+  const uint32_t rem = sid - x * col;
+  const uint32_t y = rem / (uint32_t)f.spp;
+  const uint32_t i = rem - y * (uint32_t)f.spp;
+  const uint4 r = path_draws(sid, f.iter_seed, 0u, 0u);
+  float sx, sy;
+  const uint32_t ix = i / (uint32_t)f.grid_y, iy = i - ix * (uint32_t)f.grid_y;
+  const float cellx = 1.f / (float)f.grid_x, celly = 1.f / (float)f.grid_y;
+  if (f.sampler == SAMPLER_INDEPENDENT) {
+    sx = u01(r.x);
+    sy = u01(r.y);
+  } else if (f.sampler == SAMPLER_GRID) {
+    sx = (float)ix * cellx + 0.5f * cellx;
+    sy = (float)iy * celly + 0.5f * celly;
+  } else {
+    sx = (float)ix * cellx + u01(r.x) * cellx;
+    sy = (float)iy * celly + u01(r.y) * celly;
+  }
+  const float px = (float)x + sx, py = (float)y + sy;
+  f.sample_rgb[sid] = make_float4(0.f, 0.f, 0.f, 0.f);
+  f.sample_pos[sid] = make_float2(px, py);
+  const float W = (float)f.width, H = (float)f.height;
+  const float fx = ((px * 2.f - W) / W) * 36.f;
+  const float fy = ((py * 2.f - H) / W) * 36.f;
+  const CameraRec& c = f.cam;
+  const float3 cn = f3(c.normal[0], c.normal[1], c.normal[2]);
+  const float3 ct = f3(c.translation[0], c.translation[1], c.translation[2]);
+  const float3 nodal = v_add(ct, v_mul(cn, c.focal_length));
+  const float3 film = xf_point(c.xf, f3(0.f, fy, fx));
+  float3 org, dir;
+  if (c.type == CAMERA_THINLENS) {
+    const float ratio = c.focal_distance / c.focal_length;
+    const float3 focal = v_add(film, v_mul(v_sub(nodal, film), ratio));
+    // rejection sampling of the unit-diameter disc, two draws per attempt
+    float ax = 0.f, ay = 0.f;
+    // attempt 0 uses draws 2,3 of the camera block; attempt k >= 1 uses
+    // block 1 + k/2 (draws 0,1 for odd k, 2,3 for even k)
+    uint4 q = r;
+    for (int attempt = 0; attempt < 64; ++attempt) {
+      uint32_t a, b;
+      if (attempt == 0) {
+        a = r.z;
+        b = r.w;
+      } else {
+        if (attempt & 1) q = path_draws(sid, f.iter_seed, 0u, 1u + (uint32_t)(attempt >> 1));
+        a = (attempt & 1) ? q.x : q.z;
+        b = (attempt & 1) ? q.y : q.w;
+      }
+      const float tx = u01(a) - 0.5f, ty = u01(b) - 0.5f;
+      if (sqrtf(tx * tx + ty * ty) < 0.5f) { ax = tx; ay = ty; break; }
+    }
+    const float scale = c.focal_length / c.aperture;
+    const float3 ap = xf_point(c.xf, f3(0.f, ax * scale, ay * scale));
+    org = v_add(ap, v_mul(cn, c.focal_length));
+    dir = v_normalize(v_sub(focal, org));
+  } else {
+    org = nodal;
+    dir = v_normalize(v_sub(nodal, film));
+  }
+  out.o[t] = make_float4(org.x, org.y, org.z, 1.f);
+  out.d[t] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0));
+  out.w[t] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)sid));
+}
+
+// -------------------------------------------------------- bin partition
+// DirectionalBins::add (src/core/DirectionalBins.cpp:37-73) as a stable
+// counting partition: count digits per tile, scan, scatter.
+constexpr int PB = 256;
+constexpr int PITEMS = kPartTile / PB;
+constexpr int PRADIX = kMaxBins;
+constexpr int kDead = 6;
+
+__device__ __forceinline__ int ray_digit(const float4& d) {
+  if (__float_as_int(d.w) < 0) return kDead;
+  return cardinal_bin(f3(d));
+}
+
+__global__ void __launch_bounds__(PB) k_part_count(const float4* __restrict__ d, int n, uint32_t* __restrict__ counts,
+                                                   int tiles) {
+  __shared__ int hist[PRADIX];
+  if (threadIdx.x < PRADIX) hist[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kPartTile;
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < PITEMS; ++k) {
+    int idx = base + k * PB + threadIdx.x;
+    int dg = idx < n ? ray_digit(d[idx]) : -1;
+    unsigned peers = __match_any_sync(0xffffffffu, dg);
+    if (dg >= 0 && lane == __ffs(peers) - 1) atomicAdd(&hist[dg], __popc(peers));
+  }
+  __syncthreads();
+  if (threadIdx.x < PRADIX) counts[threadIdx.x * tiles + blockIdx.x] = (uint32_t)hist[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n, const uint32_t* __restrict__ scanned, int tiles,
+                                                     RayBuf dst, int cap, const int* __restrict__ bin_count) {
+  __shared__ RankSmem<PB, PRADIX> sm;
+  __shared__ uint32_t sidx[kPartTile];
+  __shared__ int gofs[PRADIX];
+  const int tile = blockIdx.x, base = tile * kPartTile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < PRADIX) {
+    const int b = threadIdx.x;
+    gofs[b] = (b < kDead) ? b * cap + bin_count[b] + (int)(scanned[b * tiles + tile] - scanned[b * tiles]) : 0;
+  }
+  int dig[PITEMS], pos[PITEMS];
+#pragma unroll
+  for (int k = 0; k < PITEMS; ++k) {
+    int idx = base + warp * 32 * PITEMS + k * 32 + lane;
+    dig[k] = idx < n ? ray_digit(src.d[idx]) : -1;
+  }
+  tile_rank<PB, PITEMS, PRADIX>(dig, pos, sm);
+#pragma unroll
+  for (int k = 0; k < PITEMS; ++k)
+    if (pos[k] >= 0) sidx[pos[k]] = (uint32_t)((warp * 32 * PITEMS + k * 32 + lane) | (dig[k] << 16));
+  __syncthreads();
+  const int count = min(kPartTile, n - base);
+  for (int p = threadIdx.x; p < count; p += PB) {
+    uint32_t e = sidx[p];
+    int b = (int)(e >> 16);
+    if (b >= kDead) continue;
+    int s = base + (int)(e & 0xffffu);
+    int o = gofs[b] + (p - sm.tile_start[b]);
+    if (o >= (b + 1) * cap) continue;  // overflow: reported by k_part_commit
+    dst.o[o] = src.o[s];
+    dst.d[o] = src.d[s];
+    dst.w[o] = src.w[s];
+  }
+}
+
+__global__ void k_part_commit(const uint32_t* __restrict__ scanned, int tiles, int* bin_count, int cap, int* err) {
+  int b = threadIdx.x;
+  if (b >= kDead) return;
+  int total = (int)(scanned[(b + 1) * tiles] - scanned[b * tiles]);
+  int c = bin_count[b] + total;
+  if (c > cap) {
+    atomicOr(err, ERR_BIN_OVERFLOW);
+    c = cap;
+  }
+  bin_count[b] = c;
+}
+
+__global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = cardinal_bin(f3(d[i]));
+}
+
+// ------------------------------------------------------------ ray keys
+// RayBoundingbox (src/core/RayBoundingbox.cpp:5-50): origin box of the batch.
+__global__ void k_origin_box(const float4* __restrict__ o, int n, uint32_t* box6) {
+  float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p = o[i];
+    mn[0] = fminf(mn[0], p.x); mn[1] = fminf(mn[1], p.y); mn[2] = fminf(mn[2], p.z);
+    mx[0] = fmaxf(mx[0], p.x); mx[1] = fmaxf(mx[1], p.y); mx[2] = fmaxf(mx[2], p.z);
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    for (int s = 16; s > 0; s >>= 1) {
+      mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], s));
+      mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], s));
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&box6[a], f2ord(mn[a]));
+      atomicMax(&box6[3 + a], f2ord(mx[a]));
+    }
+}
+
+__global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d, int n,
+                                                 const uint32_t* __restrict__ box6, uint32_t* __restrict__ keys) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 lo = f3(ord2f(box6[0]), ord2f(box6[1]), ord2f(box6[2]));
+  float3 hi = f3(ord2f(box6[3]), ord2f(box6[4]), ord2f(box6[5]));
+  float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+  float3 sc = f3(ex > 0.f ? 64.0f / ex : 0.f, ey > 0.f ? 64.0f / ey : 0.f, ez > 0.f ? 64.0f / ez : 0.f);
+  keys[i] = ray_sort_key(f3(o[i]), f3(d[i]), lo, sc);
+}
+
+// RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
+__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const uint32_t* __restrict__ perm, int n, RayBuf dst) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int i = perm ? (int)perm[j] : j;
+  dst.o[j] = src.o[i];
+  dst.d[j] = src.d[i];
+  dst.w[j] = src.w[i];
+}
+
+// -------------------------------------------------------------- traversal
+__global__ void __launch_bounds__(128) k_trace_closest(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                       const float4* __restrict__ o, const float4* __restrict__ d, int n,
+                                                       float4* __restrict__ hits, int* err) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 ro = o[i], rd = d[i];
+  TriHit h;
+  h.t = MSC_TFAR; h.u = 0.f; h.v = 0.f; h.tri = -1;
+  int ovf = 0;
+  bvh_trace<false>(nodes, tris, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
+  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+  hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+}
+
+// CompareHit key (include/core/RayUncompressed.h:63-69): (geomID, primID) with
+// misses first.  Triangles are numbered geomID-major, so the global triangle
+// index + 1 orders exactly like (geomID, primID), and 0 is a miss.
+__global__ void __launch_bounds__(TB) k_hit_keys(const int* __restrict__ tri_orig, const float4* __restrict__ hits,
+                                                 int n, uint32_t* __restrict__ keys) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int k = __float_as_int(hits[i].w);
+  keys[i] = k < 0 ? 0u : (uint32_t)tri_orig[k] + 1u;
+}
+
+// ------------------------------------------------------------------ shading
+struct BsdfEval {
+  float3 f;
+  float cos_theta;
+  float pdf;
+};
+
+// LambertShader::evaluate (src/core/LambertShader.cpp:27-47), NullShader::evaluate
+// (src/core/NullShader.cpp:25-39) and the Phong extension.
+__device__ __forceinline__ BsdfEval bsdf_evaluate(const ShaderRec& s, float3 wi, float3 wo, float3 n) {
+  BsdfEval e;
+  const float ci = v_dot(n, wi);
+  const float co = v_dot(n, wo);
+  const float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
+  if (s.type == SHADER_NULL) {
+    e.f = f3(0.f, 0.f, 0.f);
+    e.cos_theta = 1.f;
+    e.pdf = 1.f * MSC_INV_PI * 0.5f;
+    return e;
+  }
+  if (s.type == SHADER_PHONG) {
+    const float3 r = v_sub(v_mul(n, 2.f * co), wo);
+    const float ca = fmaxf(0.f, v_dot(r, wi));
+    const float lobe = pow_pos(ca, s.exponent);
+    if (ci < 0.f || co < 0.f) e.f = f3(0.f, 0.f, 0.f);
+    else e.f = v_mul(v_mul(col, s.reflectance), ((s.exponent + 2.f) * MSC_INV_PI * 0.5f) * lobe);
+    e.cos_theta = ci < 0.f ? 0.f : ci;
+    e.pdf = ((s.exponent + 1.f) * MSC_INV_PI * 0.5f) * lobe;
+    return e;
+  }
+  if (ci < 0.f || co < 0.f) e.f = f3(0.f, 0.f, 0.f);
+  else e.f = v_mul(v_mul(col, s.reflectance), MSC_INV_PI);
+  e.cos_theta = ci < 0.f ? 0.f : ci;
+  e.pdf = e.cos_theta * MSC_INV_PI;
+  return e;
+}
+
+// Orthonormal frame around axis a as in LambertShader::sample
+// (src/core/LambertShader.cpp:63-65): tmp = a.x > 0.99 ? Y : X, s = |tmp x a|, t = |a x s|.
+__device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z) {
+  const float3 tmp = a.x > 0.99f ? f3(0.f, 1.f, 0.f) : f3(1.f, 0.f, 0.f);
+  const float3 s = v_normalize(v_cross(tmp, a));
+  const float3 t = v_normalize(v_cross(a, s));
+  return v_add(v_add(v_mul(t, x), v_mul(s, y)), v_mul(a, z));
+}
+
+__device__ __forceinline__ void add_rgb(float4* p, float3 v) {
+  float4 c = *p;
+  c.x += v.x;
+  c.y += v.y;
+  c.z += v.z;
+  *p = c;
+}
+
+// Integrator::operator() (src/core/Integrator.cpp:12-255), one hit per thread.
+__global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf batch, const float4* __restrict__ hits,
+                                              const uint32_t* __restrict__ order, int n, RayBuf next, ShadowBuf sh,
+                                              int* sh_count) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = j < n;
+  bool emit = false, cont = false;
+  float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sd = so, scol = so;
+  float4 no = so, nd = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), nw = so;
+  if (live) {
+    const int i = order ? (int)order[j] : j;
+    const float4 ro = batch.o[i], rd = batch.d[i], rw = batch.w[i], h = hits[i];
+    const int k = __float_as_int(h.w);
+    const int depth = __float_as_int(rd.w);
+    const int sid = __float_as_int(rw.w);
+    const float3 w = f3(rw);
+    if (k >= 0) {  // a miss adds nothing (Integrator.cpp:26-27)
+      const float4 ta = __ldg(&sc.tris[3 * k + 0]);
+      const float4 tb = __ldg(&sc.tris[3 * k + 1]);
+      const float4 tc = __ldg(&sc.tris[3 * k + 2]);
+      const GeomRec g = sc.geoms[__float_as_int(ta.w)];
+      const ShaderRec s = sc.shaders[g.shader];
+      const float3 dn = v_normalize(f3(rd));
+      const float t = h.x;
+      if (s.light >= 0) {
+        // emitter hit: QuadLight::radiance (src/core/QuadLight.cpp:69-84), Integrator.cpp:37-76
+        const LightRec& L = sc.lights[s.light];
+        const float3 ln = f3(L.normal[0], L.normal[1], L.normal[2]);
+        const float cosl = v_dot(ln, v_neg(dn));
+        const float le = cosl < 0.f ? 0.f : L.intensity;
+        const float pdfa = 1.f / (L.scale[0] * L.scale[1]);
+        float mis = 1.0f;
+        if (depth > 0) {
+          const float pdfw = pdfa * (t * t) / fabsf(cosl);
+          mis = mis_weight(ro.w, pdfw * sc.light_pick, f.mis_power);
+        }
+        if (le > MSC_EPSILON) add_rgb(&f.sample_rgb[sid], f3(le * mis * w.x, le * mis * w.y, le * mis * w.z));
+      } else {
+        const float3 nrm = v_normalize(v_cross(f3(tb), f3(tc)));  // = -normalize(Ng) (Integrator.cpp:121-125)
+        const float3 pos = v_add(f3(ro), v_mul(dn, t));
+        const float3 wo = v_neg(dn);
+        const uint4 ra = path_draws((uint32_t)sid, f.iter_seed, (uint32_t)depth + 1u, 0u);
+        // next-event estimation (Integrator.cpp:103-178)
+        if (sc.num_lights > 0) {
+          int li = (int)((float)sc.num_lights * u01(ra.x));
+          if (li >= sc.num_lights) li = sc.num_lights - 1;
+          const LightRec& L = sc.lights[li];
+          // QuadLight::illuminate (src/core/QuadLight.cpp:41-67)
+          const float3 smp = xf_point(L.xf, f3(0.f, u01(ra.y) - 0.5f, u01(ra.z) - 0.5f));
+          const float3 ln = f3(L.normal[0], L.normal[1], L.normal[2]);
+          float cosl = v_dot(v_normalize(v_sub(pos, smp)), ln);
+          const float le = cosl < 0.f ? 0.f : L.intensity;
+          cosl = cosl < 0.f ? 0.f : cosl;
+          const float3 tol = v_sub(smp, pos);
+          const float3 wi = v_normalize(tol);
+          const float dist = v_len(tol);
+          const float pdfw = (v_dot(tol, tol) / cosl) / (L.scale[0] * L.scale[1]);
+          if (le > MSC_EPSILON) {
+            const BsdfEval e = bsdf_evaluate(s, wi, wo, nrm);
+            if (v_maxc(e.f) > MSC_EPSILON) {
+              const float a = pdfw * sc.light_pick;
+              const float mis = mis_weight(a, e.pdf, f.mis_power);
+              const float k0 = (mis * e.cos_theta) / a;
+              const float3 c = f3(k0 * (le * e.f.x), k0 * (le * e.f.y), k0 * (le * e.f.z));
+              emit = true;
+              so = make_float4(pos.x, pos.y, pos.z, dist);
+              sd = make_float4(wi.x, wi.y, wi.z, __int_as_float(sid));
+              scol = make_float4(c.x * w.x, c.y * w.y, c.z * w.z, 0.f);
+            }
+          }
+        }
+        // continuation with Russian roulette (Integrator.cpp:181-246)
+        if (depth < f.max_depth && s.type != SHADER_NULL) {
+          float q = fminf(1.f, s.reflectance / f.threshold);
+          if (depth < f.min_depth) q = 1.f;
+          if (!(u01(ra.w) > q)) {
+            const uint4 rb = path_draws((uint32_t)sid, f.iter_seed, (uint32_t)depth + 1u, 1u);
+            float sp, cp;
+            sincos_turns(u01(rb.x), &sp, &cp);
+            float3 wi;
+            BsdfEval e;
+            bool ok = true;
+            const float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
+            if (s.type == SHADER_PHONG) {
+              // cos(alpha) = xi^(1/(e+1)) around the mirror direction
+              const float ca = pow_pos(u01(rb.y), 1.f / (s.exponent + 1.f));
+              const float sa = sqrtf(fmaxf(0.f, 1.f - ca * ca));
+              const float3 r = v_sub(v_mul(nrm, 2.f * v_dot(nrm, wo)), wo);
+              wi = frame_dir(v_normalize(r), cp * sa, sp * sa, ca);
+              e = bsdf_evaluate(s, wi, wo, nrm);
+              ok = e.cos_theta > 0.f && e.pdf > 0.f;
+            } else {
+              // LambertShader::sample (src/core/LambertShader.cpp:49-73) with
+              // sin(acos(sqrt(xi))) = sqrt(1 - xi) and cos(acos(sqrt(xi))) = sqrt(xi)
+              const float st = sqrtf(1.f - u01(rb.y));
+              const float ct = sqrtf(u01(rb.y));
+              wi = frame_dir(nrm, cp * st, sp * st, ct);
+              e.f = v_mul(v_mul(col, s.reflectance), MSC_INV_PI);
+              e.cos_theta = v_dot(nrm, wi);
+              e.pdf = e.cos_theta * MSC_INV_PI;
+              ok = e.pdf > 0.f;
+            }
+            if (ok) {
+              const float g0 = e.cos_theta / e.pdf;
+              cont = true;
+              no = make_float4(pos.x, pos.y, pos.z, e.pdf);
+              nd = make_float4(wi.x, wi.y, wi.z, __int_as_float(depth + 1));
+              nw = make_float4(((w.x * e.f.x) * g0) / q, ((w.y * e.f.y) * g0) / q, ((w.z * e.f.z) * g0) / q,
+                               __int_as_float(sid));
+            }
+          }
+        }
+      }
+    }
+  }
+  // warp-aggregated append of shadow rays
+  const unsigned m = __ballot_sync(0xffffffffu, emit);
+  if (m) {
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(sh_count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (emit) {
+      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      sh.o[slot] = so;
+      sh.d[slot] = sd;
+      sh.c[slot] = scol;
+    }
+  }
+  if (live) {
+    next.o[j] = no;
+    next.d[j] = cont ? nd : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    next.w[j] = nw;
+  }
+}
+
+// rtcOccluded with mask 0x0FFFFFFF (Integrator.cpp:153-174); an unoccluded
+// shadow ray adds its weighted contribution to its sample.
+__global__ void __launch_bounds__(128) k_trace_shadow(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                      ShadowBuf sh, const int* __restrict__ count, float4* sample_rgb,
+                                                      int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= *count) return;
+  const float4 o = sh.o[i], d = sh.d[i];
+  TriHit h;
+  int ovf = 0;
+  const bool blocked = bvh_trace<true>(nodes, tris, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
+  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+  if (!blocked) add_rgb(&sample_rgb[__float_as_int(d.w)], f3(sh.c[i]));
+}
+
+__global__ void __launch_bounds__(128) k_occluded(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                  const float4* __restrict__ o, const float4* __restrict__ d, int n,
+                                                  int* out, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 ro = o[i], rd = d[i];
+  TriHit h;
+  int ovf = 0;
+  out[i] = bvh_trace<true>(nodes, tris, f3(ro), f3(rd), MSC_TNEAR, ro.w, &h, &ovf) ? 1 : 0;
+  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+}
+
+// ------------------------------------------------------------------ filters
+// TentFilter::convolve (src/core/TentFilter.cpp:5-63): gather over the 3x3
+// neighbour pixels; samples are x-major, pixels row-major.
+__global__ void __launch_bounds__(TB) k_filter_tent(DevFrame f, float* __restrict__ pixels) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= f.width * f.height) return;
+  const int x = idx / f.height, y = idx - x * f.height;
+  const float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
+  float sr = 0.f, sg = 0.f, sb = 0.f, den = 0.f;
+  for (int mx = -1; mx < 2; ++mx) {
+    for (int my = -1; my < 2; ++my) {
+      const int px = x + mx, py = y + my;
+      if (px < 0 || px >= f.width || py < 0 || py >= f.height) continue;
+      const size_t b = ((size_t)px * f.height + py) * f.spp;
+      for (int s = 0; s < f.spp; ++s) {
+        const float2 p = f.sample_pos[b + s];
+        const float4 c = f.sample_rgb[b + s];
+        const float dx = fmaxf(0.f, 1.f - fabsf(p.x - cx));
+        const float dy = fmaxf(0.f, 1.f - fabsf(p.y - cy));
+        const float m = dx * dy;
+        den = den + m;
+        sr += c.x * m;
+        sg += c.y * m;
+        sb += c.z * m;
+      }
+    }
+  }
+  float* px = pixels + 3 * ((size_t)y * f.width + x);
+  px[0] += sr / den;
+  px[1] += sg / den;
+  px[2] += sb / den;
+}
+
+// BoxFilter::convolve (src/core/BoxFilter.cpp:5-37).
+__global__ void __launch_bounds__(TB) k_filter_box(DevFrame f, float* __restrict__ pixels) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= f.width * f.height) return;
+  const int x = idx / f.height, y = idx - x * f.height;
+  const size_t b = ((size_t)x * f.height + y) * f.spp;
+  float sr = 0.f, sg = 0.f, sb = 0.f;
+  for (int s = 0; s < f.spp; ++s) {
+    const float4 c = f.sample_rgb[b + s];
+    sr += c.x;
+    sg += c.y;
+    sb += c.z;
+  }
+  const float ns = (float)f.spp;
+  float* px = pixels + 3 * ((size_t)y * f.width + x);
+  px[0] += sr / ns;
+  px[1] += sg / ns;
+  px[2] += sb / ns;
+}
+
+}  // namespace
+
+int launch_raygen(const DevFrame& f, uint32_t first, int n, RayBuf out, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_raygen<<<grid_for(n), TB, 0, s>>>(f, first, n, out);
+  return 1;
+}
+
+int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const int tiles = (n + kPartTile - 1) / kPartTile;
+  k_part_count<<<tiles, PB, 0, s>>>(src.d, n, pool.tile_counts, tiles);
+  // one extra row (the dead bucket) follows the six bins, so every bin's
+  // total is the difference of two scanned row starts
+  k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * PRADIX, nullptr);
+  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, pool.tile_counts, tiles, pool.rays, pool.cap, pool.count);
+  k_part_commit<<<1, 32, 0, s>>>(pool.tile_counts, tiles, pool.count, pool.cap, pool.err);
+  return 4;
+}
+
+int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_cardinal<<<grid_for(n), TB, 0, s>>>(d, n, out);
+  return 1;
+}
+
+int launch_origin_box(const float4* o, int n, uint32_t* box6, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_origin_box<<<min(grid_for(n), 512), TB, 0, s>>>(o, n, box6);
+  return 1;
+}
+
+int launch_ray_keys(const float4* o, const float4* d, int n, const uint32_t* box6, uint32_t* keys, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_ray_keys<<<grid_for(n), TB, 0, s>>>(o, d, n, box6, keys);
+  return 1;
+}
+
+int launch_gather(const RayBuf& src, const uint32_t* perm, int n, RayBuf dst, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_gather<<<grid_for(n), TB, 0, s>>>(src, perm, n, dst);
+  return 1;
+}
+
+int launch_trace_closest(const DevScene& sc, const float4* o, const float4* d, int n, float4* hits, int* err,
+                         cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_trace_closest<<<grid_for(n, 128), 128, 0, s>>>(sc.nodes, sc.tris, o, d, n, hits, err);
+  return 1;
+}
+
+int launch_hit_keys(const DevScene& sc, const float4* hits, int n, uint32_t* keys, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_hit_keys<<<grid_for(n), TB, 0, s>>>(sc.tri_orig, hits, n, keys);
+  return 1;
+}
+
+int launch_shade(const DevScene& sc, const DevFrame& f, const RayBuf& batch, const float4* hits, const uint32_t* order,
+                 int n, RayBuf next, ShadowBuf sh, int* sh_count, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_shade<<<grid_for(n), TB, 0, s>>>(sc, f, batch, hits, order, n, next, sh, sh_count);
+  return 1;
+}
+
+int launch_trace_shadow(const DevScene& sc, const ShadowBuf& sh, const int* sh_count, int max_n, float4* sample_rgb,
+                        int* err, cudaStream_t s) {
+  if (max_n <= 0) return 0;
+  k_trace_shadow<<<grid_for(max_n, 128), 128, 0, s>>>(sc.nodes, sc.tris, sh, sh_count, sample_rgb, err);
+  return 1;
+}
+
+int launch_occluded(const DevScene& sc, const float4* o, const float4* d, int n, int* occluded, int* err,
+                    cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_occluded<<<grid_for(n, 128), 128, 0, s>>>(sc.nodes, sc.tris, o, d, n, occluded, err);
+  return 1;
+}
+
+int launch_filter(const DevFrame& f, int filter, float* pixels, cudaStream_t s) {
+  const int n = f.width * f.height;
+  if (filter == FILTER_BOX) k_filter_box<<<grid_for(n), TB, 0, s>>>(f, pixels);
+  else k_filter_tent<<<grid_for(n), TB, 0, s>>>(f, pixels);
+  return 1;
+}
+
+}  // namespace mscg

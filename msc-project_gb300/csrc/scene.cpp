@@ -1,0 +1,787 @@
+// Scene input: a YAML subset parser, an OBJ reader with tinyobjloader's
+// semantics, and the assembly of the reference's scene tables.
+// See scene.h for the reference files each part follows.
+#include "scene.h"
+
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <unordered_map>
+#include <sstream>
+
+namespace mscg {
+
+// =============================================================== YAML subset
+
+const YNode* YNode::get(const std::string& key) const {
+  if (kind != Map) return nullptr;
+  for (const auto& kv : map)
+    if (kv.first == key) return &kv.second;
+  return nullptr;
+}
+
+namespace {
+
+struct YLine {
+  int indent;
+  std::string text;  // without indentation and comments
+  int lineno;
+};
+
+std::string rtrim(const std::string& s) {
+  size_t e = s.size();
+  while (e > 0 && (s[e - 1] == ' ' || s[e - 1] == '\t' || s[e - 1] == '\r')) --e;
+  return s.substr(0, e);
+}
+
+std::string trim(const std::string& s) {
+  size_t b = 0;
+  while (b < s.size() && (s[b] == ' ' || s[b] == '\t')) ++b;
+  return rtrim(s.substr(b));
+}
+
+// Removes a '#' comment that is not inside quotes.
+std::string strip_comment(const std::string& s) {
+  bool sq = false, dq = false;
+  for (size_t i = 0; i < s.size(); ++i) {
+    char c = s[i];
+    if (c == '\'' && !dq) sq = !sq;
+    else if (c == '"' && !sq) dq = !dq;
+    else if (c == '#' && !sq && !dq && (i == 0 || s[i - 1] == ' ' || s[i - 1] == '\t')) return s.substr(0, i);
+  }
+  return s;
+}
+
+std::string unquote(const std::string& s) {
+  if (s.size() >= 2 && ((s.front() == '"' && s.back() == '"') || (s.front() == '\'' && s.back() == '\'')))
+    return s.substr(1, s.size() - 2);
+  return s;
+}
+
+// Position of the "key: " separator of a block mapping line, or npos.
+size_t find_map_colon(const std::string& s) {
+  bool sq = false, dq = false;
+  int depth = 0;
+  for (size_t i = 0; i < s.size(); ++i) {
+    char c = s[i];
+    if (c == '\'' && !dq) sq = !sq;
+    else if (c == '"' && !sq) dq = !dq;
+    else if (!sq && !dq) {
+      if (c == '[' || c == '{') ++depth;
+      else if (c == ']' || c == '}') --depth;
+      else if (c == ':' && depth == 0 && (i + 1 == s.size() || s[i + 1] == ' ' || s[i + 1] == '\t')) return i;
+    }
+  }
+  return std::string::npos;
+}
+
+struct FlowParser {
+  const std::string& s;
+  size_t p = 0;
+  std::string err;
+  explicit FlowParser(const std::string& str) : s(str) {}
+  void ws() { while (p < s.size() && (s[p] == ' ' || s[p] == '\t')) ++p; }
+  bool parse(YNode* out) {
+    ws();
+    if (p >= s.size()) { out->kind = YNode::Null; return true; }
+    if (s[p] == '[') {
+      ++p;
+      out->kind = YNode::Seq;
+      ws();
+      if (p < s.size() && s[p] == ']') { ++p; return true; }
+      while (true) {
+        YNode item;
+        if (!parse(&item)) return false;
+        out->seq.push_back(item);
+        ws();
+        if (p < s.size() && s[p] == ',') { ++p; continue; }
+        if (p < s.size() && s[p] == ']') { ++p; return true; }
+        err = "unterminated flow sequence";
+        return false;
+      }
+    }
+    if (s[p] == '{') {
+      ++p;
+      out->kind = YNode::Map;
+      ws();
+      if (p < s.size() && s[p] == '}') { ++p; return true; }
+      while (true) {
+        ws();
+        size_t k0 = p;
+        while (p < s.size() && s[p] != ':' && s[p] != ',' && s[p] != '}') ++p;
+        if (p >= s.size() || s[p] != ':') { err = "bad flow mapping"; return false; }
+        std::string key = unquote(trim(s.substr(k0, p - k0)));
+        ++p;
+        YNode val;
+        if (!parse(&val)) return false;
+        out->map.emplace_back(key, val);
+        ws();
+        if (p < s.size() && s[p] == ',') { ++p; continue; }
+        if (p < s.size() && s[p] == '}') { ++p; return true; }
+        err = "unterminated flow mapping";
+        return false;
+      }
+    }
+    size_t b = p;
+    bool sq = false, dq = false;
+    while (p < s.size()) {
+      char c = s[p];
+      if (c == '\'' && !dq) sq = !sq;
+      else if (c == '"' && !sq) dq = !dq;
+      else if (!sq && !dq && (c == ',' || c == ']' || c == '}')) break;
+      ++p;
+    }
+    out->kind = YNode::Scalar;
+    out->scalar = unquote(trim(s.substr(b, p - b)));
+    return true;
+  }
+};
+
+bool parse_inline_value(const std::string& text, YNode* out, std::string* err) {
+  std::string t = trim(text);
+  if (t.empty()) { out->kind = YNode::Null; return true; }
+  if (t[0] == '[' || t[0] == '{') {
+    FlowParser fp(t);
+    if (!fp.parse(out)) { *err = fp.err; return false; }
+    fp.ws();
+    if (fp.p != t.size()) { *err = "trailing characters after flow collection"; return false; }
+    return true;
+  }
+  out->kind = YNode::Scalar;
+  out->scalar = unquote(t);
+  return true;
+}
+
+bool parse_block(const std::vector<YLine>& lines, size_t* i, int indent, YNode* out, std::string* err);
+
+// Parses the value that follows "key:" (inline text or a nested block).
+bool parse_after_key(const std::vector<YLine>& lines, size_t* i, int indent, const std::string& rest,
+                     YNode* out, std::string* err) {
+  if (!trim(rest).empty()) return parse_inline_value(rest, out, err);
+  if (*i < lines.size() && (lines[*i].indent > indent ||
+                            (lines[*i].indent == indent && lines[*i].text.rfind("- ", 0) == 0)))
+    return parse_block(lines, i, lines[*i].indent, out, err);
+  out->kind = YNode::Null;
+  return true;
+}
+
+bool parse_block(const std::vector<YLine>& lines, size_t* i, int indent, YNode* out, std::string* err) {
+  if (*i >= lines.size()) { out->kind = YNode::Null; return true; }
+  bool is_seq = lines[*i].text == "-" || lines[*i].text.rfind("- ", 0) == 0;
+  out->kind = is_seq ? YNode::Seq : YNode::Map;
+  while (*i < lines.size() && lines[*i].indent == indent) {
+    const YLine& ln = lines[*i];
+    if (is_seq) {
+      if (!(ln.text == "-" || ln.text.rfind("- ", 0) == 0)) break;
+      std::string rest = ln.text.size() > 1 ? ln.text.substr(2) : std::string();
+      ++*i;
+      YNode item;
+      size_t colon = find_map_colon(trim(rest));
+      if (!trim(rest).empty() && colon != std::string::npos && trim(rest)[0] != '[' && trim(rest)[0] != '{') {
+        // "- key: value" starts a mapping whose further keys sit at indent + 2
+        std::vector<YLine> sub;
+        YLine first{indent + 2, trim(rest), ln.lineno};
+        sub.push_back(first);
+        size_t j = *i;
+        while (j < lines.size() && lines[j].indent > indent) sub.push_back(lines[j++]);
+        size_t k = 0;
+        if (!parse_block(sub, &k, indent + 2, &item, err)) return false;
+        *i = j;
+      } else if (trim(rest).empty()) {
+        if (*i < lines.size() && lines[*i].indent > indent) {
+          if (!parse_block(lines, i, lines[*i].indent, &item, err)) return false;
+        }
+      } else if (!parse_inline_value(rest, &item, err)) {
+        return false;
+      }
+      out->seq.push_back(item);
+    } else {
+      size_t colon = find_map_colon(ln.text);
+      if (colon == std::string::npos) {
+        *err = "line " + std::to_string(ln.lineno) + ": expected 'key: value'";
+        return false;
+      }
+      std::string key = unquote(trim(ln.text.substr(0, colon)));
+      std::string rest = ln.text.substr(colon + 1);
+      ++*i;
+      YNode val;
+      if (!parse_after_key(lines, i, indent, rest, &val, err)) return false;
+      out->map.emplace_back(key, val);
+    }
+  }
+  if (*i < lines.size() && lines[*i].indent > indent) {
+    *err = "line " + std::to_string(lines[*i].lineno) + ": bad indentation";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+bool yaml_parse_documents(const std::string& text, std::vector<YNode>* docs, std::string* err) {
+  docs->clear();
+  std::vector<std::vector<YLine>> groups(1);
+  std::istringstream in(text);
+  std::string raw;
+  int lineno = 0;
+  bool any_content = false;
+  while (std::getline(in, raw)) {
+    ++lineno;
+    std::string s = rtrim(strip_comment(raw));
+    std::string t = trim(s);
+    if (t == "---" || t.rfind("--- ", 0) == 0) {
+      if (any_content || !groups.back().empty()) groups.emplace_back();
+      any_content = true;
+      continue;
+    }
+    if (t == "...") continue;
+    if (t.empty()) continue;
+    if (!s.empty() && s[0] == '%') continue;  // directives
+    int ind = 0;
+    while (ind < (int)s.size() && s[ind] == ' ') ++ind;
+    if (ind < (int)s.size() && s[ind] == '\t') {
+      *err = "line " + std::to_string(lineno) + ": tab indentation";
+      return false;
+    }
+    groups.back().push_back(YLine{ind, t, lineno});
+    any_content = true;
+  }
+  for (auto& g : groups) {
+    YNode doc;
+    if (!g.empty()) {
+      size_t i = 0;
+      if (!parse_block(g, &i, g[0].indent, &doc, err)) return false;
+      if (i != g.size()) {
+        *err = "line " + std::to_string(g[i].lineno) + ": unexpected content";
+        return false;
+      }
+    }
+    docs->push_back(doc);
+  }
+  while (!docs->empty() && docs->back().kind == YNode::Null) docs->pop_back();
+  return true;
+}
+
+// ================================================================ OBJ reader
+
+// tryParseDouble's grammar and arithmetic (tiny_obj_loader.cpp:131-242):
+// integer digits accumulate as m = m*10 + d, fraction digits add d*10^-k,
+// and the result is sign * ldexp(m * 5^e, e).  A malformed number yields 0.
+double obj_parse_number(const char* s, const char* end) {
+  if (s >= end) return 0.0;
+  double mantissa = 0.0;
+  int exponent = 0;
+  char sign = '+', exp_sign = '+';
+  const char* c = s;
+  int read = 0;
+  bool more = false;
+  if (*c == '+' || *c == '-') { sign = *c; ++c; }
+  else if (!isdigit((unsigned char)*c)) return 0.0;
+  while ((more = (c != end)) && isdigit((unsigned char)*c)) {
+    mantissa *= 10;
+    mantissa += (int)(*c - '0');
+    ++c; ++read;
+  }
+  if (read == 0) return 0.0;
+  if (!more) goto assemble;
+  if (*c == '.') {
+    ++c;
+    read = 1;
+    while ((more = (c != end)) && isdigit((unsigned char)*c)) {
+      mantissa += (int)(*c - '0') * pow(10.0, -read);
+      ++read; ++c;
+    }
+  } else if (*c == 'e' || *c == 'E') {
+  } else {
+    goto assemble;
+  }
+  if (!more) goto assemble;
+  if (*c == 'e' || *c == 'E') {
+    ++c;
+    if ((more = (c != end)) && (*c == '+' || *c == '-')) { exp_sign = *c; ++c; }
+    else if (isdigit((unsigned char)*c)) {}
+    else return 0.0;
+    read = 0;
+    while ((more = (c != end)) && isdigit((unsigned char)*c)) {
+      exponent *= 10;
+      exponent += (int)(*c - '0');
+      ++c; ++read;
+    }
+    exponent *= (exp_sign == '+' ? 1 : -1);
+    if (read == 0) return 0.0;
+  }
+assemble:
+  return (sign == '+' ? 1 : -1) * ldexp(mantissa * pow(5.0, exponent), exponent);
+}
+
+namespace {
+
+struct VIdx { int v, vt, vn; };
+// tinyobj keys its vertex cache on the (v, vt, vn) triple (tiny_obj_loader.cpp:58-67);
+// only equality matters for the output, so a hash map gives the same result.
+struct VIdxHash {
+  size_t operator()(const VIdx& a) const {
+    uint64_t h = (uint64_t)(uint32_t)a.v * 0x9e3779b97f4a7c15ull;
+    h ^= (uint64_t)(uint32_t)a.vt * 0xc2b2ae3d27d4eb4full + (h << 6) + (h >> 2);
+    h ^= (uint64_t)(uint32_t)a.vn * 0x165667b19e3779f9ull + (h << 6) + (h >> 2);
+    return (size_t)h;
+  }
+};
+struct VIdxEq {
+  bool operator()(const VIdx& a, const VIdx& b) const { return a.v == b.v && a.vt == b.vt && a.vn == b.vn; }
+};
+
+inline bool is_sp(char c) { return c == ' ' || c == '\t'; }
+inline bool is_nl(char c) { return c == '\r' || c == '\n' || c == '\0'; }
+inline int fix_index(int idx, int n) { return idx > 0 ? idx - 1 : (idx == 0 ? 0 : n + idx); }
+
+float next_float(const char*& tok) {
+  tok += strspn(tok, " \t");
+  const char* e = tok + strcspn(tok, " \t\r");
+  float f = (float)obj_parse_number(tok, e);
+  tok = e;
+  return f;
+}
+
+VIdx parse_triple(const char*& tok, int nv, int nvn, int nvt) {
+  VIdx vi{-1, -1, -1};
+  vi.v = fix_index(atoi(tok), nv);
+  tok += strcspn(tok, "/ \t\r");
+  if (tok[0] != '/') return vi;
+  ++tok;
+  if (tok[0] == '/') {
+    ++tok;
+    vi.vn = fix_index(atoi(tok), nvn);
+    tok += strcspn(tok, "/ \t\r");
+    return vi;
+  }
+  vi.vt = fix_index(atoi(tok), nvt);
+  tok += strcspn(tok, "/ \t\r");
+  if (tok[0] != '/') return vi;
+  ++tok;
+  vi.vn = fix_index(atoi(tok), nvn);
+  tok += strcspn(tok, "/ \t\r");
+  return vi;
+}
+
+}  // namespace
+
+bool obj_load_text(const char* text, size_t len, ObjMesh* out) {
+  std::vector<float> v, vn, vt;
+  std::vector<std::vector<VIdx>> faces;
+  std::string line;
+  size_t pos = 0;
+  while (pos < len) {
+    size_t e = pos;
+    while (e < len && text[e] != '\n') ++e;
+    line.assign(text + pos, e - pos);
+    pos = e + 1;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.size() > 8191) line.resize(8191);  // tinyobj reads lines into an 8192-byte buffer
+    if (line.empty()) continue;
+    const char* tok = line.c_str();
+    tok += strspn(tok, " \t");
+    if (tok[0] == '\0' || tok[0] == '#') continue;
+    if (tok[0] == 'v' && is_sp(tok[1])) {
+      tok += 2;
+      float x = next_float(tok), y = next_float(tok), z = next_float(tok);
+      v.push_back(x); v.push_back(y); v.push_back(z);
+      continue;
+    }
+    if (tok[0] == 'v' && tok[1] == 'n' && is_sp(tok[2])) {
+      tok += 3;
+      float x = next_float(tok), y = next_float(tok), z = next_float(tok);
+      vn.push_back(x); vn.push_back(y); vn.push_back(z);
+      continue;
+    }
+    if (tok[0] == 'v' && tok[1] == 't' && is_sp(tok[2])) {
+      tok += 3;
+      float x = next_float(tok), y = next_float(tok);
+      vt.push_back(x); vt.push_back(y);
+      continue;
+    }
+    if (tok[0] == 'f' && is_sp(tok[1])) {
+      tok += 2;
+      tok += strspn(tok, " \t");
+      std::vector<VIdx> face;
+      while (!is_nl(tok[0])) {
+        face.push_back(parse_triple(tok, (int)(v.size() / 3), (int)(vn.size() / 3), (int)(vt.size() / 2)));
+        tok += strspn(tok, " \t\r");
+      }
+      faces.push_back(std::move(face));
+      continue;
+    }
+  }
+  // exportFaceGroupToShape (tiny_obj_loader.cpp:366-412): fan triangulation,
+  // one vertex per distinct (v, vt, vn) triple in first-use order.
+  out->positions.clear(); out->normals.clear(); out->texcoords.clear(); out->indices.clear();
+  std::unordered_map<VIdx, uint32_t, VIdxHash, VIdxEq> cache;
+  cache.reserve(v.size() / 3 + 16);
+  auto vertex = [&](const VIdx& i) -> uint32_t {
+    auto it = cache.find(i);
+    if (it != cache.end()) return it->second;
+    if (i.v < 0 || (size_t)(3 * i.v + 2) >= v.size()) return UINT32_MAX;
+    out->positions.push_back(v[3 * i.v + 0]);
+    out->positions.push_back(v[3 * i.v + 1]);
+    out->positions.push_back(v[3 * i.v + 2]);
+    if (i.vn >= 0 && (size_t)(3 * i.vn + 2) < vn.size()) {
+      out->normals.push_back(vn[3 * i.vn + 0]);
+      out->normals.push_back(vn[3 * i.vn + 1]);
+      out->normals.push_back(vn[3 * i.vn + 2]);
+    }
+    if (i.vt >= 0 && (size_t)(2 * i.vt + 1) < vt.size()) {
+      out->texcoords.push_back(vt[2 * i.vt + 0]);
+      out->texcoords.push_back(vt[2 * i.vt + 1]);
+    }
+    uint32_t idx = (uint32_t)(out->positions.size() / 3 - 1);
+    cache[i] = idx;
+    return idx;
+  };
+  for (const auto& f : faces) {
+    if (f.size() < 3) continue;
+    VIdx i0 = f[0], i2 = f[1], i1;
+    for (size_t k = 2; k < f.size(); ++k) {
+      i1 = i2;
+      i2 = f[k];
+      uint32_t a = vertex(i0), b = vertex(i1), c = vertex(i2);
+      if (a == UINT32_MAX || b == UINT32_MAX || c == UINT32_MAX) return false;
+      out->indices.push_back(a);
+      out->indices.push_back(b);
+      out->indices.push_back(c);
+    }
+  }
+  return true;
+}
+
+bool obj_load_file(const std::string& path, ObjMesh* out, std::string* err) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) { *err = "cannot open OBJ file [" + path + "]"; return false; }
+  std::string s((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  if (!obj_load_text(s.data(), s.size(), out)) { *err = "OBJ face references a missing vertex in [" + path + "]"; return false; }
+  return true;
+}
+
+// ================================================================ transforms
+
+namespace {
+struct M3 { float a[3][3]; };
+M3 m3_mul(const M3& x, const M3& y) {
+  M3 r;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) r.a[i][j] = (x.a[i][0] * y.a[0][j] + x.a[i][1] * y.a[1][j]) + x.a[i][2] * y.a[2][j];
+  return r;
+}
+M3 rot_axis(int axis, float deg) {
+  float ang = deg * MSC_PI_180;
+  float c = std::cos(ang), s = std::sin(ang);
+  M3 r = {{{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}};
+  int u = (axis + 1) % 3, v = (axis + 2) % 3;
+  r.a[u][u] = c; r.a[u][v] = -s;
+  r.a[v][u] = s; r.a[v][v] = c;
+  return r;
+}
+Affine3 to_affine(const M3& l, const float t[3]) {
+  Affine3 a;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) a.m[i][j] = l.a[i][j];
+    a.m[i][3] = t[i];
+  }
+  return a;
+}
+}  // namespace
+
+Affine3 make_trs_xyz(const float t[3], const float r_deg[3], const float s[3]) {
+  M3 l = m3_mul(m3_mul(rot_axis(0, r_deg[0]), rot_axis(1, r_deg[1])), rot_axis(2, r_deg[2]));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) l.a[i][j] = l.a[i][j] * s[j];
+  return to_affine(l, t);
+}
+
+Affine3 make_tr_yxz(const float t[3], const float r_deg[3]) {
+  M3 l = m3_mul(m3_mul(rot_axis(1, r_deg[1]), rot_axis(0, r_deg[0])), rot_axis(2, r_deg[2]));
+  return to_affine(l, t);
+}
+
+// normalize(L^-T X): the first column of the cofactor matrix, signed by det(L).
+void normal_of_x_axis(const Affine3& a, float out[3]) {
+  const float(*L)[4] = a.m;
+  float c0 = L[1][1] * L[2][2] - L[1][2] * L[2][1];
+  float c1 = -(L[0][1] * L[2][2] - L[0][2] * L[2][1]);
+  float c2 = L[0][1] * L[1][2] - L[0][2] * L[1][1];
+  float det = (L[0][0] * c0 + L[1][0] * c1) + L[2][0] * c2;
+  if (det < 0.f) { c0 = -c0; c1 = -c1; c2 = -c2; }
+  float inv = 1.0f / std::sqrt((c0 * c0 + c1 * c1) + c2 * c2);
+  out[0] = c0 * inv; out[1] = c1 * inv; out[2] = c2 * inv;
+}
+
+static void xf_host_point(const Affine3& a, const float p[3], float out[3]) {
+  for (int i = 0; i < 3; ++i) out[i] = ((a.m[i][0] * p[0] + a.m[i][1] * p[1]) + a.m[i][2] * p[2]) + a.m[i][3];
+}
+
+// ============================================================ scene assembly
+
+namespace {
+
+bool as_float(const YNode* n, float* out) {
+  if (!n || n->kind != YNode::Scalar) return false;
+  const char* s = n->scalar.c_str();
+  char* e = nullptr;
+  float v = strtof(s, &e);
+  if (e == s) return false;
+  while (*e == ' ') ++e;
+  if (*e != '\0') return false;
+  *out = v;
+  return true;
+}
+bool as_int(const YNode* n, int* out) {
+  if (!n || n->kind != YNode::Scalar) return false;
+  const char* s = n->scalar.c_str();
+  char* e = nullptr;
+  long v = strtol(s, &e, 10);
+  if (e == s) return false;
+  while (*e == ' ') ++e;
+  if (*e != '\0') return false;
+  *out = (int)v;
+  return true;
+}
+bool as_vec(const YNode* n, int k, float* out) {
+  if (!n || n->kind != YNode::Seq || (int)n->seq.size() != k) return false;
+  for (int i = 0; i < k; ++i)
+    if (!as_float(&n->seq[i], &out[i])) return false;
+  return true;
+}
+std::string as_str(const YNode* n) { return (n && n->kind == YNode::Scalar) ? n->scalar : std::string(); }
+
+struct Ctx {
+  std::string* err;
+  bool fail(const std::string& m) { *err = m; return false; }
+};
+
+bool decode_texture(const YNode* n, ShaderRec* sh, Ctx& c) {
+  std::string ty = as_str(n ? n->get("type") : nullptr);
+  if (ty == "Constant") {  // include/core/ConstantTexture.h:74-85
+    if (n->size() != 2 || !as_vec(n->get("colour"), 3, sh->colour)) return c.fail("bad Constant texture");
+    return true;
+  }
+  if (ty == "Standard" || ty == "Layered")
+    return c.fail("texture type '" + ty + "' needs an image reader that this build does not have yet");
+  return c.fail("unknown texture type '" + ty + "'");
+}
+
+}  // namespace
+
+bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) {
+  std::ifstream f(yaml_path, std::ios::binary);
+  if (!f) { *err = "cannot open scene file [" + yaml_path + "]"; return false; }
+  std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  std::vector<YNode> docs;
+  if (!yaml_parse_documents(text, &docs, err)) return false;
+  Ctx c{err};
+  if (docs.size() < 2) return c.fail("scene file needs a setup document and a scene document");
+  std::string dir = ".";
+  size_t slash = yaml_path.find_last_of('/');
+  if (slash != std::string::npos) dir = yaml_path.substr(0, slash);
+  *out = SceneDesc();
+  SceneDesc& S = *out;
+  const YNode& setup = docs[0];
+  const YNode& scene = docs[1];
+
+  // camera default: ThinLens with the default constructor's values
+  {
+    float t[3] = {0, 0, 0}, r[3] = {0, 0, 0};
+    S.camera.type = CAMERA_THINLENS;
+    S.camera.xf = make_tr_yxz(t, r);
+    normal_of_x_axis(S.camera.xf, S.camera.normal);
+    for (int i = 0; i < 3; ++i) S.camera.translation[i] = 0;
+    S.camera.focal_length = 55.f;
+    S.camera.aperture = 5.6f;
+    S.camera.focal_distance = 1000.f;
+  }
+  if (const YNode* n = setup.get("image")) {  // Image.h:56-69
+    if (n->kind != YNode::Map || n->size() != 3 || !as_int(n->get("width"), &S.width) ||
+        !as_int(n->get("height"), &S.height) || !as_int(n->get("sample base"), &S.base))
+      return c.fail("bad image block (needs width, height, sample base)");
+    if (S.width <= 0 || S.height <= 0 || S.base <= 0) return c.fail("image sizes must be positive");
+  }
+  if (const YNode* n = setup.get("settings")) {  // Settings.h:30-45
+    Settings& st = S.settings;
+    if (n->kind != YNode::Map || n->size() != 6 || !as_int(n->get("min depth"), &st.min_depth) ||
+        !as_int(n->get("max depth"), &st.max_depth) || !as_float(n->get("threshold"), &st.threshold) ||
+        !as_int(n->get("bucket size"), &st.bucket_size) || !as_int(n->get("shading size"), &st.shading_size) ||
+        !as_int(n->get("bin exponent"), &st.bin_exponent))
+      return c.fail("bad settings block");
+    if (st.bin_exponent < 6 || st.bin_exponent > 26) return c.fail("bin exponent must lie in [6, 26]");
+  }
+  if (const YNode* n = setup.get("camera")) {
+    std::string ty = as_str(n->get("type"));
+    float t[3], r[3];
+    if (ty == "PinHole") {  // PinHoleCamera.h:98-113
+      if (n->size() != 4 || !as_vec(n->get("translation"), 3, t) || !as_vec(n->get("rotation"), 3, r) ||
+          !as_float(n->get("focal length"), &S.camera.focal_length))
+        return c.fail("bad PinHole camera");
+      S.camera.type = CAMERA_PINHOLE;
+    } else if (ty == "ThinLens") {  // ThinLensCamera.h:132-149
+      if (n->size() != 6 || !as_vec(n->get("translation"), 3, t) || !as_vec(n->get("rotation"), 3, r) ||
+          !as_float(n->get("focal length"), &S.camera.focal_length) ||
+          !as_float(n->get("focal distance"), &S.camera.focal_distance) ||
+          !as_float(n->get("aperture"), &S.camera.aperture))
+        return c.fail("bad ThinLens camera");
+      S.camera.type = CAMERA_THINLENS;
+    } else {
+      return c.fail("unknown camera type '" + ty + "'");
+    }
+    S.camera.xf = make_tr_yxz(t, r);
+    normal_of_x_axis(S.camera.xf, S.camera.normal);
+    for (int i = 0; i < 3; ++i) S.camera.translation[i] = t[i];
+  }
+  if (const YNode* n = setup.get("filter")) {
+    std::string ty = as_str(n->get("type"));
+    if (n->size() != 1) return c.fail("bad filter block");
+    if (ty == "Tent") S.filter = FILTER_TENT;
+    else if (ty == "Box") S.filter = FILTER_BOX;
+    else return c.fail("unknown filter type '" + ty + "'");
+  }
+  if (const YNode* n = setup.get("sampler")) {
+    std::string ty = as_str(n->get("type"));
+    if (n->size() != 1) return c.fail("bad sampler block");
+    if (ty == "Stratified") S.sampler = SAMPLER_STRATIFIED;
+    else if (ty == "Independent") S.sampler = SAMPLER_INDEPENDENT;
+    else if (ty == "Grid") S.sampler = SAMPLER_GRID;
+    else return c.fail("unknown sampler type '" + ty + "'");
+  }
+  if (docs.size() >= 3) {
+    const YNode* e = docs[2].get("extensions");
+    if (e) {
+      for (const auto& kv : e->map) {
+        int iv = 0;
+        if (kv.first == "samples per pixel") { if (!as_int(&kv.second, &S.ext.spp) || S.ext.spp <= 0) return c.fail("bad samples per pixel"); }
+        else if (kv.first == "mis") {
+          std::string m = as_str(&kv.second);
+          if (m == "power") S.ext.mis_power = 1;
+          else if (m == "balance") S.ext.mis_power = 0;
+          else return c.fail("mis must be power or balance");
+        }
+        else if (kv.first == "ray sort") { if (!as_int(&kv.second, &S.ext.ray_sort)) return c.fail("bad ray sort"); }
+        else if (kv.first == "hit sort") { if (!as_int(&kv.second, &S.ext.hit_sort)) return c.fail("bad hit sort"); }
+        else if (kv.first == "seed") { if (!as_int(&kv.second, &iv)) return c.fail("bad seed"); S.ext.seed = (uint32_t)iv; }
+        else if (kv.first == "paths per generation") { if (!as_int(&kv.second, &S.ext.generation) || S.ext.generation < 0) return c.fail("bad paths per generation"); }
+        else return c.fail("unknown extension '" + kv.first + "'");
+      }
+    }
+  }
+
+  auto add_tris = [&](const std::vector<float>& pos3, const std::vector<uint32_t>& idx, const std::vector<float>& uv,
+                      int geom, bool light) {
+    size_t nt = idx.size() / 3;
+    for (size_t t = 0; t < nt; ++t) {
+      for (int k = 0; k < 3; ++k) {
+        uint32_t vi = idx[3 * t + k];
+        for (int a = 0; a < 3; ++a) S.tri_v.push_back(pos3[3 * vi + a]);
+        bool has_uv = (size_t)(2 * vi + 1) < uv.size();
+        S.tri_uv.push_back(has_uv ? uv[2 * vi + 0] : 0.f);
+        S.tri_uv.push_back(has_uv ? uv[2 * vi + 1] : 0.f);
+      }
+      S.tri_geom.push_back(geom);
+      S.tri_is_light.push_back(light ? 1 : 0);
+    }
+  };
+
+  if (scene.kind != YNode::Map && scene.kind != YNode::Null) return c.fail("scene document must be a mapping");
+  // First pass: objects and shaders in document order (Pathtracer.cpp:166-217).
+  for (const auto& kv : scene.map) {
+    const YNode& n = kv.second;
+    if (kv.first == "object") {
+      std::string ty = as_str(n.get("type"));
+      if (ty != "Polygon") continue;
+      float t[3], r[3], s[3];
+      int shader = 0;
+      std::string fname = as_str(n.get("filename"));
+      if (n.size() != 6 || fname.empty() || !as_vec(n.get("translation"), 3, t) || !as_vec(n.get("rotation"), 3, r) ||
+          !as_vec(n.get("scale"), 3, s) || !as_int(n.get("shader"), &shader))
+        return c.fail("bad Polygon object");
+      ObjMesh mesh;
+      if (!obj_load_file(dir + "/" + fname, &mesh, err)) return false;
+      Affine3 xf = make_trs_xyz(t, r, s);  // PolygonObject.cpp:17-22
+      std::vector<float> pos(mesh.positions.size());
+      for (size_t i = 0; i + 2 < mesh.positions.size(); i += 3) xf_host_point(xf, &mesh.positions[i], &pos[i]);
+      GeomRec g;
+      g.shader = shader;
+      g.first_prim = (int)S.tri_geom.size();
+      g.prim_count = (int)(mesh.indices.size() / 3);
+      g.light = -1;
+      S.geoms.push_back(g);
+      add_tris(pos, mesh.indices, mesh.texcoords, (int)S.geoms.size() - 1, false);
+    } else if (kv.first == "shader") {
+      std::string ty = as_str(n.get("type"));
+      ShaderRec sh;
+      memset(&sh, 0, sizeof(sh));
+      sh.light = -1;
+      if (ty == "Lambert") {  // LambertShader.h:140-174
+        sh.type = SHADER_LAMBERT;
+        if (n.size() != 3 || !as_float(n.get("reflectance"), &sh.reflectance)) return c.fail("bad Lambert shader");
+        if (!decode_texture(n.get("texture"), &sh, c)) return false;
+      } else if (ty == "Phong") {  // extension: modified Phong lobe
+        sh.type = SHADER_PHONG;
+        if (n.size() != 4 || !as_float(n.get("reflectance"), &sh.reflectance) ||
+            !as_float(n.get("exponent"), &sh.exponent) || sh.exponent < 0.f)
+          return c.fail("bad Phong shader");
+        if (!decode_texture(n.get("texture"), &sh, c)) return false;
+      } else {
+        continue;
+      }
+      S.shaders.push_back(sh);
+    }
+  }
+  // Second pass: lights (Pathtracer.cpp:219-272).  Each adds a Null shader,
+  // an empty object pointing at it, and the emitter triangles.
+  for (const auto& kv : scene.map) {
+    if (kv.first != "light") continue;
+    const YNode& n = kv.second;
+    std::string ty = as_str(n.get("type"));
+    if (ty != "Quad") continue;
+    LightRec L;
+    memset(&L, 0, sizeof(L));
+    L.type = LIGHT_QUAD;
+    float t[3], r[3];
+    if (n.size() != 5 || !as_vec(n.get("translation"), 3, t) || !as_vec(n.get("rotation"), 3, r) ||
+        !as_vec(n.get("scale"), 2, L.scale) || !as_float(n.get("intensity"), &L.intensity))
+      return c.fail("bad Quad light");
+    float s3[3] = {1.f, L.scale[0], L.scale[1]};
+    L.xf = make_trs_xyz(t, r, s3);
+    normal_of_x_axis(L.xf, L.normal);
+    int light_id = (int)S.lights.size();
+    int shader_id = (int)S.shaders.size();
+    ShaderRec ns;
+    memset(&ns, 0, sizeof(ns));
+    ns.type = SHADER_NULL;
+    ns.light = light_id;
+    ns.reflectance = 1.f;
+    S.shaders.push_back(ns);
+    GeomRec g;
+    g.shader = shader_id;
+    g.first_prim = (int)S.tri_geom.size();
+    g.prim_count = 2;
+    g.light = light_id;
+    S.geoms.push_back(g);
+    S.lights.push_back(L);
+    // unit quad in the local YZ plane (QuadLight.cpp:7-21)
+    const float quad[6][3] = {{0.f, -0.5f, -0.5f}, {0.f, 0.5f, -0.5f}, {0.f, 0.5f, 0.5f},
+                              {0.f, 0.5f, 0.5f},   {0.f, -0.5f, 0.5f}, {0.f, -0.5f, -0.5f}};
+    std::vector<float> pos(18);
+    for (int i = 0; i < 6; ++i) xf_host_point(L.xf, quad[i], &pos[3 * i]);
+    std::vector<uint32_t> idx = {0, 1, 2, 3, 4, 5};
+    add_tris(pos, idx, std::vector<float>(), (int)S.geoms.size() - 1, true);
+  }
+  for (size_t g = 0; g < S.geoms.size(); ++g) {
+    int sh = S.geoms[g].shader;
+    if (sh < 0 || sh >= (int)S.shaders.size())
+      return c.fail("object " + std::to_string(g) + " names shader " + std::to_string(sh) + " which does not exist");
+  }
+  return true;
+}
+
+}  // namespace mscg

@@ -1,0 +1,135 @@
+// Binary LBVH layout and the stack-in-registers traversal used for both the
+// closest-hit query (replacing rtcIntersect, src/core/RayIntersect.cpp:7-12)
+// and the occlusion query (replacing rtcOccluded with the light mask
+// 0x0FFFFFFF, src/core/Integrator.cpp:153-174).
+//
+// Node i (internal) = 4 float4:
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (child0, child1, 0, 0) as ints; a child >= 0 is an internal node,
+//        a child < 0 is the leaf ~k holding triangle k (in leaf order).
+// Triangle k = 3 float4: (v0, geomID), (e1 = v1 - v0, is_light), (e2 = v2 - v0, global prim).
+#pragma once
+
+#include "dmath.h"
+
+namespace mscg {
+
+constexpr int kTraceStack = 64;
+constexpr int kTraceStepCap = 1 << 22;
+
+struct TriHit {
+  float t, u, v;
+  int tri;  // leaf-order triangle index, -1 for a miss
+};
+
+// Moller-Trumbore with u, v the weights of v1 and v2 (the barycentric
+// convention PolygonObject::texture relies on, src/core/PolygonObject.cpp:45-63).
+// Accepts tmin < t < tmax.
+__device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float tmin,
+                                              float tmax, float* t_out, float* u_out, float* v_out) {
+  float3 p = v_cross(d, e2);
+  float det = v_dot(e1, p);
+  if (det == 0.0f) return false;
+  float inv = 1.0f / det;
+  float3 s = v_sub(o, v0);
+  float u = v_dot(s, p) * inv;
+  if (u < 0.0f || u > 1.0f) return false;
+  float3 q = v_cross(s, e1);
+  float v = v_dot(d, q) * inv;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  float t = v_dot(e2, q) * inv;
+  if (!(t > tmin && t < tmax)) return false;
+  *t_out = t;
+  *u_out = u;
+  *v_out = v;
+  return true;
+}
+
+__device__ __forceinline__ float safe_rcp(float x) {
+  const float tiny = 1e-12f;
+  if (fabsf(x) < tiny) x = x < 0.0f ? -tiny : tiny;
+  return 1.0f / x;
+}
+
+// Returns true on a hit.  ANY: stop at the first hit, skipping light triangles.
+// *overflow is set to 1 when the traversal stack would overflow (the ray is then
+// answered from the part of the tree already visited) and to 2 at the step cap.
+template <bool ANY>
+__device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, const float4* __restrict__ tris, float3 o,
+                                          float3 d, float tmin, float tmax, TriHit* hit, int* overflow) {
+  const float3 id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  const float3 ood = f3(o.x * id.x, o.y * id.y, o.z * id.z);
+  int stack[kTraceStack];
+  int sp = 0;
+  int node = 0;
+  bool found = false;
+  // box test bound widened by a few ulps so rounding never culls a true hit
+  const float widen = 1.0000004f;
+  // a well-formed tree visits far fewer nodes; the cap only guards against a
+  // malformed one (reported through *overflow = 2)
+  int steps = 0;
+  while (true) {
+    while (node >= 0) {
+      if (++steps > kTraceStepCap) {
+        *overflow = 2;
+        return found;
+      }
+      const float4 n0 = __ldg(&nodes[4 * node + 0]);
+      const float4 n1 = __ldg(&nodes[4 * node + 1]);
+      const float4 n2 = __ldg(&nodes[4 * node + 2]);
+      const float4 n3 = __ldg(&nodes[4 * node + 3]);
+      const float c0lx = fmaf(n0.x, id.x, -ood.x), c0hx = fmaf(n0.y, id.x, -ood.x);
+      const float c0ly = fmaf(n0.z, id.y, -ood.y), c0hy = fmaf(n0.w, id.y, -ood.y);
+      const float c0lz = fmaf(n2.x, id.z, -ood.z), c0hz = fmaf(n2.y, id.z, -ood.z);
+      const float c1lx = fmaf(n1.x, id.x, -ood.x), c1hx = fmaf(n1.y, id.x, -ood.x);
+      const float c1ly = fmaf(n1.z, id.y, -ood.y), c1hy = fmaf(n1.w, id.y, -ood.y);
+      const float c1lz = fmaf(n2.z, id.z, -ood.z), c1hz = fmaf(n2.w, id.z, -ood.z);
+      const float c0min = fmaxf(fmaxf(fminf(c0lx, c0hx), fminf(c0ly, c0hy)), fmaxf(fminf(c0lz, c0hz), tmin));
+      const float c0max = fminf(fminf(fmaxf(c0lx, c0hx), fmaxf(c0ly, c0hy)), fminf(fmaxf(c0lz, c0hz), tmax)) * widen;
+      const float c1min = fmaxf(fmaxf(fminf(c1lx, c1hx), fminf(c1ly, c1hy)), fmaxf(fminf(c1lz, c1hz), tmin));
+      const float c1max = fminf(fminf(fmaxf(c1lx, c1hx), fmaxf(c1ly, c1hy)), fminf(fmaxf(c1lz, c1hz), tmax)) * widen;
+      const bool t0 = c0min <= c0max;
+      const bool t1 = c1min <= c1max;
+      const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
+      if (t0 && t1) {
+        int nearc = ch0, farc = ch1;
+        if (c1min < c0min) { nearc = ch1; farc = ch0; }
+        if (sp < kTraceStack) stack[sp++] = farc;
+        else *overflow = 1;
+        node = nearc;
+      } else if (t0) {
+        node = ch0;
+      } else if (t1) {
+        node = ch1;
+      } else {
+        if (sp == 0) return found;
+        node = stack[--sp];
+      }
+    }
+    // leaf
+    {
+      const int k = ~node;
+      const float4 a = __ldg(&tris[3 * k + 0]);
+      const float4 b = __ldg(&tris[3 * k + 1]);
+      const float4 c = __ldg(&tris[3 * k + 2]);
+      if (!ANY || __float_as_int(b.w) == 0) {
+        float t, u, v;
+        if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
+          found = true;
+          if (ANY) return true;
+          tmax = t;
+          hit->t = t;
+          hit->u = u;
+          hit->v = v;
+          hit->tri = k;
+        }
+      }
+    }
+    if (sp == 0) return found;
+    node = stack[--sp];
+  }
+}
+
+}  // namespace mscg

@@ -1,0 +1,270 @@
+"""Python binding of the GB300 path tracer's C ABI (include/msc_gpu.h).
+
+`Pathtracer` mirrors the reference's engine class msc::Pathtracer
+(include/core/Pathtracer.h:36-110 of joshbainbridge/msc-project): construct
+from a scene YAML, then process() / image() / clear() / active() /
+terminate().  The stage helpers call the device stages on numpy arrays.
+
+The CUDA library is required: importing works without it, but every call
+raises if libmscgpu.so is missing or no GPU is present.  There is no CPU
+fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libmscgpu.so")
+
+MSC_OK = 0
+STAGES = ["raygen", "bins", "ray_keys", "ray_sort", "gather", "trace", "hit_sort", "shade", "shadow", "filter",
+          "other"]
+
+
+class MscError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("msc error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Stats(C.Structure):
+    _fields_ = [("closest_queries", C.c_uint64), ("shadow_queries", C.c_uint64), ("batches", C.c_uint64),
+                ("kernel_launches", C.c_uint64), ("process_ms", C.c_double), ("stage_ms", C.c_double * 12),
+                ("stage_launches", C.c_uint64 * 12), ("width", C.c_int), ("height", C.c_int), ("spp", C.c_int),
+                ("triangles", C.c_int), ("lights", C.c_int), ("iteration", C.c_int)]
+
+
+_lib = None
+
+
+def load_library():
+    """Loads libmscgpu.so; raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MscError(-3, "libmscgpu.so is not built (run __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH)
+    P, I, F, U32 = C.c_void_p, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+    sig = {
+        "msc_create": (I, [C.c_char_p, C.POINTER(P)]),
+        "msc_destroy": (I, [P]),
+        "msc_process": (I, [P, C.POINTER(I)]),
+        "msc_process_device": (I, [P, C.POINTER(I)]),
+        "msc_image": (I, [P, C.POINTER(F), C.POINTER(I), C.POINTER(I)]),
+        "msc_clear": (I, [P]),
+        "msc_active": (I, [P, C.POINTER(I)]),
+        "msc_terminate": (I, [P]),
+        "msc_last_error": (C.c_char_p, [P]),
+        "msc_get_stats": (I, [P, C.POINTER(_Stats)]),
+        "msc_set_profiling": (I, [P, I]),
+        "msc_get_samples": (I, [P, F, F]),
+        "msc_stage_cardinal": (I, [F, I, C.POINTER(C.c_int32)]),
+        "msc_stage_bin_partition": (I, [F, I, I, F, C.POINTER(C.c_int32)]),
+        "msc_stage_ray_keys": (I, [F, F, I, U32]),
+        "msc_sort_pairs": (I, [U32, U32, I, I]),
+        "msc_sort_pairs_device": (I, [P, P, I, I, P]),
+        "msc_trace_closest": (I, [P, F, F, I, F, F, F, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+        "msc_trace_occluded": (I, [P, F, F, F, I, C.POINTER(C.c_int32)]),
+        "msc_generate_scene": (I, [I, C.c_uint32, C.c_double, C.c_char_p, C.c_char_p, I]),
+        "msc_obj_load": (I, [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]),
+        "msc_scene_load_host": (I, [C.c_char_p, C.POINTER(C.c_int32), F, C.POINTER(C.c_int32)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols():
+    """Names declared in include/msc_gpu.h that the binding resolves."""
+    lib = load_library()
+    return [n for n in dir(lib) if n.startswith("msc_")]
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _check(rc, h=None):
+    if rc != MSC_OK:
+        lib = load_library()
+        msg = lib.msc_last_error(h)
+        raise MscError(rc, msg.decode() if msg else "")
+
+
+class Pathtracer:
+    """msc::Pathtracer over the C ABI (include/core/Pathtracer.h:36-110)."""
+
+    def __init__(self, yaml_path):
+        lib = load_library()
+        h = C.c_void_p()
+        rc = lib.msc_create(os.fsencode(yaml_path), C.byref(h))
+        if rc != MSC_OK:
+            msg = lib.msc_last_error(None)
+            raise MscError(rc, msg.decode() if msg else "")
+        self._h = h
+        self._lib = lib
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.msc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def process(self):
+        it = C.c_int(0)
+        _check(self._lib.msc_process(self._h, C.byref(it)), self._h)
+        return it.value
+
+    def process_device(self):
+        it = C.c_int(0)
+        _check(self._lib.msc_process_device(self._h, C.byref(it)), self._h)
+        return it.value
+
+    def image(self):
+        """Accumulated image as an (H, W, 3) float32 copy."""
+        p = C.POINTER(C.c_float)()
+        w, h = C.c_int(), C.c_int()
+        _check(self._lib.msc_image(self._h, C.byref(p), C.byref(w), C.byref(h)), self._h)
+        return np.ctypeslib.as_array(p, shape=(h.value * w.value * 3,)).reshape(h.value, w.value, 3).copy()
+
+    def clear(self):
+        _check(self._lib.msc_clear(self._h), self._h)
+
+    def active(self):
+        a = C.c_int(0)
+        _check(self._lib.msc_active(self._h, C.byref(a)), self._h)
+        return bool(a.value)
+
+    def terminate(self):
+        _check(self._lib.msc_terminate(self._h), self._h)
+
+    def set_profiling(self, on):
+        _check(self._lib.msc_set_profiling(self._h, 1 if on else 0), self._h)
+
+    def stats(self):
+        s = _Stats()
+        _check(self._lib.msc_get_stats(self._h, C.byref(s)), self._h)
+        d = {k: getattr(s, k) for k, _ in _Stats._fields_ if k not in ("stage_ms", "stage_launches")}
+        d["stage_ms"] = {STAGES[i]: s.stage_ms[i] for i in range(len(STAGES))}
+        d["stage_launches"] = {STAGES[i]: int(s.stage_launches[i]) for i in range(len(STAGES))}
+        return d
+
+    def samples(self):
+        st = self.stats()
+        n = st["width"] * st["height"] * st["spp"]
+        rgb = np.zeros((n, 3), np.float32)
+        xy = np.zeros((n, 2), np.float32)
+        _check(self._lib.msc_get_samples(self._h, _ptr(rgb, C.c_float), _ptr(xy, C.c_float)), self._h)
+        return rgb, xy
+
+    def trace_closest(self, org, dirs):
+        org = np.ascontiguousarray(org, np.float32)
+        dirs = np.ascontiguousarray(dirs, np.float32)
+        n = org.shape[0]
+        t, u, v = (np.zeros(n, np.float32) for _ in range(3))
+        g, p = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        _check(self._lib.msc_trace_closest(self._h, _ptr(org, C.c_float), _ptr(dirs, C.c_float), n,
+                                           _ptr(t, C.c_float), _ptr(u, C.c_float), _ptr(v, C.c_float),
+                                           _ptr(g, C.c_int32), _ptr(p, C.c_int32)), self._h)
+        return t, u, v, g, p
+
+    def trace_occluded(self, org, dirs, tmax):
+        org = np.ascontiguousarray(org, np.float32)
+        dirs = np.ascontiguousarray(dirs, np.float32)
+        tmax = np.ascontiguousarray(tmax, np.float32)
+        n = org.shape[0]
+        occ = np.zeros(n, np.int32)
+        _check(self._lib.msc_trace_occluded(self._h, _ptr(org, C.c_float), _ptr(dirs, C.c_float),
+                                            _ptr(tmax, C.c_float), n, _ptr(occ, C.c_int32)), self._h)
+        return occ
+
+
+def cardinal(dirs):
+    lib = load_library()
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(dirs.shape[0], np.int32)
+    _check(lib.msc_stage_cardinal(_ptr(dirs, C.c_float), dirs.shape[0], _ptr(out, C.c_int32)))
+    return out
+
+
+def bin_partition(rays, cap):
+    """rays: (n, 12) float32 records; returns (6*cap, 12) bins and 6 counts."""
+    lib = load_library()
+    rays = np.ascontiguousarray(rays, np.float32)
+    out = np.zeros((6 * cap, 12), np.float32)
+    counts = np.zeros(6, np.int32)
+    _check(lib.msc_stage_bin_partition(_ptr(rays, C.c_float), rays.shape[0], cap, _ptr(out, C.c_float),
+                                       _ptr(counts, C.c_int32)))
+    return out, counts
+
+
+def ray_keys(org, dirs):
+    lib = load_library()
+    org = np.ascontiguousarray(org, np.float32)
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    keys = np.zeros(org.shape[0], np.uint32)
+    _check(lib.msc_stage_ray_keys(_ptr(org, C.c_float), _ptr(dirs, C.c_float), org.shape[0],
+                                  _ptr(keys, C.c_uint32)))
+    return keys
+
+
+def sort_pairs(keys, vals, bits=32):
+    lib = load_library()
+    k = np.ascontiguousarray(keys, np.uint32).copy()
+    v = np.ascontiguousarray(vals, np.uint32).copy()
+    _check(lib.msc_sort_pairs(_ptr(k, C.c_uint32), _ptr(v, C.c_uint32), k.shape[0], bits))
+    return k, v
+
+
+def generate_scene(config, seed, out_dir, scale=1.0):
+    lib = load_library()
+    os.makedirs(out_dir, exist_ok=True)
+    buf = C.create_string_buffer(4096)
+    rc = lib.msc_generate_scene(config, seed, scale, os.fsencode(out_dir), buf, 4096)
+    if rc != MSC_OK:
+        msg = lib.msc_last_error(None)
+        raise MscError(rc, msg.decode() if msg else "")
+    return buf.value.decode()
+
+
+def obj_load(path):
+    """(positions (n,3), texcoords (m,2), indices (k,3)) read by the product's OBJ reader."""
+    lib = load_library()
+    sizes = np.zeros(3, np.int64)
+    _check(lib.msc_obj_load(os.fsencode(path), None, None, None, _ptr(sizes, C.c_int64)))
+    pos = np.zeros(int(sizes[0]), np.float32)
+    tex = np.zeros(int(sizes[1]), np.float32)
+    idx = np.zeros(int(sizes[2]), np.uint32)
+    _check(lib.msc_obj_load(os.fsencode(path), _ptr(pos, C.c_float), _ptr(tex, C.c_float), _ptr(idx, C.c_uint32),
+                            _ptr(sizes, C.c_int64)))
+    return pos.reshape(-1, 3), tex.reshape(-1, 2), idx.reshape(-1, 3)
+
+
+def scene_load_host(yaml_path):
+    """Host-only scene parse: (info dict, tri_v (T,9), tri_geom (T,))."""
+    lib = load_library()
+    info = np.zeros(8, np.int32)
+    _check(lib.msc_scene_load_host(os.fsencode(yaml_path), _ptr(info, C.c_int32), None, None))
+    T = int(info[3])
+    tv = np.zeros((T, 9), np.float32)
+    tg = np.zeros(T, np.int32)
+    _check(lib.msc_scene_load_host(os.fsencode(yaml_path), _ptr(info, C.c_int32), _ptr(tv, C.c_float),
+                                   _ptr(tg, C.c_int32)))
+    keys = ["width", "height", "spp", "triangles", "lights", "shaders", "geometries", "camera"]
+    return dict(zip(keys, [int(x) for x in info])), tv, tg

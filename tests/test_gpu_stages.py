@@ -1,0 +1,138 @@
+"""Stage parity on the GPU through the C ABI: cardinal bins, the stable bin
+partition, ray sort keys and the radix sort are bit-exact against the CPU
+oracle; closest-hit and occlusion queries match it except at stated near-ties."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dirs(rng, n):
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    # exact ties between components and signed zeros exercise the tie rules
+    d[: n // 16, 1] = d[: n // 16, 0]
+    d[n // 16: n // 8, 2] = -d[n // 16: n // 8, 0]
+    d[n // 8: n // 8 + 8] = np.array([[0, 0, 0], [-0.0, 0, 0], [1, 1, 1], [-1, -1, -1], [0, -0.0, 1], [0, 0, -0.0],
+                                      [1, -1, 0], [-1, 1, 0]], np.float32)
+    return d
+
+
+@pytest.mark.parametrize("n", [1, 7, 1000, 200003])
+def test_cardinal_bins_bit_exact(built, n):
+    mscgpu, oracle = built
+    d = _dirs(np.random.default_rng(n), max(n, 16))[:n]
+    assert np.array_equal(mscgpu.cardinal(d), oracle.cardinal(d))
+
+
+def _rays(rng, n, dead_frac=0.2):
+    r = np.zeros((n, 12), np.float32)
+    r[:, 0:3] = rng.uniform(-5, 5, size=(n, 3))
+    r[:, 3] = rng.uniform(0.1, 1, size=n)
+    r[:, 4:7] = _dirs(rng, n)
+    depth = rng.integers(0, 8, size=n).astype(np.int32)
+    depth[rng.random(n) < dead_frac] = -1
+    r[:, 7] = depth.view(np.float32)
+    r[:, 8:11] = rng.uniform(0, 1, size=(n, 3))
+    r[:, 11] = np.arange(n, dtype=np.int32).view(np.float32)
+    return r
+
+
+@pytest.mark.parametrize("n", [0, 1, 5, 2047, 2048, 2049, 100000])
+def test_bin_partition_stable_and_bit_exact(built, n):
+    mscgpu, oracle = built
+    rays = _rays(np.random.default_rng(n + 1), n)
+    cap = max(n, 1)
+    got, gc = mscgpu.bin_partition(rays, cap)
+    want, wc = oracle.bin_partition(rays, cap)
+    assert np.array_equal(gc, wc)
+    for b in range(6):
+        g = got[b * cap: b * cap + gc[b]]
+        w = want[b * cap: b * cap + wc[b]]
+        assert np.array_equal(g.view(np.uint32), w.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 3, 4097, 65536, 300001])
+def test_ray_keys_bit_exact(built, n):
+    mscgpu, oracle = built
+    rng = np.random.default_rng(n + 2)
+    org = rng.uniform(-3, 7, size=(n, 3)).astype(np.float32)
+    org[: n // 3, 1] = 2.5  # a flat extent on part of the batch
+    d = _dirs(rng, max(n, 16))[:n]
+    d[np.abs(d).max(axis=1) == 0] = [0, 0, 1]
+    assert np.array_equal(mscgpu.ray_keys(org, d), oracle.ray_keys(org, d))
+
+
+@pytest.mark.parametrize("n,bits", [(1, 32), (2, 8), (4095, 32), (4096, 16), (4097, 22), (100000, 30),
+                                    (1 << 20, 32), (777777, 11)])
+def test_radix_sort_is_the_stable_order(built, n, bits):
+    mscgpu, oracle = built
+    rng = np.random.default_rng(n * 31 + bits)
+    keys = rng.integers(0, 1 << min(bits, 20), size=n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 4] = keys[0]  # long runs of equal keys test stability
+    if bits < 32:
+        keys |= rng.integers(0, 2, size=n, dtype=np.uint32) << np.uint32(31)  # bits above `bits` are ignored
+    vals = np.arange(n, dtype=np.uint32)
+    gk, gv = mscgpu.sort_pairs(keys, vals, bits)
+    wk, wv = oracle.stable_sort_pairs(keys, vals, bits)
+    assert np.array_equal(gv, wv)
+    assert np.array_equal(gk, wk)
+
+
+def test_radix_sort_full_size_properties(built):
+    """2^24 keys: output sorted, a permutation of the input, stable."""
+    mscgpu, _ = built
+    n = 1 << 24
+    rng = np.random.default_rng(5)
+    keys = rng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    keys[::3] = 12345
+    vals = np.arange(n, dtype=np.uint32)
+    gk, gv = mscgpu.sort_pairs(keys, vals, 32)
+    assert np.all(gk[1:] >= gk[:-1])
+    assert np.array_equal(np.sort(gv), vals)
+    assert np.array_equal(keys[gv], gk)
+    eq = gk[1:] == gk[:-1]
+    assert np.all(gv[1:][eq] > gv[:-1][eq])
+
+
+def _scene_rays(oracle_scene, rng, n):
+    tv, _ = oracle_scene.triangles_array()
+    lo, hi = tv.reshape(-1, 3).min(0), tv.reshape(-1, 3).max(0)
+    org = rng.uniform(lo, hi, size=(n, 3)).astype(np.float32)
+    d = _dirs(rng, n)
+    d[np.abs(d).max(axis=1) == 0] = [0, 1, 0]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return org, d.astype(np.float32)
+
+
+def test_closest_hit_matches_oracle(built, box_scene):
+    mscgpu, oracle = built
+    s = oracle.Scene(box_scene)
+    org, d = _scene_rays(s, np.random.default_rng(11), 200000)
+    with mscgpu.Pathtracer(box_scene) as pt:
+        t, u, v, g, p = pt.trace_closest(org, d)
+    wt, wu, wv, wg, wp = s.trace(org, d)
+    same = (g == wg) & (p == wp)
+    # primitive ids agree except at near-ties: two hits within 1e-5 relative distance
+    tie = ~same & (np.abs(t - wt) <= 1e-5 * np.maximum(np.abs(wt), 1e-3))
+    assert np.all(same | tie), np.flatnonzero(~(same | tie))[:10]
+    assert tie.mean() < 1e-3
+    hit = same & (wg >= 0)
+    assert hit.sum() > 1000
+    for a, b in ((t, wt), (u, wu), (v, wv)):
+        assert np.all(np.abs(a[hit] - b[hit]) <= 1e-5 * np.maximum(np.abs(b[hit]), 1e-3))
+    # the same arithmetic on both sides: most hits agree to the bit
+    assert (t[hit].view(np.uint32) == wt[hit].view(np.uint32)).mean() > 0.999
+
+
+def test_occlusion_matches_oracle(built, box_scene):
+    mscgpu, oracle = built
+    s = oracle.Scene(box_scene)
+    rng = np.random.default_rng(12)
+    org, d = _scene_rays(s, rng, 100000)
+    tmax = rng.uniform(0.01, 3.0, size=org.shape[0]).astype(np.float32)
+    with mscgpu.Pathtracer(box_scene) as pt:
+        got = pt.trace_occluded(org, d, tmax)
+    want = s.occluded(org, d, tmax)
+    assert (got != want).mean() < 1e-3
+    assert 0.05 < want.mean() < 0.95
