@@ -63,6 +63,14 @@ int msc_active(msc_handle* h, int* active);
  * Thread-safe; a running msc_process stops at its next batch boundary. */
 int msc_terminate(msc_handle* h);
 
+/* Writes the accumulated image: ".exr" gives RGBA half-float OpenEXR with alpha 1 as the
+ * reference's batch mode writes it (src/main.cpp:199-213); ".pfm" a float portable map.
+ * divide_by_iterations != 0 writes pixels / iteration (the display scaling of main.cpp:169-174). */
+int msc_save_image(msc_handle* h, const char* path, int divide_by_iterations);
+
+/* Host-only form of the writer above for any row-major RGB float image. */
+int msc_write_image_file(const char* path, int width, int height, const float* rgb);
+
 /* Message of the last failing call on this handle (or of the last failed msc_create when h is NULL). */
 const char* msc_last_error(msc_handle* h);
 

@@ -31,6 +31,8 @@
 namespace mscg {
 bool generate_scene(int config, uint32_t seed, double scale, const std::string& dir, std::string* yaml,
                     std::string* err);
+bool write_exr_rgba_half(const std::string& path, int w, int h, const float* rgb, std::string* err);
+bool write_pfm(const std::string& path, int w, int h, const float* rgb, std::string* err);
 }
 
 using namespace mscg;
@@ -586,6 +588,41 @@ int msc_active(msc_handle* h, int* active) {
 int msc_terminate(msc_handle* h) {
   if (!h) return MSC_ERR_ARG;
   h->terminate.store(true);
+  return MSC_OK;
+}
+
+int msc_save_image(msc_handle* h, const char* path, int divide_by_iterations) {
+  if (!h || !path) return MSC_ERR_ARG;
+  const float* px = nullptr;
+  int w = 0, ht = 0;
+  int rc = msc_image(h, &px, &w, &ht);
+  if (rc != MSC_OK) return rc;
+  std::vector<float> buf(px, px + (size_t)3 * w * ht);
+  if (divide_by_iterations && h->iteration > 0)
+    for (float& v : buf) v /= (float)h->iteration;
+  std::string p(path), err;
+  bool ok = false;
+  try {
+    if (p.size() >= 4 && p.compare(p.size() - 4, 4, ".pfm") == 0) ok = write_pfm(p, w, ht, buf.data(), &err);
+    else ok = write_exr_rgba_half(p, w, ht, buf.data(), &err);
+  } catch (const std::exception& e) {
+    err = e.what();
+  }
+  if (!ok) { h->err = err; return MSC_ERR_ARG; }
+  return MSC_OK;
+}
+
+int msc_write_image_file(const char* path, int width, int height, const float* rgb) {
+  if (!path || !rgb || width <= 0 || height <= 0) return MSC_ERR_ARG;
+  std::string p(path), err;
+  bool ok = false;
+  try {
+    if (p.size() >= 4 && p.compare(p.size() - 4, 4, ".pfm") == 0) ok = write_pfm(p, width, height, rgb, &err);
+    else ok = write_exr_rgba_half(p, width, height, rgb, &err);
+  } catch (const std::exception& e) {
+    err = e.what();
+  }
+  if (!ok) { g_create_error = err; return MSC_ERR_ARG; }
   return MSC_OK;
 }
 

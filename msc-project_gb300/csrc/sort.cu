@@ -14,7 +14,7 @@ namespace {
 
 constexpr int RADIX = 1 << kSortRadixBits;
 
-__global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift,
+__global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift, uint32_t mask,
                                                               uint32_t* __restrict__ counts, int num_tiles) {
   __shared__ int hist[RADIX];
   for (int i = threadIdx.x; i < RADIX; i += kSortBlock) hist[i] = 0;
@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __
 #pragma unroll 4
   for (int k = 0; k < kSortItems; ++k) {
     int idx = base + k * kSortBlock + threadIdx.x;
-    int d = idx < n ? (int)((keys[idx] >> shift) & (RADIX - 1)) : -1;
+    int d = idx < n ? (int)((keys[idx] >> shift) & mask) : -1;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     if (d >= 0 && lane == __ffs(peers) - 1) atomicAdd(&hist[d], __popc(peers));
   }
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __
 __global__ void __launch_bounds__(kSortBlock) k_radix_downsweep(const uint32_t* __restrict__ keys_in,
                                                                 const uint32_t* __restrict__ vals_in,
                                                                 uint32_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out, int n, int shift,
+                                                                uint32_t* __restrict__ vals_out, int n, int shift, uint32_t mask,
                                                                 const uint32_t* __restrict__ offsets, int num_tiles) {
   __shared__ RankSmem<kSortBlock, RADIX> sm;
   __shared__ uint32_t skey[kSortTile];
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_downsweep(const uint32_t* 
     bool ok = idx < n;
     key[k] = ok ? keys_in[idx] : 0u;
     val[k] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
-    dig[k] = ok ? (int)((key[k] >> shift) & (RADIX - 1)) : -1;
+    dig[k] = ok ? (int)((key[k] >> shift) & mask) : -1;
   }
   tile_rank<kSortBlock, kSortItems, RADIX>(dig, pos, sm);
 #pragma unroll
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_downsweep(const uint32_t* 
   const int count = min(kSortTile, n - base);
   for (int p = threadIdx.x; p < count; p += kSortBlock) {
     uint32_t k = skey[p];
-    int d = (int)((k >> shift) & (RADIX - 1));
+    int d = (int)((k >> shift) & mask);
     uint32_t o = gofs[d] + (uint32_t)(p - sm.tile_start[d]);
     keys_out[o] = k;
     vals_out[o] = sval[p];
@@ -162,9 +162,13 @@ int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
     uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
     uint32_t* dst_v = to_out ? vals_out : s.vals_alt;
     const int shift = p * kSortRadixBits;
-    k_radix_upsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, n, shift, s.counts, tiles);
+    // the last pass only looks at the bits below `bits`
+    const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
+    const uint32_t mask = (1u << width) - 1u;
+    k_radix_upsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, n, shift, mask, s.counts, tiles);
     k_scan_exclusive<<<1, 1024, 0, stream>>>(s.counts, tiles * RADIX, nullptr);
-    k_radix_downsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, shift, s.counts, tiles);
+    k_radix_downsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, shift, mask, s.counts,
+                                                         tiles);
     launches += 3;
     src_k = dst_k;
     src_v = dst_v;

@@ -23,7 +23,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["sort.cu", "bvh.cu", "render.cu", "engine.cu"]
-CPP_SOURCES = ["scene.cpp", "scenegen.cpp"]
+CPP_SOURCES = ["scene.cpp", "scenegen.cpp", "imageio.cpp"]
+CLI = os.path.join(HERE, "msc-gpu")
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true",
@@ -74,6 +75,10 @@ def build(verbose=False, force=False):
     if force or jobs or not os.path.exists(LIB) or _stale(LIB, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lpthread", "-ldl", "-lrt"],
              os.path.join(OUT_DIR, "link.log"))
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    if force or _stale(CLI, [cli_src, LIB]):
+        _run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"), cli_src, "-o", CLI, "-L" + HERE,
+              "-lmscgpu", "-Wl,-rpath,$ORIGIN"], os.path.join(OUT_DIR, "cli.log"))
     return LIB
 
 
