@@ -126,6 +126,16 @@ int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
  * Scratch is allocated per call. */
 int msc_sort_pairs_device(uint32_t* keys, uint32_t* vals, int n, int bits, void* stream);
 
+/* Same sort as msc_sort_pairs_device, for callers that cannot allocate device memory
+ * while they run (a host that reserves its whole device budget up front, or a
+ * latency-critical loop that cannot take cudaFree's device synchronisation).
+ * No counterpart in the reference.  Allocates nothing: its scratch is a static
+ * device array sized for at most 1,048,576 pairs, held by every GPU that loads
+ * the library; larger n returns MSC_ERR_ARG with a message in msc_last_error(NULL).
+ * The first call on a device looks up that array's address (make it before any
+ * stream capture); calls that overlap on the GPU share the array and race. */
+int msc_sort_pairs_device_noalloc(uint32_t* keys, uint32_t* vals, int n, int bits, void* stream);
+
 /* Closest hit against the handle's scene (rtcIntersect, src/core/RayIntersect.cpp:7-12)
  * on [0.001, 1e5].  geom/prim are the reference's geomID/primID, -1 for a miss. */
 int msc_trace_closest(msc_handle* h, const float* org, const float* dir, int n, float* t, float* u, float* v,

@@ -38,8 +38,15 @@ bool write_pfm(const std::string& path, int w, int h, const float* rgb, std::str
 using namespace mscg;
 
 namespace {
-
 thread_local std::string g_create_error;
+}
+
+namespace mscg {
+// Message returned by msc_last_error(NULL) on this thread.
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace mscg
+
+namespace {
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 

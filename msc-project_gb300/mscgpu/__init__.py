@@ -65,6 +65,7 @@ def load_library():
         "msc_stage_ray_keys": (I, [F, F, I, U32]),
         "msc_sort_pairs": (I, [U32, U32, I, I]),
         "msc_sort_pairs_device": (I, [P, P, I, I, P]),
+        "msc_sort_pairs_device_noalloc": (I, [P, P, I, I, P]),
         "msc_trace_closest": (I, [P, F, F, I, F, F, F, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
         "msc_trace_occluded": (I, [P, F, F, F, I, C.POINTER(C.c_int32)]),
         "msc_generate_scene": (I, [I, C.c_uint32, C.c_double, C.c_char_p, C.c_char_p, I]),
