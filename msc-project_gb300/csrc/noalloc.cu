@@ -31,8 +31,7 @@ void set_global_error(const std::string& msg);  // defined in engine.cu
 namespace {
 
 constexpr int kNoAllocMaxPairs = 1 << 20;
-constexpr size_t kNoAllocTiles = (kNoAllocMaxPairs + mscg::kSortTile - 1) / mscg::kSortTile;
-constexpr size_t kNoAllocBytes = 2 * (size_t)kNoAllocMaxPairs * 4 + kNoAllocTiles * (1u << mscg::kSortRadixBits) * 4;
+constexpr size_t kNoAllocBytes = mscg::sort_scratch_bytes(kNoAllocMaxPairs);
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocBytes];
 

@@ -102,26 +102,49 @@ __device__ __forceinline__ void tile_rank(const int (&digit)[ITEMS], int (&pos)[
 // Single-block exclusive scan of data[0..len) in place; total written to *total if non-null.
 __global__ void k_scan_exclusive(uint32_t* data, int len, uint32_t* total);
 
-struct SortScratch {
-  uint32_t* keys_alt = nullptr;
-  uint32_t* vals_alt = nullptr;
-  uint32_t* counts = nullptr;   // RADIX * max tiles
-  int capacity = 0;
-};
-
 constexpr int kSortBlock = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortBlock * kSortItems;
 constexpr int kSortRadixBits = 8;
+constexpr int kSortMaxPasses = 4;
 
-size_t sort_scratch_bytes(int capacity);
+struct SortScratch {
+  uint32_t* keys_alt = nullptr;
+  uint32_t* vals_alt = nullptr;
+  uint32_t* counts = nullptr;   // reduce-then-scan: RADIX * tiles (aliases the first half of `status`)
+  uint32_t* status = nullptr;   // look-back words: 2 arrays of RADIX * tiles
+  uint32_t* hist = nullptr;     // kSortMaxPasses * RADIX global digit counts
+  uint32_t* ctl = nullptr;      // kSortMaxPasses tile counters, then the error word
+  int capacity = 0;
+};
+
+constexpr size_t sort_align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t sort_tiles(int capacity) {
+  return capacity <= 0 ? 1 : ((size_t)capacity + kSortTile - 1) / kSortTile;
+}
+// Scratch bytes for sorts of up to `capacity` pairs.
+constexpr size_t sort_scratch_bytes(int capacity) {
+  return 2 * sort_align256((size_t)(capacity > 0 ? capacity : 1) * 4) +
+         sort_align256(2 * sort_tiles(capacity) * (1u << kSortRadixBits) * 4) +
+         sort_align256((size_t)kSortMaxPasses * (1u << kSortRadixBits) * 4 + 64);
+}
 // Carves the scratch buffers out of `base` (sort_scratch_bytes(capacity) bytes, 256-aligned).
 void sort_scratch_bind(SortScratch* s, void* base, int capacity);
 
 // Stable LSD sort of (keys_in, vals_in) on bits [0, bits) into (keys_out, vals_out).
 // vals_in == nullptr means vals_in[i] = i.  Input buffers are left unchanged
-// unless they alias the outputs.  Returns the number of kernel launches.
+// unless they alias the outputs.  One histogram kernel for all passes, then
+// one kernel per 8-bit pass with a decoupled look-back across tiles.  Spin
+// waits are capped; a cap that runs out sets bit 8 of *err (when err is not
+// null).  Returns the number of kernel launches.
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream);
+               int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr);
+
+// The same order with three kernels per pass (upsweep count, one-block scan,
+// downsweep scatter) and no inter-block waiting.
+int sort_pairs_reduce_scan(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                           int n, int bits, SortScratch& s, cudaStream_t stream);
+
+constexpr int kSortErrLookback = 256;
 
 }  // namespace mscg

@@ -1,11 +1,19 @@
-// Stable LSD radix sort of 32-bit keys with 32-bit values (reduce-then-scan
-// per 8-bit digit): an upsweep counts digits per tile, one block scans the
-// digit-major count table, and a downsweep ranks each tile stably, stages it
-// in shared memory in digit order and writes contiguous runs.
+// Stable LSD radix sort of 32-bit keys with 32-bit values, 8-bit digits.
 //
-// It replaces the reference's comparison sorts on the batch
-// (tbb::parallel_sort in src/core/RaySort.cpp:17,97 and the hit sort in
-// src/core/Pathtracer.cpp:335-339) with a key-based stable order.
+// sort_pairs (the one the render loop uses): one histogram kernel counts the
+// digits of every pass in a single read of the keys; then each pass is one
+// kernel.  A block takes the next tile from a counter, ranks its keys stably
+// (tile_rank: warp match + per-warp counters), publishes its per-digit counts,
+// and sums its predecessors' counts by a decoupled look-back (each tile first
+// posts an aggregate, then its inclusive prefix).  The tile is staged in
+// shared memory in digit order, so the global scatter writes contiguous runs.
+//
+// sort_pairs_reduce_scan: the same order with upsweep / one-block scan /
+// downsweep kernels per pass, kept as a wait-free reference path.
+//
+// Both replace the reference's comparison sorts of a batch (tbb::parallel_sort
+// in src/core/RaySort.cpp:17,97 and the hit sort of src/core/Pathtracer.cpp:335-339)
+// with a key-based stable order.
 #include "radix.cuh"
 
 namespace mscg {
@@ -13,9 +21,139 @@ namespace mscg {
 namespace {
 
 constexpr int RADIX = 1 << kSortRadixBits;
+constexpr uint32_t kFlagAggregate = 1u;
+constexpr uint32_t kFlagPrefix = 2u;
+constexpr int kLookbackSpinCap = 1 << 20;
 
-__global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift, uint32_t mask,
-                                                              uint32_t* __restrict__ counts, int num_tiles) {
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+__device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+
+// ------------------------------------------------------------- onesweep
+__global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __restrict__ keys, int n, int passes,
+                                                              int bits, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[kSortMaxPasses][RADIX];
+  for (int i = threadIdx.x; i < kSortMaxPasses * RADIX; i += kSortBlock) (&sh[0][0])[i] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * kSortBlock;
+  for (int base = blockIdx.x * kSortBlock; base < n; base += stride) {
+    const int idx = base + threadIdx.x;
+    const bool ok = idx < n;
+    const uint32_t key = ok ? keys[idx] : 0u;
+    for (int p = 0; p < passes; ++p) {
+      const int shift = p * kSortRadixBits;
+      const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
+      const int d = ok ? (int)((key >> shift) & ((1u << width) - 1u)) : -1;
+      const unsigned peers = __match_any_sync(0xffffffffu, d);
+      if (d >= 0 && lane == __ffs(peers) - 1) atomicAdd(&sh[p][d], (uint32_t)__popc(peers));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * RADIX; i += kSortBlock) {
+    const uint32_t c = (&sh[0][0])[i];
+    if (c) atomicAdd(&hist[i], c);
+  }
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_tmp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tmp[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += warp_tmp[w];
+  __syncthreads();
+  return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              uint32_t* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, int n, int shift,
+                                                              uint32_t mask, int pass,
+                                                              const uint32_t* __restrict__ hist, uint32_t* status_cur,
+                                                              uint32_t* status_next, uint32_t* ctl, int* err) {
+  static_assert(RADIX == kSortBlock, "one digit per thread");
+  __shared__ RankSmem<kSortBlock, RADIX> sm;
+  __shared__ uint32_t skey[kSortTile];
+  __shared__ uint32_t sval[kSortTile];
+  __shared__ uint32_t gofs[RADIX];
+  __shared__ uint32_t warp_tmp[kSortBlock / 32];
+  __shared__ int s_tile;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl[pass], 1u);
+  const uint32_t dstart = block_excl_scan(hist[pass * RADIX + threadIdx.x], warp_tmp);  // syncs inside
+  const int tile = s_tile;
+  const int base = tile * kSortTile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // the next pass reads status_next from zero; the pass that last used it has finished
+  if (status_next) status_next[tile * RADIX + threadIdx.x] = 0u;
+  uint32_t key[kSortItems], val[kSortItems];
+  int dig[kSortItems], pos[kSortItems];
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const int idx = base + warp * 32 * kSortItems + k * 32 + lane;
+    const bool ok = idx < n;
+    key[k] = ok ? keys_in[idx] : 0u;
+    val[k] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
+    dig[k] = ok ? (int)((key[k] >> shift) & mask) : -1;
+  }
+  tile_rank<kSortBlock, kSortItems, RADIX>(dig, pos, sm);
+  {
+    const int d = threadIdx.x;
+    const uint32_t cnt = (uint32_t)sm.tile_count[d];
+    uint32_t excl = 0;
+    if (tile == 0) {
+      st_volatile(&status_cur[d], (cnt << 2) | kFlagPrefix);
+    } else {
+      st_volatile(&status_cur[tile * RADIX + d], (cnt << 2) | kFlagAggregate);
+      int t = tile - 1;
+      int spins = 0;
+      while (t >= 0) {
+        const uint32_t v = ld_volatile(&status_cur[t * RADIX + d]);
+        const uint32_t f = v & 3u;
+        if (f == 0u) {  // the predecessor has not posted yet; it is running, so this ends
+          if (++spins > kLookbackSpinCap) {
+            atomicOr(err, kSortErrLookback);
+            break;
+          }
+          continue;
+        }
+        excl += v >> 2;
+        if (f == kFlagPrefix) break;
+        --t;
+      }
+      st_volatile(&status_cur[tile * RADIX + d], ((excl + cnt) << 2) | kFlagPrefix);
+    }
+    gofs[d] = dstart + excl;
+  }
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    if (pos[k] >= 0) {
+      skey[pos[k]] = key[k];
+      sval[pos[k]] = val[k];
+    }
+  }
+  __syncthreads();
+  const int count = min(kSortTile, n - base);
+  for (int p = threadIdx.x; p < count; p += kSortBlock) {
+    const uint32_t k = skey[p];
+    const int d = (int)((k >> shift) & mask);
+    const uint32_t o = gofs[d] + (uint32_t)(p - sm.tile_start[d]);
+    keys_out[o] = k;
+    vals_out[o] = sval[p];
+  }
+}
+
+// ------------------------------------------------------ reduce-then-scan
+__global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift,
+                                                              uint32_t mask, uint32_t* __restrict__ counts,
+                                                              int num_tiles) {
   __shared__ int hist[RADIX];
   for (int i = threadIdx.x; i < RADIX; i += kSortBlock) hist[i] = 0;
   __syncthreads();
@@ -35,8 +173,9 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __
 __global__ void __launch_bounds__(kSortBlock) k_radix_downsweep(const uint32_t* __restrict__ keys_in,
                                                                 const uint32_t* __restrict__ vals_in,
                                                                 uint32_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out, int n, int shift, uint32_t mask,
-                                                                const uint32_t* __restrict__ offsets, int num_tiles) {
+                                                                uint32_t* __restrict__ vals_out, int n, int shift,
+                                                                uint32_t mask, const uint32_t* __restrict__ offsets,
+                                                                int num_tiles) {
   __shared__ RankSmem<kSortBlock, RADIX> sm;
   __shared__ uint32_t skey[kSortTile];
   __shared__ uint32_t sval[kSortTile];
@@ -79,6 +218,36 @@ __global__ void k_copy_u32(const uint32_t* __restrict__ src, uint32_t* __restric
   if (i < n) dst[i] = iota ? (uint32_t)i : src[i];
 }
 
+// Shared front part of both sorts: the zero-bit case and odd-pass aliasing.
+int sort_prologue(const uint32_t*& src_k, const uint32_t*& src_v, const uint32_t* keys_in, const uint32_t* vals_in,
+                  uint32_t* keys_out, uint32_t* vals_out, int n, int passes, SortScratch& s, cudaStream_t stream,
+                  bool* done) {
+  *done = false;
+  int launches = 0;
+  src_k = keys_in;
+  src_v = vals_in;
+  if (passes == 0) {
+    const int tb = 256, g = (n + tb - 1) / tb;
+    if (keys_in != keys_out) cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
+    if (vals_in == nullptr) {
+      k_copy_u32<<<g, tb, 0, stream>>>(nullptr, vals_out, n, 1);
+      ++launches;
+    } else if (vals_in != vals_out) {
+      cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
+    }
+    *done = true;
+    return launches;
+  }
+  if ((passes % 2) == 1 && (keys_in == keys_out || (vals_in != nullptr && vals_in == vals_out))) {
+    // an odd pass count writes the outputs first: move the inputs out of the way
+    cudaMemcpyAsync(s.keys_alt, keys_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
+    if (vals_in) cudaMemcpyAsync(s.vals_alt, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
+    src_k = s.keys_alt;
+    src_v = vals_in ? s.vals_alt : nullptr;
+  }
+  return launches;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, int len, uint32_t* total) {
@@ -117,52 +286,73 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, int len
   }
 }
 
-static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-size_t sort_scratch_bytes(int capacity) {
-  size_t tiles = (size_t)(capacity + kSortTile - 1) / kSortTile;
-  if (tiles == 0) tiles = 1;
-  return align256((size_t)capacity * 4) * 2 + align256(tiles * RADIX * 4);
-}
-
 void sort_scratch_bind(SortScratch* s, void* base, int capacity) {
+  const size_t cap = (size_t)(capacity > 0 ? capacity : 1);
   char* p = (char*)base;
   s->keys_alt = (uint32_t*)p;
-  p += align256((size_t)capacity * 4);
+  p += sort_align256(cap * 4);
   s->vals_alt = (uint32_t*)p;
-  p += align256((size_t)capacity * 4);
-  s->counts = (uint32_t*)p;
+  p += sort_align256(cap * 4);
+  s->status = (uint32_t*)p;
+  s->counts = s->status;
+  p += sort_align256(2 * sort_tiles(capacity) * RADIX * 4);
+  s->hist = (uint32_t*)p;
+  s->ctl = s->hist + kSortMaxPasses * RADIX;
   s->capacity = capacity;
 }
 
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream) {
+               int bits, SortScratch& s, cudaStream_t stream, int* err) {
   if (n <= 0) return 0;
-  int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
-  int launches = 0;
-  if (passes == 0) {
-    const int tb = 256, g = (n + tb - 1) / tb;
-    if (keys_in != keys_out) { cudaMemcpyAsync(keys_out, keys_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream); }
-    if (vals_in == nullptr) { k_copy_u32<<<g, tb, 0, stream>>>(nullptr, vals_out, n, 1); ++launches; }
-    else if (vals_in != vals_out) cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
-    return launches;
-  }
+  const int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
+  const uint32_t* src_k;
+  const uint32_t* src_v;
+  bool done;
+  int launches = sort_prologue(src_k, src_v, keys_in, vals_in, keys_out, vals_out, n, passes, s, stream, &done);
+  if (done) return launches;
   const int tiles = (n + kSortTile - 1) / kSortTile;
-  const uint32_t* src_k = keys_in;
-  const uint32_t* src_v = vals_in;
-  if ((passes % 2) == 1 && (keys_in == keys_out || (vals_in != nullptr && vals_in == vals_out))) {
-    // an odd pass count writes the outputs first: move the inputs out of the way
-    cudaMemcpyAsync(s.keys_alt, keys_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
-    if (vals_in) cudaMemcpyAsync(s.vals_alt, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, stream);
-    src_k = s.keys_alt;
-    src_v = vals_in ? s.vals_alt : nullptr;
-  }
+  uint32_t* status0 = s.status;
+  uint32_t* status1 = s.status + (size_t)tiles * RADIX;
+  // zero the first look-back array, the histograms, the tile counters and the error word
+  cudaMemsetAsync(status0, 0, (size_t)tiles * RADIX * 4, stream);
+  cudaMemsetAsync(s.hist, 0, (size_t)kSortMaxPasses * RADIX * 4 + 64, stream);
+  int* errw = err ? err : (int*)(s.ctl + kSortMaxPasses);
+  const int hist_blocks = tiles < 2 * 152 ? tiles : 2 * 152;
+  k_onesweep_hist<<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, passes, bits, s.hist);
+  ++launches;
   for (int p = 0; p < passes; ++p) {
-    bool to_out = ((passes - 1 - p) % 2) == 0;
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
     uint32_t* dst_v = to_out ? vals_out : s.vals_alt;
     const int shift = p * kSortRadixBits;
-    // the last pass only looks at the bits below `bits`
+    const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;  // the last pass may be narrower
+    const uint32_t mask = (1u << width) - 1u;
+    uint32_t* cur = (p & 1) ? status1 : status0;
+    uint32_t* next = (p + 1 < passes) ? ((p & 1) ? status0 : status1) : nullptr;
+    k_onesweep_pass<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, shift, mask, p, s.hist, cur, next,
+                                                      s.ctl, errw);
+    ++launches;
+    src_k = dst_k;
+    src_v = dst_v;
+  }
+  return launches;
+}
+
+int sort_pairs_reduce_scan(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                           int n, int bits, SortScratch& s, cudaStream_t stream) {
+  if (n <= 0) return 0;
+  const int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
+  const uint32_t* src_k;
+  const uint32_t* src_v;
+  bool done;
+  int launches = sort_prologue(src_k, src_v, keys_in, vals_in, keys_out, vals_out, n, passes, s, stream, &done);
+  if (done) return launches;
+  const int tiles = (n + kSortTile - 1) / kSortTile;
+  for (int p = 0; p < passes; ++p) {
+    const bool to_out = ((passes - 1 - p) % 2) == 0;
+    uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
+    uint32_t* dst_v = to_out ? vals_out : s.vals_alt;
+    const int shift = p * kSortRadixBits;
     const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
     const uint32_t mask = (1u << width) - 1u;
     k_radix_upsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, n, shift, mask, s.counts, tiles);
