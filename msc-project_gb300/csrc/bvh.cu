@@ -5,6 +5,11 @@
 // sort -> one thread per internal node finds its range and split -> one
 // thread per leaf walks to the root, the second arrival at each node
 // forming its box -> pack into the traversal layout of trace.cuh.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "bvh.h"
 #include "dmath.h"
 #include "radix.cuh"
@@ -187,10 +192,154 @@ __global__ void k_scene_bounds(const float4* __restrict__ node_box, float* out) 
 
 size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ------------------------------------------------------------------ 8-wide collapse
+// The binary LBVH is collapsed top-down: a wide node starts from the two
+// children of a binary node and repeatedly opens the child with the largest
+// surface area until it has 8 children or none is left to open.  A binary
+// subtree of at most kWideLeafMax triangles becomes one leaf child; its
+// triangles are re-emitted so that a node's leaf triangles are contiguous
+// from the node's triangle base.  Child boxes are quantised to 8 bits per
+// axis against the node box with power-of-two steps, rounded outward so the
+// decoded box always contains the child.
+constexpr int kWideLeafMax = 3;
+
+struct WideBuild {
+  std::vector<uint32_t> words;  // 20 words per node
+  std::vector<int> tri_perm;    // new triangle order -> leaf index of the binary tree
+};
+
+float surface(const float4& lo, const float4& hi) {
+  float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+void quantise_axis(float lo, float hi, int* e_out, float* scale_out) {
+  double ext = (double)hi - (double)lo;
+  int e = -126;
+  if (ext > 0.0) {
+    e = (int)std::ceil(std::log2(ext / 255.0));
+    while (std::ldexp(255.0, e) < ext) ++e;
+    if (e < -126) e = -126;
+    if (e > 127) e = 127;
+  }
+  *e_out = e;
+  *scale_out = (float)std::ldexp(1.0, e);
+}
+
+uint32_t q_lo(float p, float s, float v) {
+  double q = std::floor(((double)v - (double)p) / (double)s);
+  int qi = (int)std::max(0.0, std::min(255.0, q));
+  while (qi > 0 && std::fma((float)qi, s, p) > v) --qi;
+  return (uint32_t)qi;
+}
+
+uint32_t q_hi(float p, float s, float v) {
+  double q = std::ceil(((double)v - (double)p) / (double)s);
+  int qi = (int)std::max(0.0, std::min(255.0, q));
+  while (qi < 255 && std::fma((float)qi, s, p) < v) ++qi;
+  return (uint32_t)qi;
+}
+
+void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>& nbox, const std::vector<float4>& lbox,
+                   WideBuild* out) {
+  // leaf range [first, first + count) of every internal node, children before parents
+  std::vector<int> first(n - 1), count(n - 1), bfs;
+  bfs.reserve(n - 1);
+  bfs.push_back(0);
+  for (size_t i = 0; i < bfs.size(); ++i) {
+    int2 c = ch[bfs[i]];
+    if (c.x >= 0) bfs.push_back(c.x);
+    if (c.y >= 0) bfs.push_back(c.y);
+  }
+  for (size_t i = bfs.size(); i-- > 0;) {
+    int b = bfs[i];
+    int2 c = ch[b];
+    int fl = c.x < 0 ? ~c.x : first[c.x], cl = c.x < 0 ? 1 : count[c.x];
+    int fr = c.y < 0 ? ~c.y : first[c.y], cr = c.y < 0 ? 1 : count[c.y];
+    first[b] = std::min(fl, fr);
+    count[b] = cl + cr;
+  }
+  auto is_leafish = [&](int c) { return c < 0 || count[c] <= kWideLeafMax; };
+  auto box_lo = [&](int c) { return c < 0 ? lbox[2 * (~c)] : nbox[2 * c]; };
+  auto box_hi = [&](int c) { return c < 0 ? lbox[2 * (~c) + 1] : nbox[2 * c + 1]; };
+  out->words.clear();
+  out->tri_perm.clear();
+  out->tri_perm.reserve(n);
+  std::vector<int> queue;  // binary node of each wide node, in wide-node order
+  queue.push_back(0);
+  out->words.resize(20);
+  for (size_t w = 0; w < queue.size(); ++w) {
+    const int b = queue[w];
+    int C[8];
+    int k = 0;
+    C[k++] = ch[b].x;
+    C[k++] = ch[b].y;
+    while (k < 8) {
+      int best = -1;
+      float best_area = -1.f;
+      for (int i = 0; i < k; ++i) {
+        if (is_leafish(C[i])) continue;
+        float a = surface(nbox[2 * C[i]], nbox[2 * C[i] + 1]);
+        if (a > best_area) { best_area = a; best = i; }
+      }
+      if (best < 0) break;
+      int c = C[best];
+      for (int j = k; j > best + 1; --j) C[j] = C[j - 1];
+      C[best] = ch[c].x;
+      C[best + 1] = ch[c].y;
+      ++k;
+    }
+    const float4 lo = nbox[2 * b], hi = nbox[2 * b + 1];
+    int e[3];
+    float s[3];
+    quantise_axis(lo.x, hi.x, &e[0], &s[0]);
+    quantise_axis(lo.y, hi.y, &e[1], &s[1]);
+    quantise_axis(lo.z, hi.z, &e[2], &s[2]);
+    uint32_t imask = 0, meta[2] = {0, 0}, q[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    const uint32_t child_base = (uint32_t)queue.size();
+    const uint32_t tri_base = (uint32_t)out->tri_perm.size();
+    for (int i = 0; i < k; ++i) {
+      const int c = C[i];
+      uint32_t m = 0;
+      if (is_leafish(c)) {
+        const int f = c < 0 ? ~c : first[c], cnt = c < 0 ? 1 : count[c];
+        const uint32_t off = (uint32_t)out->tri_perm.size() - tri_base;
+        for (int t = 0; t < cnt; ++t) out->tri_perm.push_back(f + t);
+        m = ((uint32_t)cnt << 5) | off;
+      } else {
+        imask |= 1u << i;
+        queue.push_back(c);
+      }
+      meta[i >> 2] |= m << (8 * (i & 3));
+      const float4 cl = box_lo(c), chh = box_hi(c);
+      const float cll[3] = {cl.x, cl.y, cl.z}, chl[3] = {chh.x, chh.y, chh.z}, pl[3] = {lo.x, lo.y, lo.z};
+      for (int a = 0; a < 3; ++a) {
+        q[a][i >> 2] |= q_lo(pl[a], s[a], cll[a]) << (8 * (i & 3));
+        q[3 + a][i >> 2] |= q_hi(pl[a], s[a], chl[a]) << (8 * (i & 3));
+      }
+    }
+    out->words.resize(20 * queue.size());
+    uint32_t* W = &out->words[20 * w];
+    memcpy(&W[0], &lo.x, 4);
+    memcpy(&W[1], &lo.y, 4);
+    memcpy(&W[2], &lo.z, 4);
+    W[3] = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
+    W[4] = child_base;
+    W[5] = tri_base;
+    W[6] = meta[0];
+    W[7] = meta[1];
+    // q_lo x, y, z then q_hi x, y, z, two words (slots 0-3, 4-7) each
+    for (int a = 0; a < 6; ++a) {
+      W[8 + 2 * a] = q[a][0];
+      W[9 + 2 * a] = q[a][1];
+    }
+  }
+}
+
 }  // namespace
 
-int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n, DeviceBvh* out, cudaStream_t stream,
-              std::string* err) {
+int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n, bool wide, DeviceBvh* out,
+              cudaStream_t stream, std::string* err) {
   if (n < 2) { *err = "the BVH needs at least two triangles"; return -1; }
   int launches = 0;
   out->num_tris = n;
@@ -239,14 +388,62 @@ int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n
   int refit_err = 0;
   cudaMemcpyAsync(&refit_err, bounds + 7, 4, cudaMemcpyDeviceToHost, stream);
   cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) {
+    cudaFree(scratch);
+    *err = std::string("BVH build failed: ") + cudaGetErrorString(e);
+    return -1;
+  }
+  if (refit_err != 0) {
+    cudaFree(scratch);
+    *err = "BVH build produced a malformed hierarchy";
+    return -1;
+  }
+  if (wide) {
+    std::vector<int2> h_ch((size_t)(n - 1));
+    std::vector<float4> h_nb((size_t)(n - 1) * 2), h_lb((size_t)n * 2), h_tris((size_t)n * 3);
+    std::vector<int> h_orig((size_t)n);
+    bool ok = cudaMemcpy(h_ch.data(), children, h_ch.size() * sizeof(int2), cudaMemcpyDeviceToHost) == cudaSuccess &&
+              cudaMemcpy(h_nb.data(), node_box, h_nb.size() * sizeof(float4), cudaMemcpyDeviceToHost) == cudaSuccess &&
+              cudaMemcpy(h_lb.data(), leaf_box, h_lb.size() * sizeof(float4), cudaMemcpyDeviceToHost) == cudaSuccess &&
+              cudaMemcpy(h_tris.data(), out->tris, h_tris.size() * sizeof(float4), cudaMemcpyDeviceToHost) ==
+                  cudaSuccess &&
+              cudaMemcpy(h_orig.data(), out->tri_orig, h_orig.size() * sizeof(int), cudaMemcpyDeviceToHost) ==
+                  cudaSuccess;
+    cudaFree(scratch);
+    if (!ok) { *err = "BVH collapse: device copy failed"; return -1; }
+    WideBuild wb;
+    collapse_wide(n, h_ch, h_nb, h_lb, &wb);
+    if ((int)wb.tri_perm.size() != n) { *err = "BVH collapse lost triangles"; return -1; }
+    std::vector<float4> p_tris((size_t)n * 3);
+    std::vector<int> p_orig((size_t)n);
+    for (int i = 0; i < n; ++i) {
+      const int s = wb.tri_perm[i];
+      p_tris[3 * i + 0] = h_tris[3 * s + 0];
+      p_tris[3 * i + 1] = h_tris[3 * s + 1];
+      p_tris[3 * i + 2] = h_tris[3 * s + 2];
+      p_orig[i] = h_orig[s];
+    }
+    out->num_wnodes = (int)(wb.words.size() / 20);
+    if (cudaMalloc(&out->wnodes, wb.words.size() * 4) != cudaSuccess ||
+        cudaMemcpy(out->wnodes, wb.words.data(), wb.words.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(out->tris, p_tris.data(), p_tris.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(out->tri_orig, p_orig.data(), p_orig.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+      *err = "out of device memory for the wide BVH";
+      return -1;
+    }
+    cudaFree(out->nodes);  // the binary nodes are not traversed in the wide form
+    out->nodes = nullptr;
+    return launches;
+  }
   cudaFree(scratch);
-  if (e != cudaSuccess) { *err = std::string("BVH build failed: ") + cudaGetErrorString(e); return -1; }
-  if (refit_err != 0) { *err = "BVH build produced a malformed hierarchy"; return -1; }
   return launches;
 }
 
 void bvh_free(DeviceBvh* b) {
   if (b->nodes) cudaFree(b->nodes);
+  if (b->wnodes) cudaFree(b->wnodes);
+  b->wnodes = nullptr;
   if (b->tris) cudaFree(b->tris);
   if (b->tri_orig) cudaFree(b->tri_orig);
   if (b->bounds_dev) cudaFree(b->bounds_dev);

@@ -162,6 +162,8 @@ void harvest_stage_events(msc_handle* h) {
 DevScene dev_scene(msc_handle* h) {
   DevScene s;
   s.nodes = h->bvh.nodes;
+  s.wnodes = h->bvh.wnodes;
+  s.num_wnodes = h->bvh.num_wnodes;
   s.tris = h->bvh.tris;
   s.tri_orig = h->bvh.tri_orig;
   s.num_tris = h->bvh.num_tris;
@@ -239,7 +241,7 @@ int setup(msc_handle* h) {
   CK(cudaMemcpy(d_g, tg.data(), tg.size() * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d_l, tl.data(), tl.size(), cudaMemcpyHostToDevice));
   std::string berr;
-  int bl = bvh_build(d_v, d_g, d_l, T, &h->bvh, h->stream, &berr);
+  int bl = bvh_build(d_v, d_g, d_l, T, d.ext.wide_bvh != 0, &h->bvh, h->stream, &berr);
   cudaFree(d_v);
   cudaFree(d_g);
   cudaFree(d_l);
@@ -350,7 +352,7 @@ int run_batch(msc_handle* h, const DevScene& sc, const DevFrame& fr, int base, i
     }
     {
       StageTimer t(h, MSC_STAGE_RAYSORT);
-      t.done(sort_pairs(h->keys, nullptr, h->keys_sorted, h->perm, nb, 32, h->ss, st));
+      t.done(sort_pairs(h->keys, nullptr, h->keys_sorted, h->perm, nb, 32, h->ss, st, h->small + 7));
     }
     StageTimer t(h, MSC_STAGE_GATHER);
     t.done(launch_gather(src, h->perm, nb, h->batch, st));
@@ -366,7 +368,7 @@ int run_batch(msc_handle* h, const DevScene& sc, const DevFrame& fr, int base, i
   if (h->desc.ext.hit_sort) {
     StageTimer t(h, MSC_STAGE_HITSORT);
     int l = launch_hit_keys(sc, h->hits, nb, h->hkeys, st);
-    l += sort_pairs(h->hkeys, nullptr, h->hkeys_sorted, h->hperm, nb, h->hit_bits, h->ss, st);
+    l += sort_pairs(h->hkeys, nullptr, h->hkeys_sorted, h->hperm, nb, h->hit_bits, h->ss, st, h->small + 7);
     t.done(l);
     order = h->hperm;
   }
@@ -422,9 +424,12 @@ int process_impl(msc_handle* h, int* iteration, bool copy_image) {
       if (!first_read) shadow_total += (uint64_t)h->h_small[6];
       first_read = false;
       if (h->h_small[7] != 0) {
-        h->err = (h->h_small[7] & ERR_BIN_OVERFLOW)    ? "a direction bin overflowed"
-                 : (h->h_small[7] & ERR_TRAVERSAL_CAP) ? "BVH traversal exceeded its step cap"
-                                                       : "BVH traversal stack overflowed";
+        const int e = h->h_small[7];
+        h->err = (e & ERR_BIN_OVERFLOW)    ? "a direction bin overflowed"
+                 : (e & ERR_TRAVERSAL_CAP) ? "BVH traversal exceeded its step cap"
+                 : (e & kSortErrLookback)  ? "radix sort look-back exceeded its spin cap"
+                 : (e & ERR_BVH_INDEX)     ? "BVH traversal met an out-of-range node or triangle index"
+                                           : "BVH traversal stack overflowed";
         return MSC_ERR_DEVICE;
       }
       if (h->terminate.load()) { aborted = true; break; }

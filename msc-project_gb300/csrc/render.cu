@@ -229,17 +229,47 @@ __global__ void __launch_bounds__(TB) k_gather(RayBuf src, const uint32_t* __res
 }
 
 // -------------------------------------------------------------- traversal
-__global__ void __launch_bounds__(128) k_trace_closest(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                       const float4* __restrict__ o, const float4* __restrict__ d, int n,
-                                                       float4* __restrict__ hits, int* err) {
+// The BVH a traversal kernel reads: WIDE selects the 8-wide quantised nodes,
+// else the binary node-pair layout.
+struct BvhRef {
+  const void* nodes;
+  const float4* tris;
+  int num_nodes;
+  int num_tris;
+};
+
+BvhRef bvh_ref(const DevScene& sc) {
+  BvhRef r;
+  r.nodes = sc.wnodes ? (const void*)sc.wnodes : (const void*)sc.nodes;
+  r.tris = sc.tris;
+  r.num_nodes = sc.num_wnodes;
+  r.num_tris = sc.num_tris;
+  return r;
+}
+
+template <bool WIDE, bool ANY>
+__device__ __forceinline__ bool scene_trace(const BvhRef& b, float3 o, float3 d, float tmin, float tmax, TriHit* h,
+                                            int* ovf) {
+  if (WIDE) return bvh8_trace<ANY>((const uint4*)b.nodes, b.tris, b.num_nodes, b.num_tris, o, d, tmin, tmax, h, ovf);
+  return bvh_trace<ANY>((const float4*)b.nodes, b.tris, o, d, tmin, tmax, h, ovf);
+}
+
+__device__ __forceinline__ int ovf_bits(int ovf) {
+  return ovf == 1 ? ERR_STACK_OVERFLOW : (ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_BVH_INDEX);
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(128) k_trace_closest(BvhRef bvh, const float4* __restrict__ o,
+                                                       const float4* __restrict__ d, int n, float4* __restrict__ hits,
+                                                       int* err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 ro = o[i], rd = d[i];
   TriHit h;
   h.t = MSC_TFAR; h.u = 0.f; h.v = 0.f; h.tri = -1;
   int ovf = 0;
-  bvh_trace<false>(nodes, tris, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
-  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+  scene_trace<WIDE, false>(bvh, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
+  if (ovf) atomicOr(err, ovf_bits(ovf));
   hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
@@ -447,29 +477,29 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
 
 // rtcOccluded with mask 0x0FFFFFFF (Integrator.cpp:153-174); an unoccluded
 // shadow ray adds its weighted contribution to its sample.
-__global__ void __launch_bounds__(128) k_trace_shadow(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                      ShadowBuf sh, const int* __restrict__ count, float4* sample_rgb,
-                                                      int* err) {
+template <bool WIDE>
+__global__ void __launch_bounds__(128) k_trace_shadow(BvhRef bvh, ShadowBuf sh, const int* __restrict__ count,
+                                                      float4* sample_rgb, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *count) return;
   const float4 o = sh.o[i], d = sh.d[i];
   TriHit h;
   int ovf = 0;
-  const bool blocked = bvh_trace<true>(nodes, tris, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
-  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+  const bool blocked = scene_trace<WIDE, true>(bvh, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
+  if (ovf) atomicOr(err, ovf_bits(ovf));
   if (!blocked) add_rgb(&sample_rgb[__float_as_int(d.w)], f3(sh.c[i]));
 }
 
-__global__ void __launch_bounds__(128) k_occluded(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                  const float4* __restrict__ o, const float4* __restrict__ d, int n,
-                                                  int* out, int* err) {
+template <bool WIDE>
+__global__ void __launch_bounds__(128) k_occluded(BvhRef bvh, const float4* __restrict__ o,
+                                                  const float4* __restrict__ d, int n, int* out, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 ro = o[i], rd = d[i];
   TriHit h;
   int ovf = 0;
-  out[i] = bvh_trace<true>(nodes, tris, f3(ro), f3(rd), MSC_TNEAR, ro.w, &h, &ovf) ? 1 : 0;
-  if (ovf) atomicOr(err, ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_STACK_OVERFLOW);
+  out[i] = scene_trace<WIDE, true>(bvh, f3(ro), f3(rd), MSC_TNEAR, ro.w, &h, &ovf) ? 1 : 0;
+  if (ovf) atomicOr(err, ovf_bits(ovf));
 }
 
 // ------------------------------------------------------------------ filters
@@ -572,7 +602,8 @@ int launch_gather(const RayBuf& src, const uint32_t* perm, int n, RayBuf dst, cu
 int launch_trace_closest(const DevScene& sc, const float4* o, const float4* d, int n, float4* hits, int* err,
                          cudaStream_t s) {
   if (n <= 0) return 0;
-  k_trace_closest<<<grid_for(n, 128), 128, 0, s>>>(sc.nodes, sc.tris, o, d, n, hits, err);
+  if (sc.wnodes) k_trace_closest<true><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, hits, err);
+  else k_trace_closest<false><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, hits, err);
   return 1;
 }
 
@@ -592,14 +623,18 @@ int launch_shade(const DevScene& sc, const DevFrame& f, const RayBuf& batch, con
 int launch_trace_shadow(const DevScene& sc, const ShadowBuf& sh, const int* sh_count, int max_n, float4* sample_rgb,
                         int* err, cudaStream_t s) {
   if (max_n <= 0) return 0;
-  k_trace_shadow<<<grid_for(max_n, 128), 128, 0, s>>>(sc.nodes, sc.tris, sh, sh_count, sample_rgb, err);
+  if (sc.wnodes)
+    k_trace_shadow<true><<<grid_for(max_n, 128), 128, 0, s>>>(bvh_ref(sc), sh, sh_count, sample_rgb, err);
+  else
+    k_trace_shadow<false><<<grid_for(max_n, 128), 128, 0, s>>>(bvh_ref(sc), sh, sh_count, sample_rgb, err);
   return 1;
 }
 
 int launch_occluded(const DevScene& sc, const float4* o, const float4* d, int n, int* occluded, int* err,
                     cudaStream_t s) {
   if (n <= 0) return 0;
-  k_occluded<<<grid_for(n, 128), 128, 0, s>>>(sc.nodes, sc.tris, o, d, n, occluded, err);
+  if (sc.wnodes) k_occluded<true><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, occluded, err);
+  else k_occluded<false><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, occluded, err);
   return 1;
 }
 

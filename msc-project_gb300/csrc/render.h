@@ -28,7 +28,9 @@ struct ShadowBuf {
 };
 
 struct DevScene {
-  const float4* nodes;
+  const float4* nodes;   // binary BVH (null when the 8-wide form is used)
+  const uint4* wnodes;   // 8-wide BVH (null for the binary form)
+  int num_wnodes;
   const float4* tris;
   const int* tri_orig;
   int num_tris;
@@ -53,7 +55,7 @@ struct DevFrame {
 };
 
 // Error bits reported through the engine's device flag word.
-enum : int { ERR_BIN_OVERFLOW = 1, ERR_STACK_OVERFLOW = 2, ERR_TRAVERSAL_CAP = 4 };
+enum : int { ERR_BIN_OVERFLOW = 1, ERR_STACK_OVERFLOW = 2, ERR_TRAVERSAL_CAP = 4, ERR_BVH_INDEX = 8 };
 
 constexpr int kMaxBins = 8;  // 6 cardinal bins + the dead bucket, rounded up
 

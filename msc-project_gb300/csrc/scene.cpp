@@ -668,6 +668,12 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
         else if (kv.first == "ray sort") { if (!as_int(&kv.second, &S.ext.ray_sort)) return c.fail("bad ray sort"); }
         else if (kv.first == "hit sort") { if (!as_int(&kv.second, &S.ext.hit_sort)) return c.fail("bad hit sort"); }
         else if (kv.first == "seed") { if (!as_int(&kv.second, &iv)) return c.fail("bad seed"); S.ext.seed = (uint32_t)iv; }
+        else if (kv.first == "bvh") {
+          std::string m = as_str(&kv.second);
+          if (m == "wide") S.ext.wide_bvh = 1;
+          else if (m == "binary") S.ext.wide_bvh = 0;
+          else return c.fail("bvh must be wide or binary");
+        }
         else if (kv.first == "paths per generation") { if (!as_int(&kv.second, &S.ext.generation) || S.ext.generation < 0) return c.fail("bad paths per generation"); }
         else return c.fail("unknown extension '" + kv.first + "'");
       }

@@ -106,6 +106,7 @@ struct Extensions {  // optional third YAML document; the reference ignores it
   int hit_sort = 1;        // sort hits on (geomID, primID)
   uint32_t seed = 0;       // mixes into every per-path draw
   int generation = 0;      // paths per camera generation (0 = automatic)
+  int wide_bvh = 1;        // 1: 8-wide quantised BVH, 0: binary LBVH
 };
 
 struct SceneDesc {

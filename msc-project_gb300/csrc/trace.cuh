@@ -132,4 +132,133 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
   }
 }
 
+// ------------------------------------------------------------ 8-wide BVH
+// Node = 5 uint4 (80 bytes):
+//   w0..w2  node box origin p (float bits)
+//   w3      per-axis step exponents e+127 (bits 0-23) and the internal-child mask (bits 24-31)
+//   w4      index of the first internal child node (internal children are consecutive)
+//   w5      index of the first leaf triangle (leaf triangles of a node are consecutive)
+//   w6, w7  one meta byte per slot: 0 empty or internal, else (count << 5) | triangle offset
+//   w8..w19 quantised child boxes, one byte per slot: lo.x, lo.y, lo.z, hi.x, hi.y, hi.z,
+//           two words each (slots 0-3, 4-7); child box = p + q * 2^e per axis.
+// Stack entries: a node index (>= 0) or ~(first triangle << 2 | count) for a leaf.
+constexpr int kWideStack = 128;
+
+__device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s) {
+  return ((s < 4 ? lo_word : hi_word) >> (8 * (s & 3))) & 0xffu;
+}
+
+// Node and triangle indices are checked against num_nodes / num_tris before
+// every fetch; a bad index ends the ray with *overflow = 3 instead of reading
+// outside the arrays.
+template <bool ANY>
+__device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const float4* __restrict__ tris,
+                                           int num_nodes, int num_tris, float3 o, float3 d, float tmin, float tmax,
+                                           TriHit* hit, int* overflow) {
+  const float3 id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  int stack[kWideStack];
+  int sp = 0;
+  int entry = 0;
+  bool found = false;
+  const float widen = 1.0000004f;
+  int steps = 0;
+  while (true) {
+    if (entry >= 0) {
+      if (++steps > kTraceStepCap) {
+        *overflow = 2;
+        return found;
+      }
+      if (entry >= num_nodes) {
+        *overflow = 3;
+        return found;
+      }
+      const uint4 A = __ldg(&wn[5 * entry + 0]);
+      const uint4 B = __ldg(&wn[5 * entry + 1]);
+      const uint4 Q0 = __ldg(&wn[5 * entry + 2]);
+      const uint4 Q1 = __ldg(&wn[5 * entry + 3]);
+      const uint4 Q2 = __ldg(&wn[5 * entry + 4]);
+      const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
+      const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
+      const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
+      const uint32_t imask = A.w >> 24;
+      const float ax = sx * id.x, ay = sy * id.y, az = sz * id.z;
+      const float bx = (__uint_as_float(A.x) - o.x) * id.x;
+      const float by = (__uint_as_float(A.y) - o.y) * id.y;
+      const float bz = (__uint_as_float(A.z) - o.z) * id.z;
+      float dist[8];
+      uint32_t hits = 0;
+#pragma unroll
+      for (int s = 0; s < 8; ++s) {
+        const bool valid = byte_of(B.z, B.w, s) != 0u || ((imask >> s) & 1u);
+        const float tlx = fmaf((float)byte_of(Q0.x, Q0.y, s), ax, bx);
+        const float tly = fmaf((float)byte_of(Q0.z, Q0.w, s), ay, by);
+        const float tlz = fmaf((float)byte_of(Q1.x, Q1.y, s), az, bz);
+        const float thx = fmaf((float)byte_of(Q1.z, Q1.w, s), ax, bx);
+        const float thy = fmaf((float)byte_of(Q2.x, Q2.y, s), ay, by);
+        const float thz = fmaf((float)byte_of(Q2.z, Q2.w, s), az, bz);
+        const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
+        const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), tmax)) * widen;
+        dist[s] = tn;
+        if (valid && tn <= tf) hits |= 1u << s;
+      }
+      if (hits == 0u) {
+        if (sp == 0) return found;
+        entry = stack[--sp];
+        continue;
+      }
+      // nearest hit child is visited next; the others go on the stack farthest first
+      int nearest = 0;
+      float nd = 3.0e38f;
+#pragma unroll
+      for (int s = 0; s < 8; ++s)
+        if (((hits >> s) & 1u) && dist[s] < nd) { nd = dist[s]; nearest = s; }
+      uint32_t rest = hits & ~(1u << nearest);
+      while (rest) {
+        int far = 0;
+        float fd = -1.0f;
+#pragma unroll
+        for (int s = 0; s < 8; ++s)
+          if (((rest >> s) & 1u) && dist[s] >= fd) { fd = dist[s]; far = s; }
+        rest &= ~(1u << far);
+        const uint32_t m = byte_of(B.z, B.w, far);
+        const int code = ((imask >> far) & 1u) ? (int)(B.x + __popc(imask & ((1u << far) - 1u)))
+                                                : ~(int)(((B.y + (m & 31u)) << 2) | (m >> 5));
+        if (sp < kWideStack) stack[sp++] = code;
+        else *overflow = 1;
+      }
+      {
+        const uint32_t m = byte_of(B.z, B.w, nearest);
+        entry = ((imask >> nearest) & 1u) ? (int)(B.x + __popc(imask & ((1u << nearest) - 1u)))
+                                          : ~(int)(((B.y + (m & 31u)) << 2) | (m >> 5));
+      }
+    } else {
+      const uint32_t code = (uint32_t)(~entry);
+      const int t0 = (int)(code >> 2);
+      const int cnt = (int)(code & 3u);
+      if (t0 + cnt > num_tris) {
+        *overflow = 3;
+        return found;
+      }
+      for (int k = t0; k < t0 + cnt; ++k) {
+        const float4 a = __ldg(&tris[3 * k + 0]);
+        const float4 b = __ldg(&tris[3 * k + 1]);
+        const float4 c = __ldg(&tris[3 * k + 2]);
+        if (ANY && __float_as_int(b.w) != 0) continue;
+        float t, u, v;
+        if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
+          found = true;
+          if (ANY) return true;
+          tmax = t;
+          hit->t = t;
+          hit->u = u;
+          hit->v = v;
+          hit->tri = k;
+        }
+      }
+      if (sp == 0) return found;
+      entry = stack[--sp];
+    }
+  }
+}
+
 }  // namespace mscg

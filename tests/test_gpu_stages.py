@@ -106,11 +106,26 @@ def _scene_rays(oracle_scene, rng, n):
     return org, d.astype(np.float32)
 
 
-def test_closest_hit_matches_oracle(built, box_scene):
+def _with_bvh(path, form, tmp_path):
+    """A copy of the scene YAML whose extension document selects the BVH form."""
+    import os
+    import shutil
+    d = os.path.dirname(path)
+    for f in os.listdir(d):
+        if f.endswith(".obj"):
+            shutil.copy(os.path.join(d, f), tmp_path / f)
+    text = open(path).read().replace("extensions:\n", "extensions:\n  bvh: %s\n" % form)
+    y = tmp_path / "scene.yaml"
+    y.write_text(text)
+    return str(y)
+
+
+@pytest.mark.parametrize("form", ["wide", "binary"])
+def test_closest_hit_matches_oracle(built, box_scene, form, tmp_path):
     mscgpu, oracle = built
     s = oracle.Scene(box_scene)
     org, d = _scene_rays(s, np.random.default_rng(11), 200000)
-    with mscgpu.Pathtracer(box_scene) as pt:
+    with mscgpu.Pathtracer(_with_bvh(box_scene, form, tmp_path)) as pt:
         t, u, v, g, p = pt.trace_closest(org, d)
     wt, wu, wv, wg, wp = s.trace(org, d)
     same = (g == wg) & (p == wp)
@@ -126,13 +141,14 @@ def test_closest_hit_matches_oracle(built, box_scene):
     assert (t[hit].view(np.uint32) == wt[hit].view(np.uint32)).mean() > 0.999
 
 
-def test_occlusion_matches_oracle(built, box_scene):
+@pytest.mark.parametrize("form", ["wide", "binary"])
+def test_occlusion_matches_oracle(built, box_scene, form, tmp_path):
     mscgpu, oracle = built
     s = oracle.Scene(box_scene)
     rng = np.random.default_rng(12)
     org, d = _scene_rays(s, rng, 100000)
     tmax = rng.uniform(0.01, 3.0, size=org.shape[0]).astype(np.float32)
-    with mscgpu.Pathtracer(box_scene) as pt:
+    with mscgpu.Pathtracer(_with_bvh(box_scene, form, tmp_path)) as pt:
         got = pt.trace_occluded(org, d, tmax)
     want = s.occluded(org, d, tmax)
     assert (got != want).mean() < 1e-3
