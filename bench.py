@@ -133,6 +133,128 @@ def cpu_baseline(yaml, seconds=15.0, threads=0):
                       % (n, first, first + n - 1, rays, dt)}
 
 
+def scene_set(n, lo_tris, hi_tris, seed):
+    """n scenes by the terrain rules with triangle counts log-uniform in [lo, hi]."""
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        target = math.exp(rng.uniform(math.log(lo_tris), math.log(hi_tris)))
+        # tris(s) ~ 2 (1024 s)^2 + 300 s * 5120
+        a, b = 2.0 * 1024 * 1024, 300 * 5120.0
+        s = (-b + math.sqrt(b * b + 4 * a * target)) / (2 * a)
+        s = min(1.0, max(0.01, s))
+        out.append(make_scene_scaled(1, seed + 17 * i, round(s, 4)))
+    return out
+
+
+def make_scene_scaled(config, seed, scale):
+    import mscgpu
+    d = os.path.join(tempfile.gettempdir(), "msc_bench_scenes", "c%d_s%d_%g" % (config, seed, scale))
+    y = os.path.join(d, "scene.yaml")
+    if not os.path.exists(y):
+        y = mscgpu.generate_scene(config, seed, d, scale=scale)
+    return y
+
+
+def sphere_camera(rng, bbox, fov_lo=30.0, fov_hi=70.0):
+    """A pinhole on the scene's bounding sphere looking at its centre (PinHoleCamera fields)."""
+    import math
+    import numpy as np
+    lo, hi = bbox
+    c = 0.5 * (lo + hi)
+    r = 0.6 * float(np.linalg.norm(hi - lo))
+    v = rng.normal(size=3)
+    v[1] = abs(v[1]) + 0.3  # from above the horizon
+    v /= np.linalg.norm(v)
+    eye = c + r * v
+    fwd = (c - eye) / np.linalg.norm(c - eye)
+    fov = rng.uniform(fov_lo, fov_hi)
+    focal = 36.0 / math.tan(math.radians(fov) / 2)
+    rz = math.degrees(math.asin(max(-1.0, min(1.0, fwd[1]))))
+    ry = math.degrees(math.atan2(-fwd[2], fwd[0]))
+    t = eye - fwd * focal  # the pinhole sits at translation + normal * focal length
+    return (tuple(float(x) for x in t), (0.0, ry, rz), focal)
+
+
+def random_jobs(rng, scenes_bboxes, n, res_choices, spp_lo, spp_hi, depth_lo, depth_hi):
+    jobs = []
+    for _ in range(n):
+        s = int(rng.integers(0, len(scenes_bboxes)))
+        res = int(rng.choice(res_choices))
+        jobs.append(dict(scene=s, width=res, height=res, spp=int(rng.integers(spp_lo, spp_hi + 1)),
+                         min_depth=3, max_depth=int(rng.integers(depth_lo, depth_hi + 1)),
+                         camera=sphere_camera(rng, scenes_bboxes[s]), seed=int(rng.integers(1, 1 << 30))))
+    return jobs
+
+
+def bench_forms(args):
+    """Batched and served forms against the one-job-at-a-time loop on the same jobs."""
+    import mscgpu
+    import numpy as np
+    t = time.time()
+    scenes = scene_set(16, 1e4, 1e6, SEED + 300)
+    bboxes = []
+    for y in scenes:
+        _, tv, _ = mscgpu.scene_load_host(y)
+        p = tv.reshape(-1, 3)
+        bboxes.append((p.min(0), p.max(0)))
+    log("batched/served scene set ready in %.1f s" % (time.time() - t))
+    rng = np.random.default_rng(SEED + 301)
+    jobs = random_jobs(rng, bboxes, 48, [128, 256, 512], 4, 32, 4, 10)
+    film = int(sum(j["width"] * j["height"] * j["spp"] for j in jobs)) + 1
+
+    def new_batch(max_active=0, film_samples=film):
+        b = mscgpu.Batch(batch_exponent=20, film_samples=film_samples)
+        for y in scenes:
+            b.add_scene(y)
+        if max_active:
+            b.set_max_active(max_active)
+        return b
+
+    out = {}
+    # batched: every job in one wavefront
+    b = new_batch()
+    for j in jobs:
+        b.submit(**j)
+    t = time.time()
+    b.run()
+    wall = time.time() - t
+    st = b.stats()
+    rays = st["closest_queries"] + st["shadow_queries"]
+    b.close()
+    # the plain per-job loop on the same jobs: one job in flight at a time
+    p = new_batch(max_active=1)
+    res, pst = p.serve([(0.0, j) for j in jobs])
+    p.close()
+    plain_rate = (pst["closest_queries"] + pst["shadow_queries"]) / pst["wall_s"] / 1e6
+    out["batched"] = {"workload": "%d jobs on 16 resident terrain scenes (1e4-1e6 tris, log-uniform), "
+                                  "128^2-512^2, 4-32 spp, depth 4-10, cameras on the bounding sphere" % len(jobs),
+                      "mrays_per_s": rays / wall / 1e6, "wall_s": wall,
+                      "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
+                      "speedup_vs_per_job_loop": (rays / wall / 1e6) / plain_rate if plain_rate else None}
+    # served: Poisson arrivals, admission by film memory
+    rate, dur = args.serve_rate, args.serve_seconds
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 1.5)))
+    arrivals = arrivals[arrivals < dur]
+    reqs = [(float(a), j) for a, j in zip(arrivals, random_jobs(rng, bboxes, len(arrivals), [128, 256], 4, 16, 4,
+                                                                    10))]
+    budget = 1 << 25
+    for label, max_active in (("served", 0), ("served_per_job_loop", 1)):
+        s = new_batch(max_active=max_active, film_samples=budget)
+        res, sst = s.serve(reqs)
+        s.close()
+        out[label] = {"requests": len(reqs), "rate_per_s": rate, "seconds": dur,
+                      "film_budget_samples": budget, "completed": sst["completed"],
+                      "mrays_per_s": sst["mrays_per_s"], "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
+                      "p999_ms": 1e3 * sst["p999_s"], "wall_s": sst["wall_s"]}
+    out["served"]["workload"] = ("Poisson %g req/s for %g s on the 16 resident scenes, 128^2-256^2, 4-16 spp, "
+                                 "depth 4-10, cameras on the bounding sphere, film budget %d samples"
+                                 % (rate, dur, budget))
+    return out
+
+
 def run_reference(args, yaml, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -177,6 +299,9 @@ def main():
     ap.add_argument("--config", type=int, default=1, help="scene config (1: large terrain scene, 0: box)")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -257,6 +382,9 @@ def main():
                    "d2h_bytes_per_step": int(img.nbytes + 32 * batches / args.steps)},
            "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks.summary(),
            "wall_ms_per_step": 1e3 * sum(wall) / args.steps}
+    out["batches_per_step"] = batches / args.steps
+    if not args.no_forms:
+        out["forms"] = bench_forms(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(yaml)
     print(json.dumps(out), flush=True)

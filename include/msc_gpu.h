@@ -146,6 +146,66 @@ int msc_trace_closest(msc_handle* h, const float* org, const float* dir, int n, 
 int msc_trace_occluded(msc_handle* h, const float* org, const float* dir, const float* tmax, int n,
                        int32_t* occluded);
 
+/* ---- batched form: many resident scenes and jobs in one wavefront ----
+ * No counterpart in the reference, which renders one scene per process.  A
+ * job is a resident scene seen through one camera at one resolution and
+ * sample count; the rays of all submitted jobs share bins, sorted batches and
+ * kernels.  Each job's image equals the image it gets when rendered alone. */
+typedef struct msc_batch msc_batch;
+
+typedef struct msc_job_desc {
+  int scene;                  /* id from msc_batch_add_scene */
+  int width, height, spp;     /* 0: the scene's own (spp other than base^2 allowed) */
+  int min_depth, max_depth;   /* -1: the scene's own */
+  int use_camera;             /* 1: the pinhole camera below replaces the scene's */
+  float translation[3], rotation[3], focal_length;  /* PinHoleCamera fields (PinHoleCamera.h:98-113) */
+  uint32_t seed;              /* 0: the scene's */
+} msc_job_desc;
+
+/* batch_exponent: rays per sorted batch (2^e); film_samples: capacity of the
+ * shared per-sample film (sum of width*height*spp over jobs in flight). */
+int msc_batch_create(int batch_exponent, int64_t film_samples, msc_batch** out);
+int msc_batch_destroy(msc_batch* b);
+const char* msc_batch_last_error(msc_batch* b);
+int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id);
+/* MSC_ERR_BUSY when the job's film does not fit in the free film capacity. */
+int msc_batch_submit(msc_batch* b, const msc_job_desc* desc, int* job_id);
+/* Renders every submitted job to completion in one merged wavefront. */
+int msc_batch_run(msc_batch* b);
+int msc_batch_job_image(msc_batch* b, int job, const float** rgb, int* width, int* height);
+/* Frees a finished job's film for new submissions. */
+int msc_batch_release_job(msc_batch* b, int job);
+int msc_batch_get_stats(msc_batch* b, msc_stats* out);
+int msc_batch_set_profiling(msc_batch* b, int on);
+/* At most n jobs admitted at once (0 = no limit).  n = 1 renders one job at a
+ * time: the plain per-job loop the batched and served forms are compared with. */
+int msc_batch_set_max_active(msc_batch* b, int n);
+
+/* ---- served form: requests admitted as they arrive and as film frees up ---- */
+typedef struct msc_request {
+  double arrival_s;           /* seconds after the call starts */
+  msc_job_desc job;
+} msc_request;
+
+typedef struct msc_request_result {
+  int job_id;
+  int status;                 /* 0 done, negative: the submit error */
+  double admit_s, done_s, latency_s;  /* latency = done - arrival */
+} msc_request_result;
+
+typedef struct msc_serve_stats {
+  int completed;
+  double wall_s, p50_s, p99_s, p999_s, mrays_per_s;
+  uint64_t closest_queries, shadow_queries;
+  int64_t peak_film_samples;
+} msc_serve_stats;
+
+/* Runs the request stream in real time on the batch object's resident scenes:
+ * arrived requests are admitted in arrival order whenever their film fits;
+ * admitted jobs share the wavefront; a finished job's image is copied to the
+ * host and its film released.  Images stay readable with msc_batch_job_image. */
+int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* results, msc_serve_stats* stats);
+
 /* ---- host-only scene input (no GPU needed) ---- */
 
 /* OBJ reading with tinyobjloader's rules (thirdparty/tinyobjloader/tiny_obj_loader.cpp:309-412,

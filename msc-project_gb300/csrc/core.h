@@ -1,0 +1,160 @@
+// The render core shared by the plain, batched and served forms.
+//
+// Resident scenes (BVH + tables) and jobs (a scene seen through one camera at
+// one resolution and sample count) live in device tables.  The core runs one
+// wavefront over the rays of every admitted job:
+//   top up: camera rays of admitted jobs are generated while fewer than one
+//           generation of paths is in flight, and partitioned into the six
+//           cardinal bins (the reference's DirectionalBins)
+//   batch:  up to 2^bin_exponent rays from the fullest bins -> origin box ->
+//           ray keys -> radix sort -> gather -> closest hit -> hit keys ->
+//           hit sort -> shade -> occlusion + accumulate -> partition into bins
+//   finish: a job whose paths are all generated and ended is filtered into
+//           its image (pixels += tent/box filter of its samples)
+// step() performs one top-up or one batch; the drivers in engine.cu loop it.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/msc_gpu.h"
+#include "bvh.h"
+#include "radix.cuh"
+#include "render.h"
+#include "scene.h"
+
+namespace mscg {
+
+struct SceneGPU {
+  SceneDesc desc;
+  DeviceBvh bvh;
+  ShaderRec* d_shaders = nullptr;
+  GeomRec* d_geoms = nullptr;
+  LightRec* d_lights = nullptr;
+  std::vector<int> h_tri_orig;  // leaf order -> global triangle index
+  SceneRec rec;
+  ~SceneGPU();
+};
+
+struct JobSpec {          // what a caller asks for; the scene's own setup fills the rest
+  int scene = 0;
+  int width = 0, height = 0, spp = 0;  // 0: the scene's
+  int min_depth = -1, max_depth = -1;  // -1: the scene's
+  int use_camera = 0;                  // 1: pinhole camera below instead of the scene's
+  float cam_translation[3] = {0, 0, 0};
+  float cam_rotation[3] = {0, 0, 0};
+  float cam_focal = 0.f;
+  uint32_t seed = 0;                   // 0: the scene's extension seed
+  int iteration = 0;
+};
+
+struct JobState {
+  JobRec rec;
+  int slot = -1;
+  uint64_t paths = 0, generated = 0, done = 0;
+  size_t sample_off = 0, sample_len = 0;
+  float* d_pixels = nullptr;
+  std::vector<float> h_pixels;
+  bool complete = false;
+  bool image_on_host = false;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+};
+
+struct CoreStats {
+  uint64_t closest = 0, shadow = 0, batches = 0, launches = 0, generations = 0;
+  double stage_ms[12] = {0};
+  uint64_t stage_launches[12] = {0};
+};
+
+class Core {
+ public:
+  std::string err;
+  CoreStats stats;
+  bool profiling = false;
+  bool ray_sort = true, hit_sort = true;
+  bool merge_bins = true;  // let a batch take rays of several bins when the fullest is short
+  int max_active = 0;      // jobs admitted at once (0 = no limit); 1 gives the one-job-at-a-time loop
+
+  ~Core();
+  // batch_exponent: rays per batch (2^e); generation: paths in flight; samples: film capacity.
+  int init(int batch_exponent, int generation, size_t sample_capacity, bool wide);
+  int add_scene(const SceneDesc& d, int* id);
+  // Admits a job if its film fits; returns MSC_ERR_BUSY when it does not (yet).
+  int add_job(const JobSpec& spec, int* id);
+  // Starts the next iteration of a finished job (same film, next random sequence).
+  int restart_job(int id);
+  int remove_job(int id);
+  // One top-up or one batch; *idle = true when no work was left.
+  int step(bool* idle);
+  // Steps until every admitted job is complete (or `stop` becomes true).
+  int run_all(const volatile bool* stop = nullptr);
+  int copy_image(int id);
+  cudaStream_t stream() const { return stream_; }
+  JobState* job(int id) { return (id >= 0 && id < (int)jobs_.size()) ? jobs_[id].get() : nullptr; }
+  SceneGPU* scene(int id) { return (id >= 0 && id < (int)scenes_.size()) ? scenes_[id].get() : nullptr; }
+  int num_scenes() const { return (int)scenes_.size(); }
+  size_t samples_free() const;
+  size_t sample_capacity() const { return sample_cap_; }
+  Film film() const { return film_; }
+  int batch_cap() const { return batch_cap_; }
+  double now() const;
+  // Closest hit / occlusion of explicit rays against scene 0 (stage entry points).
+  int trace_closest(const float* org, const float* dir, int n, float4* hits_host);
+  int trace_occluded(const float* org, const float* dir, const float* tmax, int n, int* occluded);
+
+ private:
+  int run_batch(const Segments& seg, int nb, int prefix_bits);
+  int finish_job(JobState& j);
+  int generate(bool* did);
+  bool alloc_samples(size_t n, size_t* off);
+  void free_samples(size_t off, size_t n);
+  void harvest();
+
+  cudaStream_t stream_ = nullptr;
+  bool wide_ = true;
+  int batch_cap_ = 0, generation_ = 0, staging_cap_ = 0;
+  std::vector<std::unique_ptr<SceneGPU>> scenes_;
+  std::vector<std::unique_ptr<JobState>> jobs_;
+  std::vector<int> free_slots_;
+  int max_slot_ = -1;
+  uint32_t total_tris_ = 0;
+  int hit_bits_ = 1;
+  SceneRec* d_scenes_ = nullptr;
+  SceneRec* h_scenes_ = nullptr;  // pinned mirror
+  JobRec* d_jobs_ = nullptr;
+  JobRec* h_jobs_ = nullptr;      // pinned mirror
+  uint32_t* d_job_done_ = nullptr;
+  uint32_t* h_job_done_ = nullptr;
+  // film pool
+  Film film_;
+  size_t sample_cap_ = 0;
+  std::vector<std::pair<size_t, size_t>> free_ranges_;  // (offset, length), sorted
+  // wavefront buffers
+  char* arena_ = nullptr;
+  BinPool bins_;
+  RayBuf staging_, batch_;
+  uint32_t *keys_ = nullptr, *keys_sorted_ = nullptr, *perm_ = nullptr, *hkeys_ = nullptr, *hkeys_sorted_ = nullptr,
+           *hperm_ = nullptr, *box6_ = nullptr;
+  SortScratch ss_;
+  float4* hits_ = nullptr;
+  ShadowBuf shadow_;
+  int* small_ = nullptr;   // [0..5] bin counts, [6] shadow count, [7] error bits
+  int* h_small_ = nullptr;
+  int* h_counts_up_ = nullptr;
+  bool last_was_batch_ = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> stage_events_;
+  std::vector<cudaEvent_t> event_pool_;
+  size_t event_used_ = 0;
+  friend struct StageClock;
+  cudaEvent_t pool_event();
+};
+
+// Device job record for a scene's own setup document (PinHole/ThinLens camera,
+// sampler, filter, depth limits) overridden by the spec.
+JobRec job_record(const SceneDesc& d, const JobSpec& spec, int scene_id);
+
+}  // namespace mscg

@@ -1,5 +1,8 @@
-// Device stages of one render iteration.  Each kernel cites the reference
-// code whose arithmetic it restates.
+// Device stages of the render loop.  Each kernel cites the reference code
+// whose arithmetic it restates.  Every ray carries its job and scene in its
+// info word, so a batch may mix jobs over several resident scenes.
+#include <algorithm>
+
 #include "radix.cuh"
 #include "render.h"
 #include "trace.cuh"
@@ -19,6 +22,15 @@ __device__ __forceinline__ float ord2f(uint32_t u) {
   return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
+// samples[i].rgb += v (one writer per sample within a batch, so no atomics)
+__device__ __forceinline__ void add_rgb(float4* p, float3 v) {
+  float4 c = *p;
+  c.x += v.x;
+  c.y += v.y;
+  c.z += v.z;
+  *p = c;
+}
+
 __device__ __forceinline__ float mis_weight(float a, float b, int power) {
   if (power) {  // power heuristic, beta = 2
     float a2 = a * a;
@@ -27,13 +39,22 @@ __device__ __forceinline__ float mis_weight(float a, float b, int power) {
   return a / (a + b);  // misBalance, include/core/Common.h:45-48
 }
 
+// Position of batch ray i in the bin pool.
+__device__ __forceinline__ int seg_source(const Segments& seg, int i) {
+  int s = 0;
+#pragma unroll
+  for (int k = 1; k < 6; ++k)
+    if (k < seg.count && i >= seg.prefix[k]) s = k;
+  return seg.start[s] + (i - seg.prefix[s]);
+}
+
 // ------------------------------------------------------------------ raygen
 // Camera::operator() (src/core/Camera.cpp:6-59) with StratifiedSampler
 // (src/core/StratifiedSampler.cpp:5-17), IndependentSampler, GridSampler and
 // PinHoleCamera::sample (src/core/PinHoleCamera.cpp:16-32) /
 // ThinLensCamera::sample (src/core/ThinLensCamera.cpp:16-56).
-// sampleID = x*H*spp + y*spp + i (Camera.cpp:28).
-__global__ void __launch_bounds__(TB) k_raygen(DevFrame f, uint32_t first, int n, RayBuf out) {
+// sampleID = x*H*spp + y*spp + i (Camera.cpp:28), local to the job.
+__global__ void __launch_bounds__(TB) k_raygen(JobRec f, int job_index, uint32_t first, int n, RayBuf out, Film film) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const uint32_t sid = first + (uint32_t)t;
@@ -57,8 +78,8 @@ __global__ void __launch_bounds__(TB) k_raygen(DevFrame f, uint32_t first, int n
     sy = (float)iy * celly + u01(r.y) * celly;
   }
   const float px = (float)x + sx, py = (float)y + sy;
-  f.sample_rgb[sid] = make_float4(0.f, 0.f, 0.f, 0.f);
-  f.sample_pos[sid] = make_float2(px, py);
+  film.rgb[f.sample_base + sid] = make_float4(0.f, 0.f, 0.f, 0.f);
+  film.pos[f.sample_base + sid] = make_float2(px, py);
   const float W = (float)f.width, H = (float)f.height;
   const float fx = ((px * 2.f - W) / W) * 36.f;
   const float fy = ((py * 2.f - H) / W) * 36.f;
@@ -66,15 +87,15 @@ __global__ void __launch_bounds__(TB) k_raygen(DevFrame f, uint32_t first, int n
   const float3 cn = f3(c.normal[0], c.normal[1], c.normal[2]);
   const float3 ct = f3(c.translation[0], c.translation[1], c.translation[2]);
   const float3 nodal = v_add(ct, v_mul(cn, c.focal_length));
-  const float3 film = xf_point(c.xf, f3(0.f, fy, fx));
+  const float3 fp = xf_point(c.xf, f3(0.f, fy, fx));
   float3 org, dir;
   if (c.type == CAMERA_THINLENS) {
     const float ratio = c.focal_distance / c.focal_length;
-    const float3 focal = v_add(film, v_mul(v_sub(nodal, film), ratio));
-    // rejection sampling of the unit-diameter disc, two draws per attempt
+    const float3 focal = v_add(fp, v_mul(v_sub(nodal, fp), ratio));
+    // rejection sampling of the unit-diameter disc: attempt 0 uses draws 2,3
+    // of the camera block; attempt k >= 1 uses block 1 + k/2 (draws 0,1 for
+    // odd k, 2,3 for even k)
     float ax = 0.f, ay = 0.f;
-    // attempt 0 uses draws 2,3 of the camera block; attempt k >= 1 uses
-    // block 1 + k/2 (draws 0,1 for odd k, 2,3 for even k)
     uint4 q = r;
     for (int attempt = 0; attempt < 64; ++attempt) {
       uint32_t a, b;
@@ -95,10 +116,10 @@ __global__ void __launch_bounds__(TB) k_raygen(DevFrame f, uint32_t first, int n
     dir = v_normalize(v_sub(focal, org));
   } else {
     org = nodal;
-    dir = v_normalize(v_sub(nodal, film));
+    dir = v_normalize(v_sub(nodal, fp));
   }
   out.o[t] = make_float4(org.x, org.y, org.z, 1.f);
-  out.d[t] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0));
+  out.d[t] = make_float4(dir.x, dir.y, dir.z, __int_as_float(ray_info(job_index, f.scene, 0)));
   out.w[t] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)sid));
 }
 
@@ -187,10 +208,11 @@ __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict_
 
 // ------------------------------------------------------------ ray keys
 // RayBoundingbox (src/core/RayBoundingbox.cpp:5-50): origin box of the batch.
-__global__ void k_origin_box(const float4* __restrict__ o, int n, uint32_t* box6) {
+__global__ void k_origin_box(const float4* __restrict__ o, Segments seg, uint32_t* box6) {
+  const int n = seg.prefix[seg.count];
   float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 p = o[i];
+    float4 p = o[seg_source(seg, i)];
     mn[0] = fminf(mn[0], p.x); mn[1] = fminf(mn[1], p.y); mn[2] = fminf(mn[2], p.z);
     mx[0] = fmaxf(mx[0], p.x); mx[1] = fmaxf(mx[1], p.y); mx[2] = fmaxf(mx[2], p.z);
   }
@@ -207,30 +229,41 @@ __global__ void k_origin_box(const float4* __restrict__ o, int n, uint32_t* box6
     }
 }
 
-__global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d, int n,
-                                                 const uint32_t* __restrict__ box6, uint32_t* __restrict__ keys) {
+__global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d,
+                                                 Segments seg, const uint32_t* __restrict__ box6, int prefix_bits,
+                                                 uint32_t* __restrict__ keys) {
+  const int n = seg.prefix[seg.count];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const int src = seg_source(seg, i);
   float3 lo = f3(ord2f(box6[0]), ord2f(box6[1]), ord2f(box6[2]));
   float3 hi = f3(ord2f(box6[3]), ord2f(box6[4]), ord2f(box6[5]));
   float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
   float3 sc = f3(ex > 0.f ? 64.0f / ex : 0.f, ey > 0.f ? 64.0f / ey : 0.f, ez > 0.f ? 64.0f / ez : 0.f);
-  keys[i] = ray_sort_key(f3(o[i]), f3(d[i]), lo, sc);
+  const float4 dd = d[src];
+  uint32_t key = ray_sort_key(f3(o[src]), f3(dd), lo, sc);
+  if (prefix_bits > 0) {
+    const uint32_t prefix = ((uint32_t)info_scene(__float_as_int(dd.w)) << 3) | (uint32_t)cardinal_bin(f3(dd));
+    key = (prefix << (32 - prefix_bits)) | (key >> prefix_bits);
+  }
+  keys[i] = key;
 }
 
 // RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
-__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const uint32_t* __restrict__ perm, int n, RayBuf dst) {
+__global__ void __launch_bounds__(TB) k_gather(RayBuf src, Segments seg, const uint32_t* __restrict__ perm,
+                                               RayBuf dst) {
+  const int n = seg.prefix[seg.count];
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  int i = perm ? (int)perm[j] : j;
+  const int i = seg_source(seg, perm ? (int)perm[j] : j);
   dst.o[j] = src.o[i];
   dst.d[j] = src.d[i];
   dst.w[j] = src.w[i];
 }
 
 // -------------------------------------------------------------- traversal
-// The BVH a traversal kernel reads: WIDE selects the 8-wide quantised nodes,
-// else the binary node-pair layout.
+// The BVH one ray reads: the 8-wide quantised nodes (WIDE) or the binary
+// node-pair layout.
 struct BvhRef {
   const void* nodes;
   const float4* tris;
@@ -238,9 +271,9 @@ struct BvhRef {
   int num_tris;
 };
 
-BvhRef bvh_ref(const DevScene& sc) {
+__host__ __device__ __forceinline__ BvhRef bvh_of(const SceneRec& sc, bool wide) {
   BvhRef r;
-  r.nodes = sc.wnodes ? (const void*)sc.wnodes : (const void*)sc.nodes;
+  r.nodes = wide ? (const void*)sc.wnodes : (const void*)sc.nodes;
   r.tris = sc.tris;
   r.num_nodes = sc.num_wnodes;
   r.num_tris = sc.num_tris;
@@ -258,30 +291,38 @@ __device__ __forceinline__ int ovf_bits(int ovf) {
   return ovf == 1 ? ERR_STACK_OVERFLOW : (ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_BVH_INDEX);
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(128) k_trace_closest(BvhRef bvh, const float4* __restrict__ o,
-                                                       const float4* __restrict__ d, int n, float4* __restrict__ hits,
-                                                       int* err) {
+// MULTI: look each ray's scene up in the table; else every ray uses scene0.
+template <bool WIDE, bool MULTI>
+__global__ void __launch_bounds__(128) k_trace_closest(const SceneRec* __restrict__ scenes, BvhRef scene0,
+                                                       const float4* __restrict__ o, const float4* __restrict__ d, int n,
+                                                       float4* __restrict__ hits, int* err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 ro = o[i], rd = d[i];
+  const BvhRef b = MULTI ? bvh_of(scenes[info_scene(__float_as_int(rd.w))], WIDE) : scene0;
   TriHit h;
   h.t = MSC_TFAR; h.u = 0.f; h.v = 0.f; h.tri = -1;
   int ovf = 0;
-  scene_trace<WIDE, false>(bvh, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
+  scene_trace<WIDE, false>(b, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
   if (ovf) atomicOr(err, ovf_bits(ovf));
   hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
 // CompareHit key (include/core/RayUncompressed.h:63-69): (geomID, primID) with
-// misses first.  Triangles are numbered geomID-major, so the global triangle
-// index + 1 orders exactly like (geomID, primID), and 0 is a miss.
-__global__ void __launch_bounds__(TB) k_hit_keys(const int* __restrict__ tri_orig, const float4* __restrict__ hits,
-                                                 int n, uint32_t* __restrict__ keys) {
+// misses first.  Triangles are numbered geomID-major within a scene and scenes
+// follow each other, so tri_base + global triangle index + 1 orders exactly
+// like (scene, geomID, primID), and 0 is a miss.
+__global__ void __launch_bounds__(TB) k_hit_keys(const SceneRec* __restrict__ scenes, const float4* __restrict__ d,
+                                                 const float4* __restrict__ hits, int n, uint32_t* __restrict__ keys) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int k = __float_as_int(hits[i].w);
-  keys[i] = k < 0 ? 0u : (uint32_t)tri_orig[k] + 1u;
+  if (k < 0) {
+    keys[i] = 0u;
+    return;
+  }
+  const SceneRec& sc = scenes[info_scene(__float_as_int(d[i].w))];
+  keys[i] = sc.tri_base + (uint32_t)sc.tri_orig[k] + 1u;
 }
 
 // ------------------------------------------------------------------ shading
@@ -330,31 +371,32 @@ __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z)
   return v_add(v_add(v_mul(t, x), v_mul(s, y)), v_mul(a, z));
 }
 
-__device__ __forceinline__ void add_rgb(float4* p, float3 v) {
-  float4 c = *p;
-  c.x += v.x;
-  c.y += v.y;
-  c.z += v.z;
-  *p = c;
-}
-
 // Integrator::operator() (src/core/Integrator.cpp:12-255), one hit per thread.
-__global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf batch, const float4* __restrict__ hits,
+// job_done[j] counts the finished paths of job j.
+__global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
+                                              Film film, RayBuf batch, const float4* __restrict__ hits,
                                               const uint32_t* __restrict__ order, int n, RayBuf next, ShadowBuf sh,
-                                              int* sh_count) {
+                                              int* sh_count, uint32_t* job_done) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = j < n;
   bool emit = false, cont = false;
+  int job = -1;
   float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sd = so, scol = so;
   float4 no = so, nd = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), nw = so;
   if (live) {
     const int i = order ? (int)order[j] : j;
     const float4 ro = batch.o[i], rd = batch.d[i], rw = batch.w[i], h = hits[i];
     const int k = __float_as_int(h.w);
-    const int depth = __float_as_int(rd.w);
+    const int info = __float_as_int(rd.w);
+    job = info_job(info);
+    const int scene = info_scene(info);
+    const int depth = info_depth(info);
     const int sid = __float_as_int(rw.w);
+    const JobRec& f = jobs[job];
+    const uint32_t sample = f.sample_base + (uint32_t)sid;
     const float3 w = f3(rw);
     if (k >= 0) {  // a miss adds nothing (Integrator.cpp:26-27)
+      const SceneRec& sc = scenes[scene];
       const float4 ta = __ldg(&sc.tris[3 * k + 0]);
       const float4 tb = __ldg(&sc.tris[3 * k + 1]);
       const float4 tc = __ldg(&sc.tris[3 * k + 2]);
@@ -374,7 +416,7 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
           const float pdfw = pdfa * (t * t) / fabsf(cosl);
           mis = mis_weight(ro.w, pdfw * sc.light_pick, f.mis_power);
         }
-        if (le > MSC_EPSILON) add_rgb(&f.sample_rgb[sid], f3(le * mis * w.x, le * mis * w.y, le * mis * w.z));
+        if (le > MSC_EPSILON) add_rgb(&film.rgb[sample], f3(le * mis * w.x, le * mis * w.y, le * mis * w.z));
       } else {
         const float3 nrm = v_normalize(v_cross(f3(tb), f3(tc)));  // = -normalize(Ng) (Integrator.cpp:121-125)
         const float3 pos = v_add(f3(ro), v_mul(dn, t));
@@ -404,8 +446,8 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
               const float3 c = f3(k0 * (le * e.f.x), k0 * (le * e.f.y), k0 * (le * e.f.z));
               emit = true;
               so = make_float4(pos.x, pos.y, pos.z, dist);
-              sd = make_float4(wi.x, wi.y, wi.z, __int_as_float(sid));
-              scol = make_float4(c.x * w.x, c.y * w.y, c.z * w.z, 0.f);
+              sd = make_float4(wi.x, wi.y, wi.z, __int_as_float((int)sample));
+              scol = make_float4(c.x * w.x, c.y * w.y, c.z * w.z, __int_as_float(scene));
             }
           }
         }
@@ -444,7 +486,7 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
               const float g0 = e.cos_theta / e.pdf;
               cont = true;
               no = make_float4(pos.x, pos.y, pos.z, e.pdf);
-              nd = make_float4(wi.x, wi.y, wi.z, __int_as_float(depth + 1));
+              nd = make_float4(wi.x, wi.y, wi.z, __int_as_float(ray_info(job, scene, depth + 1)));
               nw = make_float4(((w.x * e.f.x) * g0) / q, ((w.y * e.f.y) * g0) / q, ((w.z * e.f.z) * g0) / q,
                                __int_as_float(sid));
             }
@@ -453,10 +495,10 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
       }
     }
   }
+  const int lane = threadIdx.x & 31;
   // warp-aggregated append of shadow rays
   const unsigned m = __ballot_sync(0xffffffffu, emit);
   if (m) {
-    const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
     int base = 0;
     if (lane == leader) base = atomicAdd(sh_count, __popc(m));
@@ -468,6 +510,10 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
       sh.c[slot] = scol;
     }
   }
+  // finished paths per job, aggregated over the lanes of one job
+  const int ended = (live && !cont) ? job : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, ended);
+  if (ended >= 0 && lane == __ffs(peers) - 1) atomicAdd(&job_done[ended], (uint32_t)__popc(peers));
   if (live) {
     next.o[j] = no;
     next.d[j] = cont ? nd : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
@@ -477,17 +523,18 @@ __global__ void __launch_bounds__(TB) k_shade(DevScene sc, DevFrame f, RayBuf ba
 
 // rtcOccluded with mask 0x0FFFFFFF (Integrator.cpp:153-174); an unoccluded
 // shadow ray adds its weighted contribution to its sample.
-template <bool WIDE>
-__global__ void __launch_bounds__(128) k_trace_shadow(BvhRef bvh, ShadowBuf sh, const int* __restrict__ count,
-                                                      float4* sample_rgb, int* err) {
+template <bool WIDE, bool MULTI>
+__global__ void __launch_bounds__(128) k_trace_shadow(const SceneRec* __restrict__ scenes, BvhRef scene0, ShadowBuf sh,
+                                                      const int* __restrict__ count, float4* sample_rgb, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= *count) return;
-  const float4 o = sh.o[i], d = sh.d[i];
+  const float4 o = sh.o[i], d = sh.d[i], c = sh.c[i];
+  const BvhRef b = MULTI ? bvh_of(scenes[__float_as_int(c.w)], WIDE) : scene0;
   TriHit h;
   int ovf = 0;
-  const bool blocked = scene_trace<WIDE, true>(bvh, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
+  const bool blocked = scene_trace<WIDE, true>(b, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
   if (ovf) atomicOr(err, ovf_bits(ovf));
-  if (!blocked) add_rgb(&sample_rgb[__float_as_int(d.w)], f3(sh.c[i]));
+  if (!blocked) add_rgb(&sample_rgb[__float_as_int(d.w)], f3(c));
 }
 
 template <bool WIDE>
@@ -505,7 +552,7 @@ __global__ void __launch_bounds__(128) k_occluded(BvhRef bvh, const float4* __re
 // ------------------------------------------------------------------ filters
 // TentFilter::convolve (src/core/TentFilter.cpp:5-63): gather over the 3x3
 // neighbour pixels; samples are x-major, pixels row-major.
-__global__ void __launch_bounds__(TB) k_filter_tent(DevFrame f, float* __restrict__ pixels) {
+__global__ void __launch_bounds__(TB) k_filter_tent(JobRec f, Film film) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= f.width * f.height) return;
   const int x = idx / f.height, y = idx - x * f.height;
@@ -515,10 +562,10 @@ __global__ void __launch_bounds__(TB) k_filter_tent(DevFrame f, float* __restric
     for (int my = -1; my < 2; ++my) {
       const int px = x + mx, py = y + my;
       if (px < 0 || px >= f.width || py < 0 || py >= f.height) continue;
-      const size_t b = ((size_t)px * f.height + py) * f.spp;
+      const size_t b = (size_t)f.sample_base + ((size_t)px * f.height + py) * f.spp;
       for (int s = 0; s < f.spp; ++s) {
-        const float2 p = f.sample_pos[b + s];
-        const float4 c = f.sample_rgb[b + s];
+        const float2 p = film.pos[b + s];
+        const float4 c = film.rgb[b + s];
         const float dx = fmaxf(0.f, 1.f - fabsf(p.x - cx));
         const float dy = fmaxf(0.f, 1.f - fabsf(p.y - cy));
         const float m = dx * dy;
@@ -529,27 +576,27 @@ __global__ void __launch_bounds__(TB) k_filter_tent(DevFrame f, float* __restric
       }
     }
   }
-  float* px = pixels + 3 * ((size_t)y * f.width + x);
+  float* px = f.pixels + 3 * ((size_t)y * f.width + x);
   px[0] += sr / den;
   px[1] += sg / den;
   px[2] += sb / den;
 }
 
 // BoxFilter::convolve (src/core/BoxFilter.cpp:5-37).
-__global__ void __launch_bounds__(TB) k_filter_box(DevFrame f, float* __restrict__ pixels) {
+__global__ void __launch_bounds__(TB) k_filter_box(JobRec f, Film film) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= f.width * f.height) return;
   const int x = idx / f.height, y = idx - x * f.height;
-  const size_t b = ((size_t)x * f.height + y) * f.spp;
+  const size_t b = (size_t)f.sample_base + ((size_t)x * f.height + y) * f.spp;
   float sr = 0.f, sg = 0.f, sb = 0.f;
   for (int s = 0; s < f.spp; ++s) {
-    const float4 c = f.sample_rgb[b + s];
+    const float4 c = film.rgb[b + s];
     sr += c.x;
     sg += c.y;
     sb += c.z;
   }
   const float ns = (float)f.spp;
-  float* px = pixels + 3 * ((size_t)y * f.width + x);
+  float* px = f.pixels + 3 * ((size_t)y * f.width + x);
   px[0] += sr / ns;
   px[1] += sg / ns;
   px[2] += sb / ns;
@@ -557,9 +604,9 @@ __global__ void __launch_bounds__(TB) k_filter_box(DevFrame f, float* __restrict
 
 }  // namespace
 
-int launch_raygen(const DevFrame& f, uint32_t first, int n, RayBuf out, cudaStream_t s) {
+int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s) {
   if (n <= 0) return 0;
-  k_raygen<<<grid_for(n), TB, 0, s>>>(f, first, n, out);
+  k_raygen<<<grid_for(n), TB, 0, s>>>(job, job_index, first, n, out, film);
   return 1;
 }
 
@@ -581,67 +628,88 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
   return 1;
 }
 
-int launch_origin_box(const float4* o, int n, uint32_t* box6, cudaStream_t s) {
+int launch_origin_box(const float4* o, const Segments& seg, uint32_t* box6, cudaStream_t s) {
+  const int n = seg.prefix[seg.count];
   if (n <= 0) return 0;
-  k_origin_box<<<min(grid_for(n), 512), TB, 0, s>>>(o, n, box6);
+  k_origin_box<<<std::min(grid_for(n), 512), TB, 0, s>>>(o, seg, box6);
   return 1;
 }
 
-int launch_ray_keys(const float4* o, const float4* d, int n, const uint32_t* box6, uint32_t* keys, cudaStream_t s) {
+int launch_ray_keys(const float4* o, const float4* d, const Segments& seg, const uint32_t* box6, int prefix_bits,
+                    uint32_t* keys, cudaStream_t s) {
+  const int n = seg.prefix[seg.count];
   if (n <= 0) return 0;
-  k_ray_keys<<<grid_for(n), TB, 0, s>>>(o, d, n, box6, keys);
+  k_ray_keys<<<grid_for(n), TB, 0, s>>>(o, d, seg, box6, prefix_bits, keys);
   return 1;
 }
 
-int launch_gather(const RayBuf& src, const uint32_t* perm, int n, RayBuf dst, cudaStream_t s) {
+int launch_gather(const RayBuf& src, const Segments& seg, const uint32_t* perm, RayBuf dst, cudaStream_t s) {
+  const int n = seg.prefix[seg.count];
   if (n <= 0) return 0;
-  k_gather<<<grid_for(n), TB, 0, s>>>(src, perm, n, dst);
+  k_gather<<<grid_for(n), TB, 0, s>>>(src, seg, perm, dst);
   return 1;
 }
 
-int launch_trace_closest(const DevScene& sc, const float4* o, const float4* d, int n, float4* hits, int* err,
-                         cudaStream_t s) {
+int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
+                         const float4* d, int n, float4* hits, int* err, cudaStream_t s) {
   if (n <= 0) return 0;
-  if (sc.wnodes) k_trace_closest<true><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, hits, err);
-  else k_trace_closest<false><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, hits, err);
+  const bool wide = scene0.wnodes != nullptr;
+  const BvhRef b0 = bvh_of(scene0, wide);
+  const int g = grid_for(n, 128);
+  if (num_scenes > 1) {
+    if (wide) k_trace_closest<true, true><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
+    else k_trace_closest<false, true><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
+  } else {
+    if (wide) k_trace_closest<true, false><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
+    else k_trace_closest<false, false><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
+  }
   return 1;
 }
 
-int launch_hit_keys(const DevScene& sc, const float4* hits, int n, uint32_t* keys, cudaStream_t s) {
-  if (n <= 0) return 0;
-  k_hit_keys<<<grid_for(n), TB, 0, s>>>(sc.tri_orig, hits, n, keys);
-  return 1;
-}
-
-int launch_shade(const DevScene& sc, const DevFrame& f, const RayBuf& batch, const float4* hits, const uint32_t* order,
-                 int n, RayBuf next, ShadowBuf sh, int* sh_count, cudaStream_t s) {
-  if (n <= 0) return 0;
-  k_shade<<<grid_for(n), TB, 0, s>>>(sc, f, batch, hits, order, n, next, sh, sh_count);
-  return 1;
-}
-
-int launch_trace_shadow(const DevScene& sc, const ShadowBuf& sh, const int* sh_count, int max_n, float4* sample_rgb,
-                        int* err, cudaStream_t s) {
-  if (max_n <= 0) return 0;
-  if (sc.wnodes)
-    k_trace_shadow<true><<<grid_for(max_n, 128), 128, 0, s>>>(bvh_ref(sc), sh, sh_count, sample_rgb, err);
-  else
-    k_trace_shadow<false><<<grid_for(max_n, 128), 128, 0, s>>>(bvh_ref(sc), sh, sh_count, sample_rgb, err);
-  return 1;
-}
-
-int launch_occluded(const DevScene& sc, const float4* o, const float4* d, int n, int* occluded, int* err,
+int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
                     cudaStream_t s) {
   if (n <= 0) return 0;
-  if (sc.wnodes) k_occluded<true><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, occluded, err);
-  else k_occluded<false><<<grid_for(n, 128), 128, 0, s>>>(bvh_ref(sc), o, d, n, occluded, err);
+  k_hit_keys<<<grid_for(n), TB, 0, s>>>(scenes, d, hits, n, keys);
   return 1;
 }
 
-int launch_filter(const DevFrame& f, int filter, float* pixels, cudaStream_t s) {
-  const int n = f.width * f.height;
-  if (filter == FILTER_BOX) k_filter_box<<<grid_for(n), TB, 0, s>>>(f, pixels);
-  else k_filter_tent<<<grid_for(n), TB, 0, s>>>(f, pixels);
+int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
+                 const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
+                 cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, hits, order, n, next, sh, sh_count, job_done);
+  return 1;
+}
+
+int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
+                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s) {
+  if (max_n <= 0) return 0;
+  const bool wide = scene0.wnodes != nullptr;
+  const BvhRef b0 = bvh_of(scene0, wide);
+  const int g = grid_for(max_n, 128);
+  if (num_scenes > 1) {
+    if (wide) k_trace_shadow<true, true><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
+    else k_trace_shadow<false, true><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
+  } else {
+    if (wide) k_trace_shadow<true, false><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
+    else k_trace_shadow<false, false><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
+  }
+  return 1;
+}
+
+int launch_occluded(const SceneRec& scene, const float4* o, const float4* d, int n, int* occluded, int* err,
+                    cudaStream_t s) {
+  if (n <= 0) return 0;
+  const bool wide = scene.wnodes != nullptr;
+  if (wide) k_occluded<true><<<grid_for(n, 128), 128, 0, s>>>(bvh_of(scene, true), o, d, n, occluded, err);
+  else k_occluded<false><<<grid_for(n, 128), 128, 0, s>>>(bvh_of(scene, false), o, d, n, occluded, err);
+  return 1;
+}
+
+int launch_filter(const JobRec& job, Film film, cudaStream_t s) {
+  const int n = job.width * job.height;
+  if (job.filter == FILTER_BOX) k_filter_box<<<grid_for(n), TB, 0, s>>>(job, film);
+  else k_filter_tent<<<grid_for(n), TB, 0, s>>>(job, film);
   return 1;
 }
 

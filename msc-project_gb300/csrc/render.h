@@ -2,10 +2,14 @@
 //
 // A ray record (the reference's RayCompressed, include/core/RayCompressed.h:14-23)
 // is three float4 in structure-of-arrays form:
-//   o = (org.xyz, lastPdf), d = (dir.xyz, rayDepth as int; < 0 = dead),
-//   w = (weight.rgb, sampleID as int).
-// A shadow ray is o = (org.xyz, tmax), d = (dir.xyz, sampleID), c = (weighted contribution.rgb, 0).
-// A hit is (t, u, v, leaf-order triangle or -1).
+//   o = (org.xyz, lastPdf)
+//   d = (dir.xyz, info)   info = job << 16 | scene << 8 | rayDepth as int; < 0 = dead
+//   w = (weight.rgb, sampleID within its job, as int)
+// A shadow ray is o = (org.xyz, tmax), d = (dir.xyz, global sample index),
+// c = (weighted contribution.rgb, scene as int).  A hit is (t, u, v, triangle or -1).
+//
+// Scenes and jobs live in device tables indexed by the ray's info word, so one
+// batch can hold rays of many jobs over many scenes.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -27,31 +31,51 @@ struct ShadowBuf {
   float4* c = nullptr;
 };
 
-struct DevScene {
-  const float4* nodes;   // binary BVH (null when the 8-wide form is used)
+constexpr int kMaxJobs = 1 << 15;
+constexpr int kMaxScenes = 256;
+constexpr int kMaxDepth = 255;
+
+__host__ __device__ __forceinline__ int ray_info(int job, int scene, int depth) {
+  return (job << 16) | (scene << 8) | depth;
+}
+__host__ __device__ __forceinline__ int info_job(int info) { return info >> 16; }
+__host__ __device__ __forceinline__ int info_scene(int info) { return (info >> 8) & 0xff; }
+__host__ __device__ __forceinline__ int info_depth(int info) { return info & 0xff; }
+
+struct SceneRec {        // one resident scene
   const uint4* wnodes;   // 8-wide BVH (null for the binary form)
-  int num_wnodes;
+  const float4* nodes;   // binary BVH (null for the wide form)
   const float4* tris;
   const int* tri_orig;
+  int num_wnodes;
   int num_tris;
   const ShaderRec* shaders;
   const GeomRec* geoms;
   const LightRec* lights;
   int num_lights;
-  float light_pick;  // 1 / num_lights (Integrator.cpp:22)
+  float light_pick;      // 1 / num_lights (Integrator.cpp:22)
+  uint32_t tri_base;     // offset of this scene's triangles in the hit-key space
+  int pad;
 };
 
-struct DevFrame {
+struct JobRec {          // one render job: a scene seen through one camera
   CameraRec cam;
   int width, height, spp;
-  int grid_x, grid_y;  // stratification cells (base x base in the reference)
+  int grid_x, grid_y;    // stratification cells (base x base in the reference)
   int sampler;
+  int filter;
   int min_depth, max_depth;
   float threshold;
   int mis_power;
   uint32_t iter_seed;
-  float4* sample_rgb;  // per-sample radiance (Image::samples r,g,b)
-  float2* sample_pos;  // per-sample film position (Image::samples x,y)
+  int scene;
+  uint32_t sample_base;  // first entry of this job in the sample arrays
+  float* pixels;         // W*H*3 accumulated image, row-major
+};
+
+struct Film {            // per-sample radiance and film position, all jobs (Image::samples)
+  float4* rgb = nullptr;
+  float2* pos = nullptr;
 };
 
 // Error bits reported through the engine's device flag word.
@@ -59,11 +83,18 @@ enum : int { ERR_BIN_OVERFLOW = 1, ERR_STACK_OVERFLOW = 2, ERR_TRAVERSAL_CAP = 4
 
 constexpr int kMaxBins = 8;  // 6 cardinal bins + the dead bucket, rounded up
 
+// Where the rays of one batch sit: up to 6 ranges of the bin pool.
+struct Segments {
+  int start[6];
+  int prefix[7];  // prefix[k] = rays in ranges before k; prefix[count] = total
+  int count;
+};
+
 // Each launcher returns the number of kernels it enqueued.
-int launch_raygen(const DevFrame& f, uint32_t first, int n, RayBuf out, cudaStream_t s);
+int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s);
 
 struct BinPool {
-  RayBuf rays;       // kMaxBins-1 bins of `cap` rays each, bin b at [b*cap, (b+1)*cap)
+  RayBuf rays;       // 6 bins of `cap` rays each, bin b at [b*cap, (b+1)*cap)
   int cap = 0;
   int* count = nullptr;      // device: rays held per bin
   uint32_t* tile_counts = nullptr;  // scratch for the partition (kMaxBins * tiles)
@@ -72,26 +103,31 @@ struct BinPool {
 };
 constexpr int kPartTile = 2048;
 // Stable partition of src[0, n) by cardinal bin, appended behind each bin's
-// current content; dead rays (d.w < 0) are dropped.
+// current content; dead rays (info < 0) are dropped.
 int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s);
 
 // Per-ray cardinal bin only (stage test).
 int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 
-// Origin box of rays [0, n) into box6 (ordered-int min xyz, max xyz; caller initialises).
-int launch_origin_box(const float4* o, int n, uint32_t* box6, cudaStream_t s);
-int launch_ray_keys(const float4* o, const float4* d, int n, const uint32_t* box6, uint32_t* keys, cudaStream_t s);
-int launch_gather(const RayBuf& src, const uint32_t* perm, int n, RayBuf dst, cudaStream_t s);
+// Origin box of the batch rays into box6 (ordered-int min xyz, max xyz; caller initialises).
+int launch_origin_box(const float4* o, const Segments& seg, uint32_t* box6, cudaStream_t s);
+// 32-bit keys; prefix_bits > 0 puts (scene << 3 | cardinal bin) above the origin/direction code.
+int launch_ray_keys(const float4* o, const float4* d, const Segments& seg, const uint32_t* box6, int prefix_bits,
+                    uint32_t* keys, cudaStream_t s);
+int launch_gather(const RayBuf& src, const Segments& seg, const uint32_t* perm, RayBuf dst, cudaStream_t s);
 
-int launch_trace_closest(const DevScene& sc, const float4* o, const float4* d, int n, float4* hits, int* err,
-                         cudaStream_t s);
-int launch_hit_keys(const DevScene& sc, const float4* hits, int n, uint32_t* keys, cudaStream_t s);
-int launch_shade(const DevScene& sc, const DevFrame& f, const RayBuf& batch, const float4* hits, const uint32_t* order,
-                 int n, RayBuf next, ShadowBuf sh, int* sh_count, cudaStream_t s);
-int launch_trace_shadow(const DevScene& sc, const ShadowBuf& sh, const int* sh_count, int max_n, float4* sample_rgb,
-                        int* err, cudaStream_t s);
-// Occlusion for explicit rays (stage test): occluded[i] = 1 if blocked in (tnear, tmax).
-int launch_occluded(const DevScene& sc, const float4* o, const float4* d, int n, int* occluded, int* err, cudaStream_t s);
-int launch_filter(const DevFrame& f, int filter, float* pixels, cudaStream_t s);
+int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
+                         const float4* d, int n, float4* hits, int* err, cudaStream_t s);
+int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
+                    cudaStream_t s);
+int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
+                 const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
+                 cudaStream_t s);
+int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
+                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s);
+// Occlusion for explicit rays of scene 0 (stage test): occluded[i] = 1 if blocked in (tnear, tmax).
+int launch_occluded(const SceneRec& scene, const float4* o, const float4* d, int n, int* occluded, int* err,
+                    cudaStream_t s);
+int launch_filter(const JobRec& job, Film film, cudaStream_t s);
 
 }  // namespace mscg

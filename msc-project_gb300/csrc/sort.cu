@@ -24,6 +24,7 @@ constexpr int RADIX = 1 << kSortRadixBits;
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;
 constexpr int kLookbackSpinCap = 1 << 20;
+constexpr int kLookbackWindow = 8;
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
 __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
@@ -112,21 +113,34 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
       st_volatile(&status_cur[d], (cnt << 2) | kFlagPrefix);
     } else {
       st_volatile(&status_cur[tile * RADIX + d], (cnt << 2) | kFlagAggregate);
+      // Look back a window of kLookbackWindow predecessors per step (independent
+      // loads), summing aggregates up to the first inclusive prefix.
       int t = tile - 1;
       int spins = 0;
       while (t >= 0) {
-        const uint32_t v = ld_volatile(&status_cur[t * RADIX + d]);
-        const uint32_t f = v & 3u;
-        if (f == 0u) {  // the predecessor has not posted yet; it is running, so this ends
+        uint32_t v[kLookbackWindow];
+#pragma unroll
+        for (int k = 0; k < kLookbackWindow; ++k)
+          v[k] = (t - k >= 0) ? ld_volatile(&status_cur[(t - k) * RADIX + d]) : kFlagPrefix;
+        int used = 0;
+        bool done = false;
+#pragma unroll
+        for (int k = 0; k < kLookbackWindow; ++k) {
+          if (done || used < k) continue;       // stop at the first prefix or the first unposted tile
+          const uint32_t f = v[k] & 3u;
+          if (f == 0u) continue;                // not posted yet: re-read from here
+          excl += v[k] >> 2;
+          used = k + 1;
+          if (f == kFlagPrefix) done = true;
+        }
+        if (done) break;
+        t -= used;
+        if (used < kLookbackWindow) {  // a predecessor has not posted yet; it is running, so this ends
           if (++spins > kLookbackSpinCap) {
             atomicOr(err, kSortErrLookback);
             break;
           }
-          continue;
         }
-        excl += v >> 2;
-        if (f == kFlagPrefix) break;
-        --t;
       }
       st_volatile(&status_cur[tile * RADIX + d], ((excl + cnt) << 2) | kFlagPrefix);
     }

@@ -35,6 +35,28 @@ class _Stats(C.Structure):
                 ("triangles", C.c_int), ("lights", C.c_int), ("iteration", C.c_int)]
 
 
+class _JobDesc(C.Structure):
+    _fields_ = [("scene", C.c_int), ("width", C.c_int), ("height", C.c_int), ("spp", C.c_int),
+                ("min_depth", C.c_int), ("max_depth", C.c_int), ("use_camera", C.c_int),
+                ("translation", C.c_float * 3), ("rotation", C.c_float * 3), ("focal_length", C.c_float),
+                ("seed", C.c_uint32)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("job", _JobDesc)]
+
+
+class _RequestResult(C.Structure):
+    _fields_ = [("job_id", C.c_int), ("status", C.c_int), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("latency_s", C.c_double)]
+
+
+class _ServeStats(C.Structure):
+    _fields_ = [("completed", C.c_int), ("wall_s", C.c_double), ("p50_s", C.c_double), ("p99_s", C.c_double),
+                ("p999_s", C.c_double), ("mrays_per_s", C.c_double), ("closest_queries", C.c_uint64),
+                ("shadow_queries", C.c_uint64), ("peak_film_samples", C.c_int64)]
+
+
 _lib = None
 
 
@@ -69,6 +91,18 @@ def load_library():
         "msc_trace_closest": (I, [P, F, F, I, F, F, F, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
         "msc_trace_occluded": (I, [P, F, F, F, I, C.POINTER(C.c_int32)]),
         "msc_generate_scene": (I, [I, C.c_uint32, C.c_double, C.c_char_p, C.c_char_p, I]),
+        "msc_batch_create": (I, [I, C.c_int64, C.POINTER(P)]),
+        "msc_batch_destroy": (I, [P]),
+        "msc_batch_last_error": (C.c_char_p, [P]),
+        "msc_batch_add_scene": (I, [P, C.c_char_p, C.POINTER(I)]),
+        "msc_batch_submit": (I, [P, C.POINTER(_JobDesc), C.POINTER(I)]),
+        "msc_batch_run": (I, [P]),
+        "msc_batch_job_image": (I, [P, I, C.POINTER(F), C.POINTER(I), C.POINTER(I)]),
+        "msc_batch_release_job": (I, [P, I]),
+        "msc_batch_get_stats": (I, [P, C.POINTER(_Stats)]),
+        "msc_batch_set_profiling": (I, [P, I]),
+        "msc_batch_set_max_active": (I, [P, I]),
+        "msc_serve": (I, [P, C.POINTER(_Request), I, C.POINTER(_RequestResult), C.POINTER(_ServeStats)]),
         "msc_obj_load": (I, [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]),
         "msc_scene_load_host": (I, [C.c_char_p, C.POINTER(C.c_int32), F, C.POINTER(C.c_int32)]),
     }
@@ -269,3 +303,102 @@ def scene_load_host(yaml_path):
                                    _ptr(tg, C.c_int32)))
     keys = ["width", "height", "spp", "triangles", "lights", "shaders", "geometries", "camera"]
     return dict(zip(keys, [int(x) for x in info])), tv, tg
+
+
+def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
+    d = _JobDesc()
+    d.scene, d.width, d.height, d.spp = scene, width, height, spp
+    d.min_depth, d.max_depth = min_depth, max_depth
+    if camera is not None:
+        t, r, f = camera
+        d.use_camera = 1
+        d.translation[:] = list(t)
+        d.rotation[:] = list(r)
+        d.focal_length = f
+    d.seed = seed
+    return d
+
+
+class Batch:
+    """Batched and served forms: many resident scenes and jobs in one wavefront."""
+
+    def __init__(self, batch_exponent=20, film_samples=1 << 26):
+        self._lib = load_library()
+        b = C.c_void_p()
+        rc = self._lib.msc_batch_create(batch_exponent, film_samples, C.byref(b))
+        if rc != MSC_OK:
+            raise MscError(rc, (self._lib.msc_batch_last_error(None) or b"").decode())
+        self._b = b
+
+    def _check(self, rc):
+        if rc != MSC_OK:
+            raise MscError(rc, (self._lib.msc_batch_last_error(self._b) or b"").decode())
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._lib.msc_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_scene(self, yaml_path):
+        sid = C.c_int()
+        self._check(self._lib.msc_batch_add_scene(self._b, os.fsencode(yaml_path), C.byref(sid)))
+        return sid.value
+
+    def submit(self, scene, **kw):
+        """kw: width, height, spp, min_depth, max_depth, camera=(translation, rotation, focal), seed."""
+        jid = C.c_int()
+        d = _job_desc(scene, **kw)
+        self._check(self._lib.msc_batch_submit(self._b, C.byref(d), C.byref(jid)))
+        return jid.value
+
+    def run(self):
+        self._check(self._lib.msc_batch_run(self._b))
+
+    def image(self, job):
+        p = C.POINTER(C.c_float)()
+        w, h = C.c_int(), C.c_int()
+        self._check(self._lib.msc_batch_job_image(self._b, job, C.byref(p), C.byref(w), C.byref(h)))
+        return np.ctypeslib.as_array(p, shape=(h.value * w.value * 3,)).reshape(h.value, w.value, 3).copy()
+
+    def release(self, job):
+        self._check(self._lib.msc_batch_release_job(self._b, job))
+
+    def set_profiling(self, on):
+        self._check(self._lib.msc_batch_set_profiling(self._b, 1 if on else 0))
+
+    def set_max_active(self, n):
+        self._check(self._lib.msc_batch_set_max_active(self._b, n))
+
+    def stats(self):
+        s = _Stats()
+        self._check(self._lib.msc_batch_get_stats(self._b, C.byref(s)))
+        d = {k: getattr(s, k) for k, _ in _Stats._fields_ if k not in ("stage_ms", "stage_launches")}
+        d["stage_ms"] = {STAGES[i]: s.stage_ms[i] for i in range(len(STAGES))}
+        return d
+
+    def serve(self, requests):
+        """requests: list of (arrival_s, job kwargs incl. scene).  Returns (results, stats)."""
+        n = len(requests)
+        reqs = (_Request * max(n, 1))()
+        for i, (t, kw) in enumerate(requests):
+            kw = dict(kw)
+            reqs[i].arrival_s = t
+            reqs[i].job = _job_desc(kw.pop("scene"), **kw)
+        res = (_RequestResult * max(n, 1))()
+        st = _ServeStats()
+        self._check(self._lib.msc_serve(self._b, reqs, n, res, C.byref(st)))
+        results = [{k: getattr(res[i], k) for k, _ in _RequestResult._fields_} for i in range(n)]
+        stats = {k: getattr(st, k) for k, _ in _ServeStats._fields_}
+        return results, stats

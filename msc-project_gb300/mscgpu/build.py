@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["sort.cu", "bvh.cu", "render.cu", "engine.cu", "noalloc.cu"]
+CU_SOURCES = ["sort.cu", "bvh.cu", "render.cu", "core.cu", "engine.cu", "noalloc.cu"]
 CPP_SOURCES = ["scene.cpp", "scenegen.cpp", "imageio.cpp"]
 CLI = os.path.join(HERE, "msc-gpu")
 

@@ -1127,6 +1127,32 @@ void oracle_triangles(const oracle_scene* s, float* v9, int32_t* geom) {
     for (size_t i = 0; i < s->tgeom.size(); ++i) geom[i] = s->tgeom[i];
 }
 
+int oracle_set_job(oracle_scene* s, int width, int height, int spp, int min_depth, int max_depth,
+                   const float* cam_t, const float* cam_r, float focal, uint32_t seed) {
+  if (width > 0) s->W = width;
+  if (height > 0) s->H = height;
+  if (spp > 0) {
+    s->spp = spp;
+    int a = 1;
+    for (int d = 1; d * d <= spp; ++d)
+      if (spp % d == 0) a = d;
+    s->gx = a;
+    s->gy = spp / a;
+    if (a * a == spp) s->base = a;
+  }
+  if (min_depth >= 0) s->min_depth = min_depth;
+  if (max_depth >= 0) s->max_depth = max_depth;
+  if (cam_t && cam_r && focal > 0.f) {  // a pinhole camera (PinHoleCamera.cpp:5-14)
+    s->cam_type = 0;
+    s->cam = orc::tr_yxz(cam_t, cam_r);
+    orc::x_normal(s->cam, s->cam_n);
+    for (int i = 0; i < 3; ++i) s->cam_t[i] = cam_t[i];
+    s->focal = focal;
+  }
+  s->seed = seed;
+  return 0;
+}
+
 void oracle_info(const oracle_scene* s, int* o) {
   o[0] = s->W; o[1] = s->H; o[2] = s->spp; o[3] = (int)s->tgeom.size(); o[4] = (int)s->lights.size();
 }

@@ -33,6 +33,11 @@ oracle_scene* oracle_load(const char* yaml_path, char* err, int errcap);
 void oracle_free(oracle_scene* s);
 /* World-space triangles (9 floats each, geomID order) and their geomIDs. */
 void oracle_triangles(const oracle_scene* s, float* v9, int32_t* geom);
+/* Per-job overrides (values <= 0 / < 0 / NULL keep the scene's): resolution,
+ * sample count (grid split as for non-square counts), depth limits, a pinhole
+ * camera (translation, rotation in degrees, focal length) and the seed. */
+int oracle_set_job(oracle_scene* s, int width, int height, int spp, int min_depth, int max_depth, const float* cam_t,
+                   const float* cam_r, float focal, uint32_t seed);
 /* w, h, spp, triangles, lights */
 void oracle_info(const oracle_scene* s, int* out5);
 

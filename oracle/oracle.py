@@ -63,6 +63,18 @@ class Scene:
             lib().oracle_free(self._s)
             self._s = None
 
+    def set_job(self, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, cam_t=None, cam_r=None, focal=0.0,
+                seed=0):
+        L = lib()
+        L.oracle_set_job.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_uint32]
+        t = (C.c_float * 3)(*cam_t) if cam_t is not None else None
+        r = (C.c_float * 3)(*cam_r) if cam_r is not None else None
+        L.oracle_set_job(self._s, width, height, spp, min_depth, max_depth, t, r, focal, seed)
+        info = (C.c_int * 5)()
+        L.oracle_info(self._s, info)
+        self.width, self.height, self.spp, self.triangles, self.lights = list(info)
+
     def triangles_array(self):
         tv = np.zeros((self.triangles, 9), np.float32)
         tg = np.zeros(self.triangles, np.int32)
