@@ -178,80 +178,129 @@ def sphere_camera(rng, bbox, fov_lo=30.0, fov_hi=70.0):
     return (tuple(float(x) for x in t), (0.0, ry, rz), focal)
 
 
-def random_jobs(rng, scenes_bboxes, n, res_choices, spp_lo, spp_hi, depth_lo, depth_hi):
-    jobs = []
-    for _ in range(n):
-        s = int(rng.integers(0, len(scenes_bboxes)))
-        res = int(rng.choice(res_choices))
-        jobs.append(dict(scene=s, width=res, height=res, spp=int(rng.integers(spp_lo, spp_hi + 1)),
-                         min_depth=3, max_depth=int(rng.integers(depth_lo, depth_hi + 1)),
-                         camera=sphere_camera(rng, scenes_bboxes[s]), seed=int(rng.integers(1, 1 << 30))))
-    return jobs
+def log_uniform_int(rng, lo, hi):
+    import math
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def random_job(rng, scene, bbox, res_choices, spp_lo, spp_hi, depth_lo=4, depth_hi=10):
+    res = int(rng.choice(res_choices))
+    return dict(scene=scene, width=res, height=res, spp=log_uniform_int(rng, spp_lo, spp_hi), min_depth=3,
+                max_depth=int(rng.integers(depth_lo, depth_hi + 1)), camera=sphere_camera(rng, bbox),
+                seed=int(rng.integers(1, 1 << 30)))
+
+
+def job_paths(j):
+    return j["width"] * j["height"] * j["spp"]
 
 
 def bench_forms(args):
-    """Batched and served forms against the one-job-at-a-time loop on the same jobs."""
+    """Batched and served forms against the one-job-at-a-time loop on the same jobs.
+
+    Batched: one job per scene over 64 terrain scenes with log-uniform triangle
+    counts, resolutions {128^2 .. 1024^2}, 4-256 spp (log-uniform), depth 4-10,
+    all submitted at once.  Served: Poisson arrivals on the first 16 scenes.
+    The per-job loop is the same engine admitting one job at a time (the plain
+    single-scene wavefront, scenes kept resident)."""
     import mscgpu
     import numpy as np
     t = time.time()
-    scenes = scene_set(16, 1e4, 1e6, SEED + 300)
-    bboxes = []
+    scenes = scene_set(args.forms_scenes, 1e4, 3e6, SEED + 300)
+    gen_s = time.time() - t
+    film_cap = 1_800_000_000  # the film pool indexes samples with 31 bits
+    t = time.time()
+    b = mscgpu.Batch(batch_exponent=20, film_samples=film_cap)
+    bboxes, tris = [], []
     for y in scenes:
-        _, tv, _ = mscgpu.scene_load_host(y)
-        p = tv.reshape(-1, 3)
-        bboxes.append((p.min(0), p.max(0)))
-    log("batched/served scene set ready in %.1f s" % (time.time() - t))
+        k = b.add_scene(y)
+        lo, hi, n = b.scene_info(k)
+        bboxes.append((lo, hi))
+        tris.append(n)
+    load_s = time.time() - t
     rng = np.random.default_rng(SEED + 301)
-    jobs = random_jobs(rng, bboxes, 48, [128, 256, 512], 4, 32, 4, 10)
-    film = int(sum(j["width"] * j["height"] * j["spp"] for j in jobs)) + 1
+    while True:  # one job per scene
+        jobs = [random_job(rng, i, bboxes[i], [128, 256, 512, 1024], 4, 256) for i in range(len(scenes))]
+        if sum(job_paths(j) for j in jobs) < film_cap:
+            break
+    film = film_cap
+    log("forms: %d scenes (%d..%d tris, %d total) generated in %.1f s, loaded + BVHs in %.1f s"
+        % (len(scenes), min(tris), max(tris), sum(tris), gen_s, load_s))
 
-    def new_batch(max_active=0, film_samples=film):
-        b = mscgpu.Batch(batch_exponent=20, film_samples=film_samples)
-        for y in scenes:
-            b.add_scene(y)
-        if max_active:
-            b.set_max_active(max_active)
-        return b
+    def rays_of(st):
+        return st["closest_queries"] + st["shadow_queries"]
 
     out = {}
-    # batched: every job in one wavefront
-    b = new_batch()
-    for j in jobs:
-        b.submit(**j)
+    # autotune on a sample of the same workload (untimed): the first 16 jobs at
+    # up to 16 spp, repeated until the tuner has booked every candidate
+    b.autotune(windows=2)
+    sample = [dict(j, spp=min(j["spp"], 16)) for j in jobs[:16]]
+    for _ in range(8):
+        ids = [b.submit(**j) for j in sample]
+        b.run()
+        for i in ids:
+            b.release(i)
+        if not b.tuning()["tuning"]:
+            break
+    tuned = b.tuning()
+    tune_log = b.tune_log()
+    # batched: every job in one wavefront, tuned choice
+    s0 = b.stats()
+    ids = [b.submit(**j) for j in jobs]
     t = time.time()
     b.run()
     wall = time.time() - t
-    st = b.stats()
-    rays = st["closest_queries"] + st["shadow_queries"]
+    rays = rays_of(b.stats()) - rays_of(s0)
+    for i in ids:
+        b.release(i)
+    # the per-job loop on the same jobs: one job in flight at a time, with the
+    # plain engine's settings (2^20 rays per batch, 128-thread traversal, both sorts)
+    b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
+    b.set_max_active(1)
+    _, pst = b.serve([(0.0, j) for j in jobs])
+    plain_rate = rays_of(pst) / pst["wall_s"] / 1e6
+    rate = rays / wall / 1e6
+    out["batched"] = {
+        "workload": "%d jobs, one per terrain scene (%d-%d tris, log-uniform; %d total), resolutions "
+                    "128^2-1024^2, 4-256 spp log-uniform, depth 4-10, RR from 3, cameras on the bounding sphere "
+                    "(fov 30-70)" % (len(jobs), min(tris), max(tris), sum(tris)),
+        "paths": sum(job_paths(j) for j in jobs), "mrays_per_s": rate, "wall_s": wall,
+        "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
+        "speedup_vs_per_job_loop": rate / plain_rate if plain_rate else None,
+        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")},
+        "tune_samples": [[t["batch_exponent"], t["trace_block"], t["ray_sort"], t["hit_sort"],
+                          round(t["mrays_per_s"], 1)] for t in tune_log]}
+    # served: Poisson arrivals on the first 16 resident scenes, at each rate
+    nres = min(16, len(scenes))
+    out["served"] = {"workload": "Poisson arrivals on %d resident scenes, 128^2-512^2, 4-64 spp log-uniform, "
+                                 "depth 4-10, cameras on the bounding sphere; admission by a film-memory budget of "
+                                 "%d samples (%.1f GB); per rate: the served form, then the per-job loop on the "
+                                 "same requests" % (nres, film, film * 24 / 1e9),
+                     "rates": []}
+    for spec in args.serve_rates.split(","):
+        rrate, dur = (float(x) for x in spec.split(":")) if ":" in spec else (float(spec), args.serve_seconds)
+        arrivals = np.cumsum(rng.exponential(1.0 / rrate, size=int(rrate * dur * 2) + 16))
+        arrivals = arrivals[arrivals < dur]
+        reqs = []
+        for a in arrivals:
+            k = int(rng.integers(0, nres))
+            reqs.append((float(a), random_job(rng, k, bboxes[k], [128, 256, 512], 4, 64)))
+        row = {"rate_per_s": rrate, "seconds": dur, "requests": len(reqs)}
+        for label, max_active in (("served", 0), ("per_job_loop", 1)):
+            b.set_max_active(max_active)
+            if max_active:
+                b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
+            else:
+                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")})
+            _, sst = b.serve(reqs)
+            row[label] = {"completed": sst["completed"], "mrays_per_s": sst["mrays_per_s"],
+                          "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
+                          "p999_ms": 1e3 * sst["p999_s"], "wall_s": sst["wall_s"],
+                          "peak_film_samples": sst["peak_film_samples"]}
+        row["speedup_vs_per_job_loop"] = (row["served"]["mrays_per_s"] / row["per_job_loop"]["mrays_per_s"]
+                                          if row["per_job_loop"]["mrays_per_s"] else None)
+        out["served"]["rates"].append(row)
+        log("served at %g req/s: %s" % (rrate, json.dumps(row)))
     b.close()
-    # the plain per-job loop on the same jobs: one job in flight at a time
-    p = new_batch(max_active=1)
-    res, pst = p.serve([(0.0, j) for j in jobs])
-    p.close()
-    plain_rate = (pst["closest_queries"] + pst["shadow_queries"]) / pst["wall_s"] / 1e6
-    out["batched"] = {"workload": "%d jobs on 16 resident terrain scenes (1e4-1e6 tris, log-uniform), "
-                                  "128^2-512^2, 4-32 spp, depth 4-10, cameras on the bounding sphere" % len(jobs),
-                      "mrays_per_s": rays / wall / 1e6, "wall_s": wall,
-                      "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
-                      "speedup_vs_per_job_loop": (rays / wall / 1e6) / plain_rate if plain_rate else None}
-    # served: Poisson arrivals, admission by film memory
-    rate, dur = args.serve_rate, args.serve_seconds
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 1.5)))
-    arrivals = arrivals[arrivals < dur]
-    reqs = [(float(a), j) for a, j in zip(arrivals, random_jobs(rng, bboxes, len(arrivals), [128, 256], 4, 16, 4,
-                                                                    10))]
-    budget = 1 << 25
-    for label, max_active in (("served", 0), ("served_per_job_loop", 1)):
-        s = new_batch(max_active=max_active, film_samples=budget)
-        res, sst = s.serve(reqs)
-        s.close()
-        out[label] = {"requests": len(reqs), "rate_per_s": rate, "seconds": dur,
-                      "film_budget_samples": budget, "completed": sst["completed"],
-                      "mrays_per_s": sst["mrays_per_s"], "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
-                      "p999_ms": 1e3 * sst["p999_s"], "wall_s": sst["wall_s"]}
-    out["served"]["workload"] = ("Poisson %g req/s for %g s on the 16 resident scenes, 128^2-256^2, 4-16 spp, "
-                                 "depth 4-10, cameras on the bounding sphere, film budget %d samples"
-                                 % (rate, dur, budget))
     return out
 
 
@@ -300,8 +349,10 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
-    ap.add_argument("--serve-rate", type=float, default=50.0)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-rates", default="100:6,600:3",
+                    help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
+    ap.add_argument("--forms-scenes", type=int, default=64)
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -168,8 +168,34 @@ int msc_batch_create(int batch_exponent, int64_t film_samples, msc_batch** out);
 int msc_batch_destroy(msc_batch* b);
 const char* msc_batch_last_error(msc_batch* b);
 int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id);
+/* The resident scene's triangle box (lo.xyz, hi.xyz) and triangle count, for
+   placing job cameras.  No reference counterpart. */
+int msc_batch_scene_info(msc_batch* b, int scene, float lo[3], float hi[3], int64_t* triangles);
 /* MSC_ERR_BUSY when the job's film does not fit in the free film capacity. */
 int msc_batch_submit(msc_batch* b, const msc_job_desc* desc, int* job_id);
+/* The batch loop's tuning point.  No choice changes a result. */
+typedef struct msc_tuning {
+  int batch_exponent; /* rays per batch = 2^batch_exponent (at most the capacity given at create) */
+  int trace_block;    /* traversal block size: 64, 128 or 256 */
+  int ray_sort;       /* 1: each batch sorted on the origin/direction key (RaySort.cpp:7-118) */
+  int hit_sort;       /* 1: each batch's hits sorted by (geomID, primID) (Pathtracer.cpp:335-339) */
+  int tuning;         /* read only: 1 while the autotuner is still sampling */
+  int samples;        /* read only: candidate samples booked by the autotuner */
+} msc_tuning;
+typedef struct msc_tune_sample {
+  int batch_exponent, trace_block, ray_sort, hit_sort;
+  double mrays_per_s; /* device-timed rays per second over the candidate's windows */
+} msc_tune_sample;
+/* Starts the online autotuner: the next batches are spread over candidate
+   choices (batch size, then traversal block, then the two sorts), each timed
+   over `windows` windows (0: 2), and the fastest is kept.  No reference
+   counterpart. */
+int msc_batch_autotune(msc_batch* b, int windows);
+int msc_batch_get_tuning(msc_batch* b, msc_tuning* out);
+/* Applies a choice (the read-only fields are ignored); stops a running autotuner. */
+int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in);
+/* The autotuner's booked samples, at most cap; *n = how many exist. */
+int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n);
 /* Renders every submitted job to completion in one merged wavefront. */
 int msc_batch_run(msc_batch* b);
 int msc_batch_job_image(msc_batch* b, int job, const float** rgb, int* width, int* height);

@@ -53,6 +53,9 @@ SceneGPU::~SceneGPU() {
   if (d_shaders) cudaFree(d_shaders);
   if (d_geoms) cudaFree(d_geoms);
   if (d_lights) cudaFree(d_lights);
+  if (d_spheres) cudaFree(d_spheres);
+  if (d_sphere_light) cudaFree(d_sphere_light);
+  if (d_texels) cudaFree(d_texels);
 }
 
 JobRec job_record(const SceneDesc& d, const JobSpec& spec, int scene_id) {
@@ -98,8 +101,10 @@ Core::~Core() {
   if (h_scenes_) cudaFreeHost(h_scenes_);
   if (h_jobs_) cudaFreeHost(h_jobs_);
   if (h_job_done_) cudaFreeHost(h_job_done_);
-  if (h_small_) cudaFreeHost(h_small_);
-  if (h_counts_up_) cudaFreeHost(h_counts_up_);
+  if (graph_) cudaGraphExecDestroy(graph_);
+  if (h_ctr_) cudaFreeHost(h_ctr_);
+  for (auto e : tune_ev_)
+    if (e) cudaEventDestroy(e);
   for (auto e : event_pool_) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -113,6 +118,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   wide_ = wide;
   batch_exponent = std::max(6, std::min(batch_exponent, 24));
   batch_cap_ = 1 << batch_exponent;
+  batch_size_ = batch_cap_;
   generation_ = std::max(generation, batch_cap_);
   staging_cap_ = std::max(batch_cap_, std::min(generation_, 4 * batch_cap_));
   sample_cap_ = std::max<size_t>(sample_capacity, 1);
@@ -121,6 +127,8 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
     return MSC_ERR_ARG;
   }
   CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&tune_ev_[0]));
+  CK(cudaEventCreate(&tune_ev_[1]));
   CK(cudaMalloc(&d_scenes_, kMaxScenes * sizeof(SceneRec)));
   CK(cudaMallocHost(&h_scenes_, kMaxScenes * sizeof(SceneRec)));
   CK(cudaMalloc(&d_jobs_, (size_t)kMaxJobs * sizeof(JobRec)));
@@ -134,7 +142,8 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   const int B = batch_cap_, G = generation_, S = staging_cap_;
   const int part_tiles = (std::max(S, B) + kPartTile - 1) / kPartTile;
   size_t bytes = 3 * al256((size_t)6 * G * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
-                 3 * al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * 4) + 2 * al256(8 * 4) +
+                 3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
+                 al256(8 * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B) + al256((size_t)B * sizeof(float4)) + 3 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)kMaxBins * part_tiles * 4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
@@ -155,8 +164,12 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   hkeys_ = A.take<uint32_t>(B);
   hkeys_sorted_ = A.take<uint32_t>(B);
   hperm_ = A.take<uint32_t>(B);
-  small_ = A.take<int>(8);
+  hhi_ = A.take<uint32_t>(B);
+  hhi_g_ = A.take<uint32_t>(B);
+  hperm1_ = A.take<uint32_t>(B);
+  ctr_ = A.take<Counters>(1);
   box6_ = A.take<uint32_t>(8);
+  plan_ = A.take<BatchPlan>(1);
   sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B)), B);
   hits_ = A.take<float4>(B);
   shadow_.o = A.take<float4>(B);
@@ -164,15 +177,32 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   shadow_.c = A.take<float4>(B);
   bins_.tile_counts = A.take<uint32_t>((size_t)kMaxBins * part_tiles);
   bins_.max_tiles = part_tiles;
-  bins_.count = small_;
-  bins_.err = small_ + 7;
+  bins_.count = ctr_->bin_count;
+  bins_.err = &ctr_->err;
   if (A.used > bytes) {
     err = "internal: device arena overflow";
     return MSC_ERR_CUDA;
   }
-  CK(cudaMemset(small_, 0, 8 * sizeof(int)));
-  CK(cudaMallocHost(&h_small_, 8 * sizeof(int)));
-  CK(cudaMallocHost(&h_counts_up_, 8 * sizeof(int)));
+  CK(cudaMemset(ctr_, 0, sizeof(Counters)));
+  CK(cudaMemset(plan_, 0, sizeof(BatchPlan)));
+  CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
+  memset(h_ctr_, 0, sizeof(Counters));
+  return MSC_OK;
+}
+
+int Core::scene_bounds(int id, float lo[3], float hi[3]) {
+  SceneGPU* sg = scene(id);
+  if (!sg) {
+    err = "no such scene";
+    return MSC_ERR_ARG;
+  }
+  float b[8];
+  CK(cudaMemcpyAsync(b, sg->bvh.bounds_dev, sizeof(b), cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  for (int i = 0; i < 3; ++i) {
+    lo[i] = b[i];
+    hi[i] = b[3 + i];
+  }
   return MSC_OK;
 }
 
@@ -248,6 +278,30 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
   r.num_lights = (int)d.lights.size();
   r.light_pick = r.num_lights > 0 ? 1.f / (float)r.num_lights : 0.f;
   r.tri_base = total_tris_;
+  r.hit_key_bits = d.ext.hit_key_bits;
+  if (!d.sphere_lights.empty()) {
+    std::vector<float4> sp;
+    for (int li : d.sphere_lights) {
+      const LightRec& L = d.lights[li];
+      sp.push_back(make_float4(L.centre[0], L.centre[1], L.centre[2], L.radius));
+    }
+    CK(cudaMalloc(&sg->d_spheres, sp.size() * sizeof(float4)));
+    CK(cudaMalloc(&sg->d_sphere_light, sp.size() * sizeof(int)));
+    CK(cudaMemcpy(sg->d_spheres, sp.data(), sp.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg->d_sphere_light, d.sphere_lights.data(), sp.size() * sizeof(int), cudaMemcpyHostToDevice));
+    r.spheres = sg->d_spheres;
+    r.sphere_light = sg->d_sphere_light;
+    r.num_spheres = (int)sp.size();
+  }
+  if (d.texels.res > 0) {
+    const size_t count = (size_t)T * d.texels.res * d.texels.res * 3;
+    CK(cudaMalloc(&sg->d_texels, count * sizeof(unsigned short)));
+    launch_face_texels(sg->d_texels, (int64_t)T, d.texels.res, d.texels.seed, stream_);
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaGetLastError());
+    r.texel_res = d.texels.res;
+    r.texels = sg->d_texels;
+  }
   if ((uint64_t)total_tris_ + (uint64_t)T + 1 >= (1ull << 32)) {
     err = "too many triangles across resident scenes";
     return MSC_ERR_ARG;
@@ -487,7 +541,7 @@ int Core::generate(bool* did) {
   for (auto& jp : jobs_)
     if (jp->slot >= 0 && !jp->complete) left_total += jp->paths - jp->generated;
   const uint64_t want = std::min<uint64_t>((uint64_t)staging_cap_, room);
-  if (want < std::min<uint64_t>((uint64_t)batch_cap_, left_total)) return MSC_OK;
+  if (want < std::min<uint64_t>((uint64_t)batch_size_, left_total)) return MSC_OK;
   uint64_t filled = 0;
   StageClock t(this, MSC_STAGE_RAYGEN);
   int launches = 0;
@@ -512,70 +566,172 @@ int Core::generate(bool* did) {
   return MSC_OK;
 }
 
-int Core::run_batch(const Segments& seg, int nb, int prefix_bits) {
+uint64_t Core::graph_key() const {
+  const uint64_t ns = scenes_.size();
+  const uint64_t k64 = (ns == 1 && scenes_[0]->rec.hit_key_bits == 64) ? 1 : 0;
+  return ns | (k64 << 15) | ((uint64_t)hit_bits_ << 16) | ((uint64_t)ray_sort << 24) | ((uint64_t)hit_sort << 25) |
+         ((uint64_t)merge_bins << 26) | ((uint64_t)wide_ << 27) | ((uint64_t)batch_size_ << 28) |
+         ((uint64_t)trace_block << 54) | (1ull << 63);
+}
+
+void Core::drop_graph() {
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
+  graph_key_ = 0;
+}
+
+// One batch body.  Every size is read on the device from the plan, so the
+// same launches serve any batch and can be captured once.
+int Core::enqueue_batch() {
   cudaStream_t st = stream_;
   const SceneRec& s0 = scenes_[0]->rec;
   const int ns = (int)scenes_.size();
+  const int B = batch_size_;
+  const int* nb = &plan_->nb;
+  int* errw = &ctr_->err;
+  int* shc = &ctr_->shadow_count;
+  int scene_bits = 0;
+  while ((1 << scene_bits) < ns) ++scene_bits;
+  {
+    StageClock t(this, MSC_STAGE_OTHER);
+    t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, box6_, ctr_, st));
+  }
   const uint32_t* perm = nullptr;
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      cudaMemsetAsync(box6_, 0xff, 12, st);
-      cudaMemsetAsync(box6_ + 3, 0x00, 12, st);
-      int l = launch_origin_box(bins_.rays.o, seg, box6_, st);
-      l += launch_ray_keys(bins_.rays.o, bins_.rays.d, seg, box6_, prefix_bits, keys_, st);
+      int l = launch_origin_box(bins_.rays.o, plan_, B, box6_, st);
+      l += launch_ray_keys(bins_.rays.o, bins_.rays.d, plan_, B, box6_, keys_, st);
       t.done(l);
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    t.done(sort_pairs(keys_, nullptr, keys_sorted_, perm_, nb, 32, ss_, st, small_ + 7));
+    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, 32, ss_, st, errw, nb);
+    if (l < 0) {
+      err = "internal: ray sort without distinct outputs";
+      return MSC_ERR_CUDA;
+    }
+    t.done(l);
     perm = perm_;
   }
   {
     StageClock t(this, MSC_STAGE_GATHER);
-    t.done(launch_gather(bins_.rays, seg, perm, batch_, st));
+    t.done(launch_gather(bins_.rays, plan_, B, perm, batch_, st));
   }
   {
     StageClock t(this, MSC_STAGE_TRACE);
-    t.done(launch_trace_closest(d_scenes_, ns, s0, batch_.o, batch_.d, nb, hits_, small_ + 7, st));
+    t.done(launch_trace_closest(d_scenes_, ns, s0, batch_.o, batch_.d, B, hits_, errw, st, nb, trace_block));
   }
   const uint32_t* order = nullptr;
-  if (hit_sort) {
+  if (hit_sort && ns == 1 && s0.hit_key_bits == 64) {
+    // 64-bit key: stable by the low word, then stable by the high word
     StageClock t(this, MSC_STAGE_HITSORT);
-    int l = launch_hit_keys(d_scenes_, batch_.d, hits_, nb, hkeys_, st);
-    l += sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, nb, hit_bits_, ss_, st, small_ + 7);
-    t.done(l);
+    int l = launch_hit_keys64(d_scenes_, hits_, B, hkeys_, hhi_, st, nb);
+    const int l1 = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm1_, B, 32, ss_, st, errw, nb);
+    l += launch_gather_u32(hhi_, hperm1_, B, hhi_g_, st, nb);
+    const int l2 = sort_pairs(hhi_g_, hperm1_, hhi_, hperm_, B, 32, ss_, st, errw, nb);
+    if (l1 < 0 || l2 < 0) {
+      err = "internal: hit sort without distinct outputs";
+      return MSC_ERR_CUDA;
+    }
+    t.done(l + l1 + l2);
+    order = hperm_;
+  } else if (hit_sort) {
+    StageClock t(this, MSC_STAGE_HITSORT);
+    int l = launch_hit_keys(d_scenes_, batch_.d, hits_, B, hkeys_, st, nb);
+    const int ls = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, B, hit_bits_, ss_, st, errw, nb);
+    if (ls < 0) {
+      err = "internal: hit sort without distinct outputs";
+      return MSC_ERR_CUDA;
+    }
+    t.done(l + ls);
     order = hperm_;
   }
   {
     StageClock t(this, MSC_STAGE_SHADE);
-    cudaMemsetAsync(small_ + 6, 0, sizeof(int), st);
-    t.done(launch_shade(d_scenes_, d_jobs_, film_, batch_, hits_, order, nb, staging_, shadow_, small_ + 6,
-                        d_job_done_, st));
+    t.done(launch_shade(d_scenes_, d_jobs_, film_, batch_, hits_, order, B, staging_, shadow_, shc, d_job_done_, st,
+                        nb));
   }
   {
     StageClock t(this, MSC_STAGE_SHADOW);
-    t.done(launch_trace_shadow(d_scenes_, ns, s0, shadow_, small_ + 6, nb, film_.rgb, small_ + 7, st));
+    t.done(launch_trace_shadow(d_scenes_, ns, s0, shadow_, shc, B, film_.rgb, errw, st, &ctr_->shadow,
+                               trace_block));
   }
   {
     StageClock t(this, MSC_STAGE_BINS);
-    t.done(launch_bin_partition(staging_, nb, bins_, st));
+    t.done(launch_bin_partition(staging_, B, bins_, st, nb));
   }
   return MSC_OK;
+}
+
+int Core::run_batches(int k) {
+  if (profiling || !use_graph) {
+    for (int i = 0; i < k; ++i) {
+      int rc = enqueue_batch();
+      if (rc != MSC_OK) return rc;
+    }
+    CK(cudaGetLastError());
+    return MSC_OK;
+  }
+  const uint64_t key = graph_key();
+  if (!graph_ || graph_key_ != key) {
+    drop_graph();
+    cudaGraph_t g = nullptr;
+    const uint64_t launches0 = stats.launches;
+    uint64_t stage0[12];
+    memcpy(stage0, stats.stage_launches, sizeof(stage0));
+    CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_batch();
+    cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+    if (rc != MSC_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) {
+      err = std::string("capturing the batch body: ") + cudaGetErrorString(ce);
+      return MSC_ERR_CUDA;
+    }
+    ce = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      graph_ = nullptr;
+      err = std::string("instantiating the batch graph: ") + cudaGetErrorString(ce);
+      return MSC_ERR_CUDA;
+    }
+    graph_launches_ = (int)(stats.launches - launches0);
+    stats.launches = launches0;  // counted per replay below
+    memcpy(stats.stage_launches, stage0, sizeof(stage0));
+    graph_key_ = key;
+  }
+  for (int i = 0; i < k; ++i) CK(cudaGraphLaunch(graph_, stream_));
+  stats.launches += (uint64_t)graph_launches_ * (uint64_t)k;
+  stats.graph_replays += (uint64_t)k;
+  return MSC_OK;
+}
+
+void Core::reset_stats() {
+  stats = CoreStats();
+  tune_pending_ = -1;  // a window in flight is not booked across a reset
+  if (ctr_) {
+    cudaMemsetAsync(&ctr_->closest, 0, 3 * sizeof(unsigned long long), stream_);
+    h_ctr_->closest = h_ctr_->shadow = h_ctr_->batches = 0;
+  }
 }
 
 int Core::step(bool* idle) {
   *idle = false;
   cudaStream_t st = stream_;
-  CK(cudaMemcpyAsync(h_small_, small_, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_ctr_, ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, st));
   if (max_slot_ >= 0)
     CK(cudaMemcpyAsync(h_job_done_, d_job_done_, (size_t)(max_slot_ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        st));
   CK(cudaStreamSynchronize(st));
   if (profiling) harvest();
-  if (last_was_batch_) stats.shadow += (uint64_t)h_small_[6];
-  last_was_batch_ = false;
-  if (h_small_[7] != 0) {
-    const int e = h_small_[7];
+  stats.closest = h_ctr_->closest;
+  stats.shadow = h_ctr_->shadow;
+  stats.batches = h_ctr_->batches;
+  if (tune_pending_ >= 0) tune_window_done();
+  if (h_ctr_->err != 0) {
+    const int e = h_ctr_->err;
     err = (e & ERR_BIN_OVERFLOW)    ? "a direction bin overflowed"
           : (e & ERR_TRAVERSAL_CAP) ? "BVH traversal exceeded its step cap"
           : (e & kSortErrLookback)  ? "radix sort look-back exceeded its spin cap"
@@ -597,41 +753,134 @@ int Core::step(bool* idle) {
   int rc = generate(&did);
   if (rc != MSC_OK) return rc;
   if (did) return MSC_OK;
-  // the next batch: the top of the fullest bin, topped up from the next
-  // fullest when merging is on and the fullest is short
-  int order[6] = {0, 1, 2, 3, 4, 5};
-  std::stable_sort(order, order + 6, [&](int a, int b) { return h_small_[a] > h_small_[b]; });
-  if (h_small_[order[0]] == 0) {
+  // enough batch bodies to take what the bins hold now (the device plans each one)
+  uint64_t total = 0, need = 0;
+  const uint64_t bs = (uint64_t)batch_size_;
+  for (int b = 0; b < 6; ++b) {
+    const uint64_t c = (uint64_t)std::max(0, h_ctr_->bin_count[b]);
+    total += c;
+    need += (c + bs - 1) / bs;
+  }
+  if (total == 0) {
     *idle = true;
     return MSC_OK;
   }
-  Segments seg;
-  memset(&seg, 0, sizeof(seg));
-  int nb = 0;
-  for (int k = 0; k < 6 && nb < batch_cap_; ++k) {
-    const int b = order[k];
-    const int cnt = h_small_[b];
-    if (cnt == 0) break;
-    if (k > 0 && !merge_bins) break;
-    const int take = std::min(batch_cap_ - nb, cnt);
-    seg.start[seg.count] = b * generation_ + cnt - take;
-    seg.prefix[seg.count] = nb;
-    seg.count += 1;
-    nb += take;
-    h_small_[b] = cnt - take;
-  }
-  seg.prefix[seg.count] = nb;
-  for (int k = 0; k < 6; ++k) h_counts_up_[k] = h_small_[k];
-  CK(cudaMemcpyAsync(small_, h_counts_up_, 6 * sizeof(int), cudaMemcpyHostToDevice, st));
-  int scene_bits = 0;
-  while ((1 << scene_bits) < (int)scenes_.size()) ++scene_bits;
-  const int prefix_bits = (seg.count > 1 || scene_bits > 0) ? scene_bits + 3 : 0;
-  rc = run_batch(seg, nb, prefix_bits);
-  if (rc != MSC_OK) return rc;
-  stats.closest += (uint64_t)nb;
-  stats.batches += 1;
-  last_was_batch_ = true;
+  if (merge_bins) need = (total + bs - 1) / bs;
+  int k = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)std::max(1, max_batches_per_step));
+  if (!tune_active_) return run_batches(k);
+  // a tuning window: this candidate's choice for at most two batch bodies
+  const int n = (int)tune_cands_.size();
+  const int c = tune_next_ % n;
+  apply(tune_cands_[c].choice);
+  k = std::min(k, 2);
+  tune_rays0_ = (double)(h_ctr_->closest + h_ctr_->shadow);
+  CK(cudaEventRecord(tune_ev_[0], stream_));
+  int rc2 = run_batches(k);
+  if (rc2 != MSC_OK) return rc2;
+  CK(cudaEventRecord(tune_ev_[1], stream_));
+  tune_pending_ = c;
+  tune_next_ += 1;
   return MSC_OK;
+}
+
+TuneChoice Core::choice() const {
+  TuneChoice c;
+  int e = 0;
+  while ((1 << (e + 1)) <= batch_size_) ++e;
+  c.batch_exp = e;
+  c.block = trace_block;
+  c.ray_sort = ray_sort;
+  c.hit_sort = hit_sort;
+  return c;
+}
+
+void Core::apply(const TuneChoice& c) {
+  const int e = std::max(6, std::min(c.batch_exp, 24));
+  batch_size_ = std::min(1 << e, batch_cap_);
+  trace_block = (c.block == 64 || c.block == 256) ? c.block : 128;
+  ray_sort = c.ray_sort;
+  hit_sort = c.hit_sort;
+}
+
+void Core::start_autotune(int windows) {
+  tune_windows_ = std::max(1, windows);
+  tune_active_ = true;
+  tune_dim_ = 0;
+  tune_pending_ = -1;
+  tune_log.clear();
+  tune_begin_dim();
+}
+
+// Candidates along one dimension around the current choice.
+void Core::tune_begin_dim() {
+  for (;;) {
+    const TuneChoice base = choice();
+    tune_cands_.clear();
+    tune_next_ = 0;
+    auto add = [&](TuneChoice c) {
+      TuneSample t;
+      t.choice = c;
+      tune_cands_.push_back(t);
+    };
+    if (tune_dim_ == 0) {
+      for (int e = 18; e <= 21; ++e)
+        if ((1 << e) <= batch_cap_) {
+          TuneChoice c = base;
+          c.batch_exp = e;
+          add(c);
+        }
+    } else if (tune_dim_ == 1) {
+      for (int b : {64, 128, 256}) {
+        TuneChoice c = base;
+        c.block = b;
+        add(c);
+      }
+    } else if (tune_dim_ == 2) {
+      for (bool on : {true, false}) {
+        TuneChoice c = base;
+        c.ray_sort = on;
+        add(c);
+      }
+    } else if (tune_dim_ == 3) {
+      for (bool on : {true, false}) {
+        TuneChoice c = base;
+        c.hit_sort = on;
+        add(c);
+      }
+    } else {
+      tune_active_ = false;
+      return;
+    }
+    if (tune_cands_.size() > 1) return;
+    ++tune_dim_;
+  }
+}
+
+// Called at a step's start, after the sync: books the window that just ended.
+void Core::tune_window_done() {
+  if (tune_pending_ < 0) return;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, tune_ev_[0], tune_ev_[1]) == cudaSuccess) {
+    TuneSample& t = tune_cands_[tune_pending_];
+    t.rays += (double)(h_ctr_->closest + h_ctr_->shadow) - tune_rays0_;
+    t.ms += ms;
+  }
+  tune_pending_ = -1;
+  if (tune_next_ < (int)tune_cands_.size() * tune_windows_) return;
+  int best = -1;
+  double best_rate = -1.0;
+  for (int i = 0; i < (int)tune_cands_.size(); ++i) {
+    const TuneSample& t = tune_cands_[i];
+    const double rate = t.ms > 0 ? t.rays / t.ms : -1.0;
+    if (rate > best_rate) {
+      best_rate = rate;
+      best = i;
+    }
+    tune_log.push_back(t);
+  }
+  if (best >= 0) apply(tune_cands_[best].choice);
+  ++tune_dim_;
+  tune_begin_dim();
 }
 
 int Core::run_all(const volatile bool* stop) {

@@ -35,6 +35,9 @@ struct SceneGPU {
   ShaderRec* d_shaders = nullptr;
   GeomRec* d_geoms = nullptr;
   LightRec* d_lights = nullptr;
+  float4* d_spheres = nullptr;        // sphere lights: centre, radius
+  int* d_sphere_light = nullptr;
+  unsigned short* d_texels = nullptr; // face texels (FP16 bits)
   std::vector<int> h_tri_orig;  // leaf order -> global triangle index
   SceneRec rec;
   ~SceneGPU();
@@ -64,8 +67,23 @@ struct JobState {
   double t_submit = 0, t_admit = 0, t_done = 0;
 };
 
+// One point of the tuning space of the batch loop.  None of these changes a
+// result: every path draws its own random sequence and adds to its own sample
+// in bounce order, whatever batch it rides in.
+struct TuneChoice {
+  int batch_exp = 20;   // rays per batch = 2^batch_exp (at most the allocated capacity)
+  int block = 128;      // traversal block size: 64, 128 or 256
+  bool ray_sort = true; // origin/direction key sort of each batch
+  bool hit_sort = true; // (geomID, primID) sort of each batch's hits
+};
+
+struct TuneSample {
+  TuneChoice choice;
+  double rays = 0, ms = 0;  // rays traced and device time over the sample windows
+};
+
 struct CoreStats {
-  uint64_t closest = 0, shadow = 0, batches = 0, launches = 0, generations = 0;
+  uint64_t closest = 0, shadow = 0, batches = 0, launches = 0, generations = 0, graph_replays = 0;
   double stage_ms[12] = {0};
   uint64_t stage_launches[12] = {0};
 };
@@ -78,11 +96,26 @@ class Core {
   bool ray_sort = true, hit_sort = true;
   bool merge_bins = true;  // let a batch take rays of several bins when the fullest is short
   int max_active = 0;      // jobs admitted at once (0 = no limit); 1 gives the one-job-at-a-time loop
+  bool use_graph = true;   // replay the batch body from a captured CUDA graph (eager launches when profiling)
+  int max_batches_per_step = 16;  // batch bodies enqueued between two host looks at the counters
+  int trace_block = 128;          // traversal block size
+
+  // Online autotuner: while on, the next batches are spread over candidate
+  // choices (coordinate descent: batch size, then traversal block, then the
+  // two sorts), each timed on the device over a few windows; the fastest in
+  // rays per ms is kept.  Results are the same under any choice.
+  void start_autotune(int windows_per_candidate = 2);
+  void stop_autotune() { tune_active_ = false; tune_pending_ = -1; }
+  bool tuning() const { return tune_active_; }
+  TuneChoice choice() const;
+  void apply(const TuneChoice& c);
+  std::vector<TuneSample> tune_log;
 
   ~Core();
   // batch_exponent: rays per batch (2^e); generation: paths in flight; samples: film capacity.
   int init(int batch_exponent, int generation, size_t sample_capacity, bool wide);
   int add_scene(const SceneDesc& d, int* id);
+  int scene_bounds(int id, float lo[3], float hi[3]);  // the device BVH's root box
   // Admits a job if its film fits; returns MSC_ERR_BUSY when it does not (yet).
   int add_job(const JobSpec& spec, int* id);
   // Starts the next iteration of a finished job (same film, next random sequence).
@@ -92,6 +125,8 @@ class Core {
   int step(bool* idle);
   // Steps until every admitted job is complete (or `stop` becomes true).
   int run_all(const volatile bool* stop = nullptr);
+  // Zeroes the statistics and the device ray counters (stream-ordered).
+  void reset_stats();
   int copy_image(int id);
   cudaStream_t stream() const { return stream_; }
   JobState* job(int id) { return (id >= 0 && id < (int)jobs_.size()) ? jobs_[id].get() : nullptr; }
@@ -101,13 +136,16 @@ class Core {
   size_t sample_capacity() const { return sample_cap_; }
   Film film() const { return film_; }
   int batch_cap() const { return batch_cap_; }
+  int batch_size() const { return batch_size_; }
   double now() const;
   // Closest hit / occlusion of explicit rays against scene 0 (stage entry points).
   int trace_closest(const float* org, const float* dir, int n, float4* hits_host);
   int trace_occluded(const float* org, const float* dir, const float* tmax, int n, int* occluded);
 
  private:
-  int run_batch(const Segments& seg, int nb, int prefix_bits);
+  int enqueue_batch();            // one batch body: plan, sort, trace, shade, shadow, re-bin
+  int run_batches(int k);         // k batch bodies (graph replays or eager)
+  void drop_graph();
   int finish_job(JobState& j);
   int generate(bool* did);
   bool alloc_samples(size_t n, size_t* off);
@@ -117,6 +155,17 @@ class Core {
   cudaStream_t stream_ = nullptr;
   bool wide_ = true;
   int batch_cap_ = 0, generation_ = 0, staging_cap_ = 0;
+  int batch_size_ = 0;  // rays per batch now (<= batch_cap_)
+  // autotuner state
+  bool tune_active_ = false;
+  int tune_dim_ = 0, tune_windows_ = 2;
+  std::vector<TuneSample> tune_cands_;
+  int tune_next_ = 0;           // candidate of the next window
+  int tune_pending_ = -1;       // candidate timed by the window in flight
+  double tune_rays0_ = 0;
+  cudaEvent_t tune_ev_[2] = {nullptr, nullptr};
+  void tune_begin_dim();
+  void tune_window_done();
   std::vector<std::unique_ptr<SceneGPU>> scenes_;
   std::vector<std::unique_ptr<JobState>> jobs_;
   std::vector<int> free_slots_;
@@ -138,14 +187,17 @@ class Core {
   BinPool bins_;
   RayBuf staging_, batch_;
   uint32_t *keys_ = nullptr, *keys_sorted_ = nullptr, *perm_ = nullptr, *hkeys_ = nullptr, *hkeys_sorted_ = nullptr,
-           *hperm_ = nullptr, *box6_ = nullptr;
+           *hperm_ = nullptr, *box6_ = nullptr, *hhi_ = nullptr, *hhi_g_ = nullptr, *hperm1_ = nullptr;
   SortScratch ss_;
   float4* hits_ = nullptr;
   ShadowBuf shadow_;
-  int* small_ = nullptr;   // [0..5] bin counts, [6] shadow count, [7] error bits
-  int* h_small_ = nullptr;
-  int* h_counts_up_ = nullptr;
-  bool last_was_batch_ = false;
+  Counters* ctr_ = nullptr;    // device counters
+  Counters* h_ctr_ = nullptr;  // pinned copy
+  BatchPlan* plan_ = nullptr;
+  cudaGraphExec_t graph_ = nullptr;
+  uint64_t graph_key_ = 0;
+  int graph_launches_ = 0;     // kernels in one replay
+  uint64_t graph_key() const;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> stage_events_;
   std::vector<cudaEvent_t> event_pool_;
   size_t event_used_ = 0;

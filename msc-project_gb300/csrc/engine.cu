@@ -193,7 +193,7 @@ int process_impl(msc_handle* h, int* iteration, bool copy_image) {
       return rc;
     }
   }
-  c.stats = CoreStats();
+  c.reset_stats();
   cudaEventRecord(h->ev_begin, c.stream());
   struct Watch {  // mirror terminate() into the core's stop flag while running
     msc_handle* h;
@@ -535,19 +535,27 @@ int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys
   uint32_t* mem = nullptr;
   int rc = MSC_OK;
   if (upload_f4(org, n, 3, 3, &o, 0.f) || upload_f4(dir, n, 3, 3, &d, 0.f)) rc = MSC_ERR_CUDA;
+  BatchPlan* plan = nullptr;
   if (rc == MSC_OK && cudaMalloc(&mem, (size_t)(n + 8) * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && cudaMalloc(&plan, sizeof(BatchPlan)) != cudaSuccess) rc = MSC_ERR_CUDA;
   if (rc == MSC_OK) {
     uint32_t* box = mem + n;
     cudaMemset(box, 0xff, 12);
     cudaMemset(box + 3, 0, 12);
-    const Segments seg = one_segment(0, n);
-    launch_origin_box(o, seg, box, 0);
-    launch_ray_keys(o, d, seg, box, 0, mem, 0);
+    BatchPlan hp;
+    memset(&hp, 0, sizeof(hp));
+    hp.seg = one_segment(0, n);
+    hp.nb = n;
+    hp.prefix_bits = 0;
+    cudaMemcpy(plan, &hp, sizeof(hp), cudaMemcpyHostToDevice);
+    launch_origin_box(o, plan, n, box, 0);
+    launch_ray_keys(o, d, plan, n, box, mem, 0);
     if (cudaMemcpy(keys, mem, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MSC_ERR_CUDA;
   }
   if (o) cudaFree(o);
   if (d) cudaFree(d);
   if (mem) cudaFree(mem);
+  if (plan) cudaFree(plan);
   return rc;
 }
 
@@ -747,6 +755,17 @@ int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id) {
   return rc;
 }
 
+int msc_batch_scene_info(msc_batch* b, int scene, float lo[3], float hi[3], int64_t* triangles) {
+  if (!b || !lo || !hi) return MSC_ERR_ARG;
+  int rc = guarded(&b->err, [&] { return b->core.scene_bounds(scene, lo, hi); });
+  if (rc != MSC_OK) {
+    b->err = b->core.err;
+    return rc;
+  }
+  if (triangles) *triangles = (int64_t)b->core.scene(scene)->bvh.num_tris;
+  return MSC_OK;
+}
+
 int msc_batch_submit(msc_batch* b, const msc_job_desc* desc, int* job_id) {
   if (!b || !desc || !job_id) return MSC_ERR_ARG;
   int rc = guarded(&b->err, [&] { return b->core.add_job(spec_of(*desc), job_id); });
@@ -756,7 +775,7 @@ int msc_batch_submit(msc_batch* b, const msc_job_desc* desc, int* job_id) {
 
 int msc_batch_run(msc_batch* b) {
   if (!b) return MSC_ERR_ARG;
-  b->core.stats = CoreStats();
+  b->core.reset_stats();
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -807,6 +826,55 @@ int msc_batch_get_stats(msc_batch* b, msc_stats* out) {
   return MSC_OK;
 }
 
+int msc_batch_autotune(msc_batch* b, int windows) {
+  if (!b || windows < 0) return MSC_ERR_ARG;
+  b->core.start_autotune(windows == 0 ? 2 : windows);
+  return MSC_OK;
+}
+
+int msc_batch_get_tuning(msc_batch* b, msc_tuning* out) {
+  if (!b || !out) return MSC_ERR_ARG;
+  const TuneChoice c = b->core.choice();
+  out->batch_exponent = c.batch_exp;
+  out->trace_block = c.block;
+  out->ray_sort = c.ray_sort ? 1 : 0;
+  out->hit_sort = c.hit_sort ? 1 : 0;
+  out->tuning = b->core.tuning() ? 1 : 0;
+  out->samples = (int)b->core.tune_log.size();
+  return MSC_OK;
+}
+
+int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in) {
+  if (!b || !in) return MSC_ERR_ARG;
+  if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > b->core.batch_cap() ||
+      (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256)) {
+    b->err = "tuning: batch exponent above the capacity or block size not 64, 128 or 256";
+    return MSC_ERR_ARG;
+  }
+  TuneChoice c;
+  c.batch_exp = in->batch_exponent;
+  c.block = in->trace_block;
+  c.ray_sort = in->ray_sort != 0;
+  c.hit_sort = in->hit_sort != 0;
+  b->core.stop_autotune();
+  b->core.apply(c);
+  return MSC_OK;
+}
+
+int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {
+  if (!b || !n || cap < 0 || (cap > 0 && !out)) return MSC_ERR_ARG;
+  const auto& log = b->core.tune_log;
+  *n = (int)log.size();
+  for (int i = 0; i < cap && i < (int)log.size(); ++i) {
+    out[i].batch_exponent = log[i].choice.batch_exp;
+    out[i].trace_block = log[i].choice.block;
+    out[i].ray_sort = log[i].choice.ray_sort ? 1 : 0;
+    out[i].hit_sort = log[i].choice.hit_sort ? 1 : 0;
+    out[i].mrays_per_s = log[i].ms > 0 ? log[i].rays / log[i].ms / 1e3 : 0.0;
+  }
+  return MSC_OK;
+}
+
 int msc_batch_set_profiling(msc_batch* b, int on) {
   if (!b) return MSC_ERR_ARG;
   b->core.profiling = on != 0;
@@ -825,7 +893,7 @@ int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* 
   if (!b || n < 0 || (n > 0 && (!reqs || !results)) || !stats) return MSC_ERR_ARG;
   return guarded(&b->err, [&]() -> int {
     Core& c = b->core;
-    c.stats = CoreStats();
+    c.reset_stats();
     std::vector<int> order((size_t)n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int x) { return reqs[a].arrival_s < reqs[x].arrival_s; });

@@ -136,9 +136,12 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity);
 // unless they alias the outputs.  One histogram kernel for all passes, then
 // one kernel per 8-bit pass with a decoupled look-back across tiles.  Spin
 // waits are capped; a cap that runs out sets bit 8 of *err (when err is not
-// null).  Returns the number of kernel launches.
+// null).  Returns the number of kernel launches.  n_dev (optional): the pair
+// count is read on the device when the kernels run and n is its upper bound
+// (sizes the grids); this form needs outputs distinct from the inputs when
+// the pass count is odd, and returns -1 otherwise.
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr);
+               int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr);
 
 // The same order with three kernels per pass (upsweep count, one-block scan,
 // downsweep scatter) and no inter-block waiting.

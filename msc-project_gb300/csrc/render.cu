@@ -5,6 +5,8 @@
 
 #include "radix.cuh"
 #include "render.h"
+
+#include <cuda_fp16.h>
 #include "trace.cuh"
 
 namespace mscg {
@@ -136,8 +138,14 @@ __device__ __forceinline__ int ray_digit(const float4& d) {
   return cardinal_bin(f3(d));
 }
 
-__global__ void __launch_bounds__(PB) k_part_count(const float4* __restrict__ d, int n, uint32_t* __restrict__ counts,
+__device__ __forceinline__ int dev_count(int n_max, const int* n_dev) {
+  return n_dev ? min(*n_dev, n_max) : n_max;
+}
+
+__global__ void __launch_bounds__(PB) k_part_count(const float4* __restrict__ d, int n_max,
+                                                   const int* __restrict__ n_dev, uint32_t* __restrict__ counts,
                                                    int tiles) {
+  const int n = dev_count(n_max, n_dev);
   __shared__ int hist[PRADIX];
   if (threadIdx.x < PRADIX) hist[threadIdx.x] = 0;
   __syncthreads();
@@ -153,8 +161,10 @@ __global__ void __launch_bounds__(PB) k_part_count(const float4* __restrict__ d,
   if (threadIdx.x < PRADIX) counts[threadIdx.x * tiles + blockIdx.x] = (uint32_t)hist[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n, const uint32_t* __restrict__ scanned, int tiles,
-                                                     RayBuf dst, int cap, const int* __restrict__ bin_count) {
+__global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, const int* __restrict__ n_dev,
+                                                     const uint32_t* __restrict__ scanned, int tiles, RayBuf dst,
+                                                     int cap, const int* __restrict__ bin_count) {
+  const int n = dev_count(n_max, n_dev);
   __shared__ RankSmem<PB, PRADIX> sm;
   __shared__ uint32_t sidx[kPartTile];
   __shared__ int gofs[PRADIX];
@@ -206,10 +216,62 @@ __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict_
   if (i < n) out[i] = cardinal_bin(f3(d[i]));
 }
 
+// ------------------------------------------------------------ batch plan
+// Pathtracer::batchLoading (src/core/Pathtracer.cpp:294-306) pops the next
+// full batch, else flushes the fullest bin.  Here: the fullest bin's top
+// (LIFO), topped up from the next fullest bins (ties to the lower bin) while
+// `merge` is set and the batch is short.  One thread; the bins are six.
+__global__ void k_plan(int* bin_count, int cap, int batch_cap, int merge, int scene_bits, BatchPlan* plan,
+                       uint32_t* box6, Counters* ctr) {
+  if (threadIdx.x != 0) return;
+  int cnt[6], order[6];
+  for (int b = 0; b < 6; ++b) {
+    cnt[b] = bin_count[b];
+    order[b] = b;
+  }
+  for (int a = 1; a < 6; ++a) {  // stable insertion sort, count descending
+    const int o = order[a];
+    int k = a;
+    while (k > 0 && cnt[order[k - 1]] < cnt[o]) {
+      order[k] = order[k - 1];
+      --k;
+    }
+    order[k] = o;
+  }
+  BatchPlan p;
+  p.seg.count = 0;
+  int nb = 0;
+  for (int k = 0; k < 6 && nb < batch_cap; ++k) {
+    const int b = order[k];
+    const int c = cnt[b];
+    if (c == 0) break;
+    if (k > 0 && !merge) break;
+    const int take = min(batch_cap - nb, c);
+    p.seg.start[p.seg.count] = b * cap + c - take;
+    p.seg.prefix[p.seg.count] = nb;
+    p.seg.count += 1;
+    nb += take;
+    bin_count[b] = c - take;
+  }
+  for (int k = p.seg.count; k < 6; ++k) p.seg.start[k] = 0;
+  for (int k = p.seg.count; k < 7; ++k) p.seg.prefix[k] = nb;
+  p.nb = nb;
+  p.prefix_bits = (p.seg.count > 1 || scene_bits > 0) ? scene_bits + 3 : 0;
+  *plan = p;
+  for (int a = 0; a < 3; ++a) {
+    box6[a] = 0xffffffffu;
+    box6[3 + a] = 0u;
+  }
+  ctr->shadow_count = 0;
+  ctr->closest += (unsigned long long)nb;
+  ctr->batches += nb > 0 ? 1ull : 0ull;
+}
+
 // ------------------------------------------------------------ ray keys
 // RayBoundingbox (src/core/RayBoundingbox.cpp:5-50): origin box of the batch.
-__global__ void k_origin_box(const float4* __restrict__ o, Segments seg, uint32_t* box6) {
-  const int n = seg.prefix[seg.count];
+__global__ void k_origin_box(const float4* __restrict__ o, const BatchPlan* __restrict__ plan, uint32_t* box6) {
+  const Segments seg = plan->seg;
+  const int n = plan->nb;
   float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 p = o[seg_source(seg, i)];
@@ -230,11 +292,13 @@ __global__ void k_origin_box(const float4* __restrict__ o, Segments seg, uint32_
 }
 
 __global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d,
-                                                 Segments seg, const uint32_t* __restrict__ box6, int prefix_bits,
-                                                 uint32_t* __restrict__ keys) {
-  const int n = seg.prefix[seg.count];
+                                                 const BatchPlan* __restrict__ plan,
+                                                 const uint32_t* __restrict__ box6, uint32_t* __restrict__ keys) {
+  const int n = plan->nb;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const Segments& seg = plan->seg;
+  const int prefix_bits = plan->prefix_bits;
   const int src = seg_source(seg, i);
   float3 lo = f3(ord2f(box6[0]), ord2f(box6[1]), ord2f(box6[2]));
   float3 hi = f3(ord2f(box6[3]), ord2f(box6[4]), ord2f(box6[5]));
@@ -250,11 +314,12 @@ __global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, c
 }
 
 // RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
-__global__ void __launch_bounds__(TB) k_gather(RayBuf src, Segments seg, const uint32_t* __restrict__ perm,
-                                               RayBuf dst) {
-  const int n = seg.prefix[seg.count];
+__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const BatchPlan* __restrict__ plan,
+                                               const uint32_t* __restrict__ perm, RayBuf dst) {
+  const int n = plan->nb;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
+  const Segments& seg = plan->seg;
   const int i = seg_source(seg, perm ? (int)perm[j] : j);
   dst.o[j] = src.o[i];
   dst.d[j] = src.d[i];
@@ -291,19 +356,67 @@ __device__ __forceinline__ int ovf_bits(int ovf) {
   return ovf == 1 ? ERR_STACK_OVERFLOW : (ovf == 2 ? ERR_TRAVERSAL_CAP : ERR_BVH_INDEX);
 }
 
+// ------------------------------------------------------- sphere lights
+// First intersection of o + t d with the sphere (centre sp.xyz, radius sp.w)
+// in (tmin, tmax), else -1.
+__device__ __forceinline__ float sphere_hit_t(float3 o, float3 d, float4 sp, float tmin, float tmax) {
+  const float3 oc = v_sub(o, f3(sp.x, sp.y, sp.z));
+  const float a = v_dot(d, d);
+  const float b = v_dot(oc, d);
+  const float c = v_dot(oc, oc) - sp.w * sp.w;
+  const float disc = b * b - a * c;
+  if (disc < 0.f) return -1.f;
+  const float q = sqrtf(disc);
+  const float t0 = (-b - q) / a;
+  if (t0 > tmin && t0 < tmax) return t0;
+  const float t1 = (-b + q) / a;
+  if (t1 > tmin && t1 < tmax) return t1;
+  return -1.f;
+}
+
+// Solid-angle pdf of sampling the sphere's cone of directions uniformly from p
+// (0 when p is inside): 1 / (2 pi (1 - cos theta_max)), with
+// 1 - cos theta_max = s2 / (1 + sqrt(1 - s2)), s2 = r^2 / |c - p|^2.
+__device__ __forceinline__ float sphere_cone_pdf(float3 p, float3 c, float r) {
+  const float3 wc = v_sub(c, p);
+  const float d2 = v_dot(wc, wc);
+  const float r2 = r * r;
+  if (!(d2 > r2)) return 0.f;
+  const float s2 = r2 / d2;
+  const float omc = s2 / (1.f + sqrtf(1.f - s2));
+  return 1.f / ((2.f * MSC_PI) * omc);
+}
+
+// Closest sphere light hit nearer than h->t (triangles win ties).
+__device__ __forceinline__ void trace_spheres(const SceneRec& sr, float3 o, float3 d, TriHit* h) {
+  const int ns = sr.num_spheres;
+  for (int q = 0; q < ns; ++q) {
+    const float t = sphere_hit_t(o, d, __ldg(&sr.spheres[q]), MSC_TNEAR, h->t);
+    if (t > 0.f) {
+      h->t = t;
+      h->u = 0.f;
+      h->v = 0.f;
+      h->tri = sphere_hit_code(q);
+    }
+  }
+}
+
 // MULTI: look each ray's scene up in the table; else every ray uses scene0.
-template <bool WIDE, bool MULTI>
-__global__ void __launch_bounds__(128) k_trace_closest(const SceneRec* __restrict__ scenes, BvhRef scene0,
-                                                       const float4* __restrict__ o, const float4* __restrict__ d, int n,
+template <bool WIDE, bool MULTI, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_trace_closest(const SceneRec* __restrict__ scenes, BvhRef scene0,
+                                                       const float4* __restrict__ o, const float4* __restrict__ d,
+                                                       int n_max, const int* __restrict__ n_dev,
                                                        float4* __restrict__ hits, int* err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= dev_count(n_max, n_dev)) return;
   float4 ro = o[i], rd = d[i];
-  const BvhRef b = MULTI ? bvh_of(scenes[info_scene(__float_as_int(rd.w))], WIDE) : scene0;
+  const int sc = MULTI ? info_scene(__float_as_int(rd.w)) : 0;
+  const BvhRef b = MULTI ? bvh_of(scenes[sc], WIDE) : scene0;
   TriHit h;
   h.t = MSC_TFAR; h.u = 0.f; h.v = 0.f; h.tri = -1;
   int ovf = 0;
   scene_trace<WIDE, false>(b, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR, &h, &ovf);
+  if (scenes[sc].num_spheres > 0) trace_spheres(scenes[sc], f3(ro), f3(rd), &h);
   if (ovf) atomicOr(err, ovf_bits(ovf));
   hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
@@ -313,16 +426,66 @@ __global__ void __launch_bounds__(128) k_trace_closest(const SceneRec* __restric
 // follow each other, so tri_base + global triangle index + 1 orders exactly
 // like (scene, geomID, primID), and 0 is a miss.
 __global__ void __launch_bounds__(TB) k_hit_keys(const SceneRec* __restrict__ scenes, const float4* __restrict__ d,
-                                                 const float4* __restrict__ hits, int n, uint32_t* __restrict__ keys) {
+                                                 const float4* __restrict__ hits, int n_max,
+                                                 const int* __restrict__ n_dev, uint32_t* __restrict__ keys) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= dev_count(n_max, n_dev)) return;
   int k = __float_as_int(hits[i].w);
-  if (k < 0) {
+  if (k < 0) {  // misses and sphere-light hits first
     keys[i] = 0u;
     return;
   }
   const SceneRec& sc = scenes[info_scene(__float_as_int(d[i].w))];
   keys[i] = sc.tri_base + (uint32_t)sc.tri_orig[k] + 1u;
+}
+
+// The 64-bit hit key of one scene: shader id (12 bits) | original face index
+// (23 bits) | u quantised to 15 bits | v to 14 bits.  Misses and sphere-light
+// hits take 0, so they come first as in CompareHit.
+__global__ void __launch_bounds__(TB) k_hit_keys64(const SceneRec* __restrict__ scenes, const float4* __restrict__ hits,
+                                                   int n_max, const int* __restrict__ n_dev, uint32_t* __restrict__ lo,
+                                                   uint32_t* __restrict__ hi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= dev_count(n_max, n_dev)) return;
+  const float4 h = hits[i];
+  const int k = __float_as_int(h.w);
+  uint64_t key = 0;
+  if (k >= 0) {
+    const SceneRec& sc = scenes[0];
+    const float4 ta = __ldg(&sc.tris[3 * k]);
+    const uint64_t shader = (uint64_t)(sc.geoms[__float_as_int(ta.w)].shader & 0xfff);
+    const uint64_t face = (uint64_t)(__ldg(&sc.tri_orig[k]) & 0x7fffff);
+    const uint64_t uq = (uint64_t)min(32767, max(0, (int)(h.y * 32768.f)));
+    const uint64_t vq = (uint64_t)min(16383, max(0, (int)(h.z * 16384.f)));
+    key = (shader << 52) | (face << 29) | (uq << 14) | vq;
+  }
+  lo[i] = (uint32_t)key;
+  hi[i] = (uint32_t)(key >> 32);
+}
+
+__global__ void __launch_bounds__(TB) k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
+                                                   int n_max, const int* __restrict__ n_dev,
+                                                   uint32_t* __restrict__ dst) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= dev_count(n_max, n_dev)) return;
+  dst[i] = src[idx[i]];
+}
+
+// FP16 bits of k / 1024 for a 10-bit k (exact: k / 1024 has at most 10 significant bits).
+__device__ __forceinline__ unsigned short k1024_half_bits(uint32_t k) {
+  if (k == 0u) return 0;
+  const int e = 31 - __clz((int)k);  // 0..9
+  return (unsigned short)(((e + 5) << 10) | ((k << (10 - e)) & 0x3ffu));
+}
+
+__global__ void k_face_texels(unsigned short* __restrict__ texels, int64_t total, int res, uint32_t seed) {
+  const int per_face = res * res * 3;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t face = (uint32_t)(x / per_face);
+    const int r = (int)(x - (int64_t)face * per_face);
+    texels[x] = k1024_half_bits(face_texel_code(seed, face, (uint32_t)(r / 3), (uint32_t)(r % 3)));
+  }
 }
 
 // ------------------------------------------------------------------ shading
@@ -334,11 +497,11 @@ struct BsdfEval {
 
 // LambertShader::evaluate (src/core/LambertShader.cpp:27-47), NullShader::evaluate
 // (src/core/NullShader.cpp:25-39) and the Phong extension.
-__device__ __forceinline__ BsdfEval bsdf_evaluate(const ShaderRec& s, float3 wi, float3 wo, float3 n) {
+// col: the texture colour at the hit.
+__device__ __forceinline__ BsdfEval bsdf_evaluate(const ShaderRec& s, float3 col, float3 wi, float3 wo, float3 n) {
   BsdfEval e;
   const float ci = v_dot(n, wi);
   const float co = v_dot(n, wo);
-  const float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
   if (s.type == SHADER_NULL) {
     e.f = f3(0.f, 0.f, 0.f);
     e.cos_theta = 1.f;
@@ -375,9 +538,12 @@ __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z)
 // job_done[j] counts the finished paths of job j.
 __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
                                               Film film, RayBuf batch, const float4* __restrict__ hits,
-                                              const uint32_t* __restrict__ order, int n, RayBuf next, ShadowBuf sh,
+                                              const uint32_t* __restrict__ order, int n_max,
+                                              const int* __restrict__ n_dev, RayBuf next, ShadowBuf sh,
                                               int* sh_count, uint32_t* job_done) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = dev_count(n_max, n_dev);
+  if (blockIdx.x * blockDim.x >= n) return;  // whole block past the batch
   const bool live = j < n;
   bool emit = false, cont = false;
   int job = -1;
@@ -395,7 +561,18 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
     const JobRec& f = jobs[job];
     const uint32_t sample = f.sample_base + (uint32_t)sid;
     const float3 w = f3(rw);
-    if (k >= 0) {  // a miss adds nothing (Integrator.cpp:26-27)
+    if (k < -1) {  // a sphere light (extension): uniform radiance on its outside
+      const SceneRec& sc = scenes[scene];
+      const LightRec& L = sc.lights[sc.sphere_light[-2 - k]];
+      const float3 dn = v_normalize(f3(rd));
+      const float3 c = f3(L.centre[0], L.centre[1], L.centre[2]);
+      const float3 pos = v_add(f3(ro), v_mul(dn, h.x));
+      const float3 nl = v_mul(v_sub(pos, c), 1.f / L.radius);
+      const float le = v_dot(nl, v_neg(dn)) < 0.f ? 0.f : L.intensity;
+      float mis = 1.0f;
+      if (depth > 0) mis = mis_weight(ro.w, sphere_cone_pdf(f3(ro), c, L.radius) * sc.light_pick, f.mis_power);
+      if (le > MSC_EPSILON) add_rgb(&film.rgb[sample], f3(le * mis * w.x, le * mis * w.y, le * mis * w.z));
+    } else if (k >= 0) {  // a miss adds nothing (Integrator.cpp:26-27)
       const SceneRec& sc = scenes[scene];
       const float4 ta = __ldg(&sc.tris[3 * k + 0]);
       const float4 tb = __ldg(&sc.tris[3 * k + 1]);
@@ -421,24 +598,63 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
         const float3 nrm = v_normalize(v_cross(f3(tb), f3(tc)));  // = -normalize(Ng) (Integrator.cpp:121-125)
         const float3 pos = v_add(f3(ro), v_mul(dn, t));
         const float3 wo = v_neg(dn);
+        // texture colour (ConstantTexture.cpp:22-25; face texels: extension)
+        float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
+        if (s.texture == TEXTURE_FACE && sc.texel_res > 0) {
+          const int res = sc.texel_res;
+          const int ti = min(res - 1, max(0, (int)(h.y * (float)res)));
+          const int tj = min(res - 1, max(0, (int)(h.z * (float)res)));
+          const size_t tx = ((size_t)__ldg(&sc.tri_orig[k]) * (size_t)(res * res) + (size_t)(tj * res + ti)) * 3;
+          col = f3(col.x * __half2float(__ushort_as_half(__ldg(&sc.texels[tx + 0]))),
+                   col.y * __half2float(__ushort_as_half(__ldg(&sc.texels[tx + 1]))),
+                   col.z * __half2float(__ushort_as_half(__ldg(&sc.texels[tx + 2]))));
+        }
         const uint4 ra = path_draws((uint32_t)sid, f.iter_seed, (uint32_t)depth + 1u, 0u);
         // next-event estimation (Integrator.cpp:103-178)
         if (sc.num_lights > 0) {
           int li = (int)((float)sc.num_lights * u01(ra.x));
           if (li >= sc.num_lights) li = sc.num_lights - 1;
           const LightRec& L = sc.lights[li];
-          // QuadLight::illuminate (src/core/QuadLight.cpp:41-67)
-          const float3 smp = xf_point(L.xf, f3(0.f, u01(ra.y) - 0.5f, u01(ra.z) - 0.5f));
-          const float3 ln = f3(L.normal[0], L.normal[1], L.normal[2]);
-          float cosl = v_dot(v_normalize(v_sub(pos, smp)), ln);
-          const float le = cosl < 0.f ? 0.f : L.intensity;
-          cosl = cosl < 0.f ? 0.f : cosl;
-          const float3 tol = v_sub(smp, pos);
-          const float3 wi = v_normalize(tol);
-          const float dist = v_len(tol);
-          const float pdfw = (v_dot(tol, tol) / cosl) / (L.scale[0] * L.scale[1]);
+          float3 wi;
+          float dist, pdfw, le;
+          if (L.type == LIGHT_SPHERE) {
+            // extension: a direction uniform in the sphere's cone, the distance to its near side
+            const float3 c = f3(L.centre[0], L.centre[1], L.centre[2]);
+            const float3 wc = v_sub(c, pos);
+            const float d2 = v_dot(wc, wc);
+            const float r2 = L.radius * L.radius;
+            le = 0.f;
+            dist = 0.f;
+            pdfw = 1.f;
+            wi = f3(0.f, 0.f, 1.f);
+            if (d2 > r2) {
+              const float s2 = r2 / d2;
+              const float omc = s2 / (1.f + sqrtf(1.f - s2));
+              const float ct = 1.f - u01(ra.y) * omc;
+              const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+              float sp, cp;
+              sincos_turns(u01(ra.z), &sp, &cp);
+              wi = frame_dir(v_mul(wc, 1.f / sqrtf(d2)), cp * st, sp * st, ct);
+              const float b = v_dot(wc, wi);
+              const float disc = b * b - (d2 - r2);
+              dist = disc > 0.f ? b - sqrtf(disc) : b;
+              pdfw = 1.f / ((2.f * MSC_PI) * omc);
+              le = dist > 0.f ? L.intensity : 0.f;
+            }
+          } else {
+            // QuadLight::illuminate (src/core/QuadLight.cpp:41-67)
+            const float3 smp = xf_point(L.xf, f3(0.f, u01(ra.y) - 0.5f, u01(ra.z) - 0.5f));
+            const float3 ln = f3(L.normal[0], L.normal[1], L.normal[2]);
+            float cosl = v_dot(v_normalize(v_sub(pos, smp)), ln);
+            le = cosl < 0.f ? 0.f : L.intensity;
+            cosl = cosl < 0.f ? 0.f : cosl;
+            const float3 tol = v_sub(smp, pos);
+            wi = v_normalize(tol);
+            dist = v_len(tol);
+            pdfw = (v_dot(tol, tol) / cosl) / (L.scale[0] * L.scale[1]);
+          }
           if (le > MSC_EPSILON) {
-            const BsdfEval e = bsdf_evaluate(s, wi, wo, nrm);
+            const BsdfEval e = bsdf_evaluate(s, col, wi, wo, nrm);
             if (v_maxc(e.f) > MSC_EPSILON) {
               const float a = pdfw * sc.light_pick;
               const float mis = mis_weight(a, e.pdf, f.mis_power);
@@ -462,14 +678,13 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
             float3 wi;
             BsdfEval e;
             bool ok = true;
-            const float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
             if (s.type == SHADER_PHONG) {
               // cos(alpha) = xi^(1/(e+1)) around the mirror direction
               const float ca = pow_pos(u01(rb.y), 1.f / (s.exponent + 1.f));
               const float sa = sqrtf(fmaxf(0.f, 1.f - ca * ca));
               const float3 r = v_sub(v_mul(nrm, 2.f * v_dot(nrm, wo)), wo);
               wi = frame_dir(v_normalize(r), cp * sa, sp * sa, ca);
-              e = bsdf_evaluate(s, wi, wo, nrm);
+              e = bsdf_evaluate(s, col, wi, wo, nrm);
               ok = e.cos_theta > 0.f && e.pdf > 0.f;
             } else {
               // LambertShader::sample (src/core/LambertShader.cpp:49-73) with
@@ -523,10 +738,12 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
 
 // rtcOccluded with mask 0x0FFFFFFF (Integrator.cpp:153-174); an unoccluded
 // shadow ray adds its weighted contribution to its sample.
-template <bool WIDE, bool MULTI>
-__global__ void __launch_bounds__(128) k_trace_shadow(const SceneRec* __restrict__ scenes, BvhRef scene0, ShadowBuf sh,
-                                                      const int* __restrict__ count, float4* sample_rgb, int* err) {
+template <bool WIDE, bool MULTI, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_trace_shadow(const SceneRec* __restrict__ scenes, BvhRef scene0, ShadowBuf sh,
+                                                      const int* __restrict__ count, float4* sample_rgb, int* err,
+                                                      unsigned long long* shadow_total) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (shadow_total && i == 0) *shadow_total += (unsigned long long)*count;
   if (i >= *count) return;
   const float4 o = sh.o[i], d = sh.d[i], c = sh.c[i];
   const BvhRef b = MULTI ? bvh_of(scenes[__float_as_int(c.w)], WIDE) : scene0;
@@ -610,14 +827,14 @@ int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBu
   return 1;
 }
 
-int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s) {
+int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
   const int tiles = (n + kPartTile - 1) / kPartTile;
-  k_part_count<<<tiles, PB, 0, s>>>(src.d, n, pool.tile_counts, tiles);
+  k_part_count<<<tiles, PB, 0, s>>>(src.d, n, n_dev, pool.tile_counts, tiles);
   // one extra row (the dead bucket) follows the six bins, so every bin's
   // total is the difference of two scanned row starts
   k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * PRADIX, nullptr);
-  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, pool.tile_counts, tiles, pool.rays, pool.cap, pool.count);
+  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, n_dev, pool.tile_counts, tiles, pool.rays, pool.cap, pool.count);
   k_part_commit<<<1, 32, 0, s>>>(pool.tile_counts, tiles, pool.count, pool.cap, pool.err);
   return 4;
 }
@@ -628,72 +845,109 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
   return 1;
 }
 
-int launch_origin_box(const float4* o, const Segments& seg, uint32_t* box6, cudaStream_t s) {
-  const int n = seg.prefix[seg.count];
-  if (n <= 0) return 0;
-  k_origin_box<<<std::min(grid_for(n), 512), TB, 0, s>>>(o, seg, box6);
+int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
+                Counters* ctr, cudaStream_t s) {
+  k_plan<<<1, 32, 0, s>>>(pool.count, pool.cap, batch_cap, merge, scene_bits, plan, box6, ctr);
   return 1;
 }
 
-int launch_ray_keys(const float4* o, const float4* d, const Segments& seg, const uint32_t* box6, int prefix_bits,
+int launch_origin_box(const float4* o, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s) {
+  if (n_max <= 0) return 0;
+  k_origin_box<<<std::min(grid_for(n_max), 512), TB, 0, s>>>(o, plan, box6);
+  return 1;
+}
+
+int launch_ray_keys(const float4* o, const float4* d, const BatchPlan* plan, int n_max, const uint32_t* box6,
                     uint32_t* keys, cudaStream_t s) {
-  const int n = seg.prefix[seg.count];
-  if (n <= 0) return 0;
-  k_ray_keys<<<grid_for(n), TB, 0, s>>>(o, d, seg, box6, prefix_bits, keys);
+  if (n_max <= 0) return 0;
+  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(o, d, plan, box6, keys);
   return 1;
 }
 
-int launch_gather(const RayBuf& src, const Segments& seg, const uint32_t* perm, RayBuf dst, cudaStream_t s) {
-  const int n = seg.prefix[seg.count];
-  if (n <= 0) return 0;
-  k_gather<<<grid_for(n), TB, 0, s>>>(src, seg, perm, dst);
+int launch_gather(const RayBuf& src, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
+                  cudaStream_t s) {
+  if (n_max <= 0) return 0;
+  k_gather<<<grid_for(n_max), TB, 0, s>>>(src, plan, perm, dst);
   return 1;
 }
+
+// Traversal block size: 64, 128 or 256 threads (an autotuner choice).
+#define MSC_TRACE_DISPATCH(KERNEL, BLOCK, WIDE, MULTI, GRID_N, S, ...)                                     \
+  do {                                                                                                  \
+    const int bs_ = (BLOCK) == 64 ? 64 : ((BLOCK) == 256 ? 256 : 128);                                  \
+    const int g_ = grid_for(GRID_N, bs_);                                                               \
+    if (bs_ == 64) {                                                                                    \
+      if (WIDE) { if (MULTI) KERNEL<true, true, 64><<<g_, 64, 0, S>>>(__VA_ARGS__);                     \
+                  else KERNEL<true, false, 64><<<g_, 64, 0, S>>>(__VA_ARGS__); }                         \
+      else { if (MULTI) KERNEL<false, true, 64><<<g_, 64, 0, S>>>(__VA_ARGS__);                         \
+             else KERNEL<false, false, 64><<<g_, 64, 0, S>>>(__VA_ARGS__); }                             \
+    } else if (bs_ == 256) {                                                                            \
+      if (WIDE) { if (MULTI) KERNEL<true, true, 256><<<g_, 256, 0, S>>>(__VA_ARGS__);                   \
+                  else KERNEL<true, false, 256><<<g_, 256, 0, S>>>(__VA_ARGS__); }                       \
+      else { if (MULTI) KERNEL<false, true, 256><<<g_, 256, 0, S>>>(__VA_ARGS__);                       \
+             else KERNEL<false, false, 256><<<g_, 256, 0, S>>>(__VA_ARGS__); }                           \
+    } else {                                                                                            \
+      if (WIDE) { if (MULTI) KERNEL<true, true, 128><<<g_, 128, 0, S>>>(__VA_ARGS__);                   \
+                  else KERNEL<true, false, 128><<<g_, 128, 0, S>>>(__VA_ARGS__); }                       \
+      else { if (MULTI) KERNEL<false, true, 128><<<g_, 128, 0, S>>>(__VA_ARGS__);                       \
+             else KERNEL<false, false, 128><<<g_, 128, 0, S>>>(__VA_ARGS__); }                           \
+    }                                                                                                   \
+  } while (0)
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
-                         const float4* d, int n, float4* hits, int* err, cudaStream_t s) {
+                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev, int block) {
   if (n <= 0) return 0;
   const bool wide = scene0.wnodes != nullptr;
   const BvhRef b0 = bvh_of(scene0, wide);
-  const int g = grid_for(n, 128);
-  if (num_scenes > 1) {
-    if (wide) k_trace_closest<true, true><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
-    else k_trace_closest<false, true><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
-  } else {
-    if (wide) k_trace_closest<true, false><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
-    else k_trace_closest<false, false><<<g, 128, 0, s>>>(scenes, b0, o, d, n, hits, err);
-  }
+  MSC_TRACE_DISPATCH(k_trace_closest, block, wide, num_scenes > 1, n, s, scenes, b0, o, d, n, n_dev, hits, err);
   return 1;
 }
 
 int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
-                    cudaStream_t s) {
+                    cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
-  k_hit_keys<<<grid_for(n), TB, 0, s>>>(scenes, d, hits, n, keys);
+  k_hit_keys<<<grid_for(n), TB, 0, s>>>(scenes, d, hits, n, n_dev, keys);
+  return 1;
+}
+
+int launch_hit_keys64(const SceneRec* scenes, const float4* hits, int n, uint32_t* lo, uint32_t* hi,
+                      cudaStream_t s, const int* n_dev) {
+  if (n <= 0) return 0;
+  k_hit_keys64<<<grid_for(n), TB, 0, s>>>(scenes, hits, n, n_dev, lo, hi);
+  return 1;
+}
+
+int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t* dst, cudaStream_t s,
+                      const int* n_dev) {
+  if (n <= 0) return 0;
+  k_gather_u32<<<grid_for(n), TB, 0, s>>>(src, idx, n, n_dev, dst);
+  return 1;
+}
+
+int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t seed, cudaStream_t s) {
+  const int64_t total = faces * (int64_t)res * res * 3;
+  if (total <= 0) return 0;
+  k_face_texels<<<152 * 8, TB, 0, s>>>(texels, total, res, seed);
   return 1;
 }
 
 int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
                  const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
-                 cudaStream_t s) {
+                 cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
-  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, hits, order, n, next, sh, sh_count, job_done);
+  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, hits, order, n, n_dev, next, sh, sh_count,
+                                     job_done);
   return 1;
 }
 
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
-                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s) {
+                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
+                        unsigned long long* shadow_total, int block) {
   if (max_n <= 0) return 0;
   const bool wide = scene0.wnodes != nullptr;
   const BvhRef b0 = bvh_of(scene0, wide);
-  const int g = grid_for(max_n, 128);
-  if (num_scenes > 1) {
-    if (wide) k_trace_shadow<true, true><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
-    else k_trace_shadow<false, true><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
-  } else {
-    if (wide) k_trace_shadow<true, false><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
-    else k_trace_shadow<false, false><<<g, 128, 0, s>>>(scenes, b0, sh, sh_count, sample_rgb, err);
-  }
+  MSC_TRACE_DISPATCH(k_trace_shadow, block, wide, num_scenes > 1, max_n, s, scenes, b0, sh, sh_count, sample_rgb,
+                     err, shadow_total);
   return 1;
 }
 

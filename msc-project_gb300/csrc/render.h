@@ -55,8 +55,16 @@ struct SceneRec {        // one resident scene
   int num_lights;
   float light_pick;      // 1 / num_lights (Integrator.cpp:22)
   uint32_t tri_base;     // offset of this scene's triangles in the hit-key space
-  int pad;
+  int hit_key_bits;      // 32 or 64 (single-scene runs)
+  const float4* spheres; // sphere lights (extension): centre, radius
+  const int* sphere_light;  // light index of each sphere
+  int num_spheres;
+  int texel_res;         // face texels per side (0: none)
+  const unsigned short* texels;  // FP16 bits, [face][j][i][rgb], face = original triangle index
 };
+
+// A closest hit on sphere light s is recorded as triangle -2 - s.
+__host__ __device__ __forceinline__ int sphere_hit_code(int s) { return -2 - s; }
 
 struct JobRec {          // one render job: a scene seen through one camera
   CameraRec cam;
@@ -90,6 +98,25 @@ struct Segments {
   int count;
 };
 
+// One batch as the device chose it (k_plan): the ranges of the bin pool it
+// takes, its size and the key prefix width.  Kernels after the plan read it
+// from device memory, so a batch body needs no host decision and can be
+// replayed from a CUDA graph.
+struct BatchPlan {
+  Segments seg;
+  int nb;
+  int prefix_bits;
+};
+
+// Device counters of the wavefront, read back in one copy.
+struct Counters {
+  int bin_count[8];     // rays held per bin (6 used)
+  int shadow_count;     // shadow rays of the current batch
+  int err;              // error bits
+  int pad[6];
+  unsigned long long closest, shadow, batches;
+};
+
 // Each launcher returns the number of kernels it enqueued.
 int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s);
 
@@ -104,27 +131,47 @@ struct BinPool {
 constexpr int kPartTile = 2048;
 // Stable partition of src[0, n) by cardinal bin, appended behind each bin's
 // current content; dead rays (info < 0) are dropped.
-int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s);
+// n_dev (optional): the count is read on the device, n is then its upper bound.
+int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev = nullptr);
+
+// The next batch from the bins: the fullest bin's top, topped up from the
+// next fullest while merge is set (the order of the host's choice before).
+// Also opens the batch: origin box reset, shadow count zeroed, counters.
+int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
+                Counters* ctr, cudaStream_t s);
 
 // Per-ray cardinal bin only (stage test).
 int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 
 // Origin box of the batch rays into box6 (ordered-int min xyz, max xyz; caller initialises).
-int launch_origin_box(const float4* o, const Segments& seg, uint32_t* box6, cudaStream_t s);
+// n_max bounds the plan's batch size (grid size).
+int launch_origin_box(const float4* o, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s);
 // 32-bit keys; prefix_bits > 0 puts (scene << 3 | cardinal bin) above the origin/direction code.
-int launch_ray_keys(const float4* o, const float4* d, const Segments& seg, const uint32_t* box6, int prefix_bits,
+int launch_ray_keys(const float4* o, const float4* d, const BatchPlan* plan, int n_max, const uint32_t* box6,
                     uint32_t* keys, cudaStream_t s);
-int launch_gather(const RayBuf& src, const Segments& seg, const uint32_t* perm, RayBuf dst, cudaStream_t s);
+int launch_gather(const RayBuf& src, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
+                  cudaStream_t s);
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
-                         const float4* d, int n, float4* hits, int* err, cudaStream_t s);
+                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev = nullptr,
+                         int block = 128);
 int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
-                    cudaStream_t s);
+                    cudaStream_t s, const int* n_dev = nullptr);
+// The 64-bit hit key of one scene (shader id 12 b, face 23 b, quantised u 15 b, v 14 b; misses and
+// sphere-light hits 0) as low and high words.
+int launch_hit_keys64(const SceneRec* scenes, const float4* hits, int n, uint32_t* lo, uint32_t* hi,
+                      cudaStream_t s, const int* n_dev = nullptr);
+int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t* dst, cudaStream_t s,
+                      const int* n_dev = nullptr);
+// Fills the scene's face texels from their seed (FP16 bits of k / 1024).
+int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t seed, cudaStream_t s);
 int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
                  const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
-                 cudaStream_t s);
+                 cudaStream_t s, const int* n_dev = nullptr);
+// shadow_total (optional): the batch's shadow count is added to it.
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
-                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s);
+                        const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
+                        unsigned long long* shadow_total = nullptr, int block = 128);
 // Occlusion for explicit rays of scene 0 (stage test): occluded[i] = 1 if blocked in (tnear, tmax).
 int launch_occluded(const SceneRec& scene, const float4* o, const float4* d, int n, int* occluded, int* err,
                     cudaStream_t s);

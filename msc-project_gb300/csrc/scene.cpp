@@ -561,10 +561,23 @@ struct Ctx {
   bool fail(const std::string& m) { *err = m; return false; }
 };
 
-bool decode_texture(const YNode* n, ShaderRec* sh, Ctx& c) {
+bool decode_texture(const YNode* n, ShaderRec* sh, FaceTexels* ft, Ctx& c) {
   std::string ty = as_str(n ? n->get("type") : nullptr);
+  sh->texture = TEXTURE_CONSTANT;
   if (ty == "Constant") {  // include/core/ConstantTexture.h:74-85
     if (n->size() != 2 || !as_vec(n->get("colour"), 3, sh->colour)) return c.fail("bad Constant texture");
+    return true;
+  }
+  if (ty == "FaceTexels") {  // extension: per-face res x res FP16 RGB texels, tinted by colour
+    int res = 0, seed = 0;
+    if (n->size() != 4 || !as_int(n->get("resolution"), &res) || !as_int(n->get("seed"), &seed) ||
+        !as_vec(n->get("colour"), 3, sh->colour) || res < 1 || res > 256)
+      return c.fail("bad FaceTexels texture (needs resolution 1-256, seed, colour)");
+    if (ft->res != 0 && (ft->res != res || ft->seed != (uint32_t)seed))
+      return c.fail("every FaceTexels texture of a scene must share one resolution and seed");
+    ft->res = res;
+    ft->seed = (uint32_t)seed;
+    sh->texture = TEXTURE_FACE;
     return true;
   }
   if (ty == "Standard" || ty == "Layered")
@@ -674,6 +687,10 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
           else if (m == "binary") S.ext.wide_bvh = 0;
           else return c.fail("bvh must be wide or binary");
         }
+        else if (kv.first == "hit key bits") {
+          if (!as_int(&kv.second, &S.ext.hit_key_bits) || (S.ext.hit_key_bits != 32 && S.ext.hit_key_bits != 64))
+            return c.fail("hit key bits must be 32 or 64");
+        }
         else if (kv.first == "paths per generation") { if (!as_int(&kv.second, &S.ext.generation) || S.ext.generation < 0) return c.fail("bad paths per generation"); }
         else return c.fail("unknown extension '" + kv.first + "'");
       }
@@ -697,6 +714,8 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
   };
 
   if (scene.kind != YNode::Map && scene.kind != YNode::Null) return c.fail("scene document must be a mapping");
+  // OBJ files named by several objects are read once
+  std::vector<std::pair<std::string, ObjMesh>> obj_cache;
   // First pass: objects and shaders in document order (Pathtracer.cpp:166-217).
   for (const auto& kv : scene.map) {
     const YNode& n = kv.second;
@@ -709,8 +728,16 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
       if (n.size() != 6 || fname.empty() || !as_vec(n.get("translation"), 3, t) || !as_vec(n.get("rotation"), 3, r) ||
           !as_vec(n.get("scale"), 3, s) || !as_int(n.get("shader"), &shader))
         return c.fail("bad Polygon object");
-      ObjMesh mesh;
-      if (!obj_load_file(dir + "/" + fname, &mesh, err)) return false;
+      const ObjMesh* found = nullptr;
+      for (const auto& e : obj_cache)
+        if (e.first == fname) found = &e.second;
+      if (!found) {
+        ObjMesh m;
+        if (!obj_load_file(dir + "/" + fname, &m, err)) return false;
+        obj_cache.emplace_back(fname, std::move(m));
+        found = &obj_cache.back().second;
+      }
+      const ObjMesh& mesh = *found;
       Affine3 xf = make_trs_xyz(t, r, s);  // PolygonObject.cpp:17-22
       std::vector<float> pos(mesh.positions.size());
       for (size_t i = 0; i + 2 < mesh.positions.size(); i += 3) xf_host_point(xf, &mesh.positions[i], &pos[i]);
@@ -729,13 +756,13 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
       if (ty == "Lambert") {  // LambertShader.h:140-174
         sh.type = SHADER_LAMBERT;
         if (n.size() != 3 || !as_float(n.get("reflectance"), &sh.reflectance)) return c.fail("bad Lambert shader");
-        if (!decode_texture(n.get("texture"), &sh, c)) return false;
+        if (!decode_texture(n.get("texture"), &sh, &S.texels, c)) return false;
       } else if (ty == "Phong") {  // extension: modified Phong lobe
         sh.type = SHADER_PHONG;
         if (n.size() != 4 || !as_float(n.get("reflectance"), &sh.reflectance) ||
             !as_float(n.get("exponent"), &sh.exponent) || sh.exponent < 0.f)
           return c.fail("bad Phong shader");
-        if (!decode_texture(n.get("texture"), &sh, c)) return false;
+        if (!decode_texture(n.get("texture"), &sh, &S.texels, c)) return false;
       } else {
         continue;
       }
@@ -748,6 +775,24 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
     if (kv.first != "light") continue;
     const YNode& n = kv.second;
     std::string ty = as_str(n.get("type"));
+    if (ty == "Sphere") {  // extension: a sphere of uniform radiance, not triangle geometry
+      LightRec L;
+      memset(&L, 0, sizeof(L));
+      L.type = LIGHT_SPHERE;
+      if (n.size() != 4 || !as_vec(n.get("translation"), 3, L.centre) || !as_float(n.get("radius"), &L.radius) ||
+          !as_float(n.get("intensity"), &L.intensity) || !(L.radius > 0.f))
+        return c.fail("bad Sphere light (needs translation, radius > 0, intensity)");
+      const int light_id = (int)S.lights.size();
+      ShaderRec ns;
+      memset(&ns, 0, sizeof(ns));
+      ns.type = SHADER_NULL;
+      ns.light = light_id;
+      ns.reflectance = 1.f;
+      S.shaders.push_back(ns);
+      S.lights.push_back(L);
+      S.sphere_lights.push_back(light_id);
+      continue;
+    }
     if (ty != "Quad") continue;
     LightRec L;
     memset(&L, 0, sizeof(L));

@@ -49,6 +49,7 @@ double obj_parse_number(const char* s, const char* end);  // tinyobj tryParseDou
 
 // ------------------------------------------------------------------ device tables
 enum ShaderType : int { SHADER_LAMBERT = 0, SHADER_NULL = 1, SHADER_PHONG = 2 };
+enum TextureType : int { TEXTURE_CONSTANT = 0, TEXTURE_FACE = 1 };
 enum LightType : int { LIGHT_QUAD = 0, LIGHT_SPHERE = 1 };
 enum CameraType : int { CAMERA_PINHOLE = 0, CAMERA_THINLENS = 1 };
 enum SamplerType : int { SAMPLER_STRATIFIED = 0, SAMPLER_INDEPENDENT = 1, SAMPLER_GRID = 2 };
@@ -59,9 +60,23 @@ struct ShaderRec {
   int light;         // light index when this is the Null shader of an emitter, else -1
   float reflectance; // LambertShader::continuation() returns it (LambertShader.cpp:22-25)
   float exponent;    // Phong exponent (extension)
-  float colour[3];   // ConstantTexture colour (ConstantTexture.cpp:22-25)
-  float pad;
+  float colour[3];   // ConstantTexture colour (ConstantTexture.cpp:22-25); tint of face texels
+  int texture;       // TextureType
 };
+
+// Per-face texels (extension): every triangle of the scene owns res x res RGB
+// texels; texel (i, j) of face f, channel c, is k / 1024 with
+// k = face_texel_code(seed, f, j * res + i, c), exact in FP16.  A FaceTexels
+// texture looks up i = min(res-1, floor(u res)), j = min(res-1, floor(v res))
+// at the hit's barycentric weights (u, v) of v1 and v2.
+struct FaceTexels {
+  int res = 0;        // 0: the scene has none
+  uint32_t seed = 0;
+};
+
+MSC_HD uint32_t face_texel_code(uint32_t seed, uint32_t face, uint32_t texel, uint32_t ch) {
+  return pcg4d(seed, face, texel, ch).w >> 22;  // 10 bits
+}
 
 struct GeomRec {     // one per reference geomID (Scene::objects index)
   int shader;
@@ -76,7 +91,7 @@ struct LightRec {
   float scale[2];    // quad extents (QuadLight::m_scale)
   Affine3 xf;        // T * Rx * Ry * Rz * diag(1, sx, sy)  (QuadLight.cpp:25-31)
   float normal[3];   // normalize(L^-T * X)                   (QuadLight.cpp:33)
-  float centre[3];   // sphere lights (extension)
+  float centre[3];   // sphere lights (extension): uniform radiance `intensity` leaving the surface
   float radius;
 };
 
@@ -107,6 +122,7 @@ struct Extensions {  // optional third YAML document; the reference ignores it
   uint32_t seed = 0;       // mixes into every per-path draw
   int generation = 0;      // paths per camera generation (0 = automatic)
   int wide_bvh = 1;        // 1: 8-wide quantised BVH, 0: binary LBVH
+  int hit_key_bits = 32;   // 32: (geomID, primID); 64: (shader 12 b, face 23 b, quantised uv 29 b)
 };
 
 struct SceneDesc {
@@ -121,6 +137,8 @@ struct SceneDesc {
   std::vector<ShaderRec> shaders;
   std::vector<GeomRec> geoms;
   std::vector<LightRec> lights;
+  std::vector<int> sphere_lights;    // light index of each sphere light, in light order
+  FaceTexels texels;
   // flattened triangles in geomID order, positions after the object transform
   std::vector<float> tri_v;          // 9 per triangle: v0, v1, v2
   std::vector<float> tri_uv;         // 6 per triangle: uv0, uv1, uv2 (0 when absent)

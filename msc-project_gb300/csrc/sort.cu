@@ -30,8 +30,14 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(co
 __device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
 
 // ------------------------------------------------------------- onesweep
-__global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __restrict__ keys, int n, int passes,
-                                                              int bits, uint32_t* __restrict__ hist) {
+__device__ __forceinline__ int sort_count(int n_max, const int* n_dev) {
+  return n_dev ? min(*n_dev, n_max) : n_max;
+}
+
+__global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __restrict__ keys, int n_max,
+                                                              const int* __restrict__ n_dev, int passes, int bits,
+                                                              uint32_t* __restrict__ hist) {
+  const int n = sort_count(n_max, n_dev);
   __shared__ uint32_t sh[kSortMaxPasses][RADIX];
   for (int i = threadIdx.x; i < kSortMaxPasses * RADIX; i += kSortBlock) (&sh[0][0])[i] = 0;
   __syncthreads();
@@ -76,7 +82,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_t
 __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
-                                                              uint32_t* __restrict__ vals_out, int n, int shift,
+                                                              uint32_t* __restrict__ vals_out, int n_max,
+                                                              const int* __restrict__ n_dev, int shift,
                                                               uint32_t mask, int pass,
                                                               const uint32_t* __restrict__ hist, uint32_t* status_cur,
                                                               uint32_t* status_next, uint32_t* ctl, int* err) {
@@ -91,6 +98,8 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
   const uint32_t dstart = block_excl_scan(hist[pass * RADIX + threadIdx.x], warp_tmp);  // syncs inside
   const int tile = s_tile;
   const int base = tile * kSortTile;
+  const int n = sort_count(n_max, n_dev);
+  if (base >= n) return;  // the whole block: past a batch smaller than the launch
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // the next pass reads status_next from zero; the pass that last used it has finished
   if (status_next) status_next[tile * RADIX + threadIdx.x] = 0u;
@@ -316,9 +325,11 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity) {
 }
 
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream, int* err) {
+               int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev) {
   if (n <= 0) return 0;
   const int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
+  if (n_dev && (passes == 0 || ((passes % 2) == 1 && (keys_in == keys_out || (vals_in && vals_in == vals_out)))))
+    return -1;  // a device count needs distinct outputs and at least one pass
   const uint32_t* src_k;
   const uint32_t* src_v;
   bool done;
@@ -332,7 +343,7 @@ int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
   cudaMemsetAsync(s.hist, 0, (size_t)kSortMaxPasses * RADIX * 4 + 64, stream);
   int* errw = err ? err : (int*)(s.ctl + kSortMaxPasses);
   const int hist_blocks = tiles < 2 * 152 ? tiles : 2 * 152;
-  k_onesweep_hist<<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, passes, bits, s.hist);
+  k_onesweep_hist<<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
   ++launches;
   for (int p = 0; p < passes; ++p) {
     const bool to_out = ((passes - 1 - p) % 2) == 0;
@@ -343,8 +354,8 @@ int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
     const uint32_t mask = (1u << width) - 1u;
     uint32_t* cur = (p & 1) ? status1 : status0;
     uint32_t* next = (p + 1 < passes) ? ((p & 1) ? status0 : status1) : nullptr;
-    k_onesweep_pass<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, shift, mask, p, s.hist, cur, next,
-                                                      s.ctl, errw);
+    k_onesweep_pass<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, n_dev, shift, mask, p, s.hist,
+                                                      cur, next, s.ctl, errw);
     ++launches;
     src_k = dst_k;
     src_v = dst_v;

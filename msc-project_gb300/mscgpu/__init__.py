@@ -102,6 +102,11 @@ def load_library():
         "msc_batch_get_stats": (I, [P, C.POINTER(_Stats)]),
         "msc_batch_set_profiling": (I, [P, I]),
         "msc_batch_set_max_active": (I, [P, I]),
+        "msc_batch_autotune": (I, [P, I]),
+        "msc_batch_get_tuning": (I, [P, C.POINTER(_Tuning)]),
+        "msc_batch_set_tuning": (I, [P, C.POINTER(_Tuning)]),
+        "msc_batch_tune_log": (I, [P, C.POINTER(_TuneSample), I, C.POINTER(I)]),
+        "msc_batch_scene_info": (I, [P, I, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int64)]),
         "msc_serve": (I, [P, C.POINTER(_Request), I, C.POINTER(_RequestResult), C.POINTER(_ServeStats)]),
         "msc_obj_load": (I, [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]),
         "msc_scene_load_host": (I, [C.c_char_p, C.POINTER(C.c_int32), F, C.POINTER(C.c_int32)]),
@@ -305,6 +310,16 @@ def scene_load_host(yaml_path):
     return dict(zip(keys, [int(x) for x in info])), tv, tg
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
+                ("tuning", C.c_int), ("samples", C.c_int)]
+
+
+class _TuneSample(C.Structure):
+    _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
+                ("mrays_per_s", C.c_double)]
+
+
 def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
     d = _JobDesc()
     d.scene, d.width, d.height, d.spp = scene, width, height, spp
@@ -356,6 +371,12 @@ class Batch:
         self._check(self._lib.msc_batch_add_scene(self._b, os.fsencode(yaml_path), C.byref(sid)))
         return sid.value
 
+    def scene_info(self, scene):
+        """(lo, hi, triangles) of a resident scene: its triangle box and count."""
+        lo, hi, n = (C.c_float * 3)(), (C.c_float * 3)(), C.c_int64()
+        self._check(self._lib.msc_batch_scene_info(self._b, scene, lo, hi, C.byref(n)))
+        return np.array(lo[:], np.float32), np.array(hi[:], np.float32), n.value
+
     def submit(self, scene, **kw):
         """kw: width, height, spp, min_depth, max_depth, camera=(translation, rotation, focal), seed."""
         jid = C.c_int()
@@ -377,6 +398,26 @@ class Batch:
 
     def set_profiling(self, on):
         self._check(self._lib.msc_batch_set_profiling(self._b, 1 if on else 0))
+
+    def autotune(self, windows=0):
+        """Start the online autotuner (batch size, traversal block, sorts)."""
+        self._check(self._lib.msc_batch_autotune(self._b, windows))
+
+    def tuning(self):
+        t = _Tuning()
+        self._check(self._lib.msc_batch_get_tuning(self._b, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}
+
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), 0, 0)
+        self._check(self._lib.msc_batch_set_tuning(self._b, C.byref(t)))
+
+    def tune_log(self):
+        n = C.c_int()
+        self._check(self._lib.msc_batch_tune_log(self._b, None, 0, C.byref(n)))
+        buf = (_TuneSample * max(1, n.value))()
+        self._check(self._lib.msc_batch_tune_log(self._b, buf, n.value, C.byref(n)))
+        return [{k: getattr(buf[i], k) for k, _ in _TuneSample._fields_} for i in range(n.value)]
 
     def set_max_active(self, n):
         self._check(self._lib.msc_batch_set_max_active(self._b, n))

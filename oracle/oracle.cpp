@@ -464,9 +464,9 @@ void point(const Aff& a, const float p[3], float o[3]) {
 }
 
 enum { LAMBERT = 0, NULLSH = 1, PHONG = 2 };
-struct Shader { int type = LAMBERT; int light = -1; float refl = 1.f, ex = 0.f; float col[3] = {0, 0, 0}; };
+struct Shader { int type = LAMBERT; int light = -1; float refl = 1.f, ex = 0.f; float col[3] = {0, 0, 0}; int tex = 0; };
 struct Geom { int shader = 0, first = 0, count = 0, light = -1; };
-struct Light { float inten = 100.f; float scale[2] = {1, 1}; Aff m; float n[3]; };
+struct Light { int type = 0; float inten = 100.f; float scale[2] = {1, 1}; Aff m; float n[3]; float c[3]; float rad = 0.f; };
 
 struct BNode { float lo[3], hi[3]; int left, right, start, count; };
 
@@ -487,6 +487,9 @@ struct oracle_scene {
   std::vector<Shader> shaders;
   std::vector<Geom> geoms;
   std::vector<Light> lights;
+  std::vector<int> sphere_lights;  // light index of each sphere light (extension)
+  int texel_res = 0;           // per-face texels (extension)
+  uint32_t texel_seed = 0;
   std::vector<float> tv;       // 9 per triangle
   std::vector<int> tgeom;
   std::vector<uint8_t> tlight;
@@ -590,8 +593,16 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
       const Node* tex = n.get("texture");
       if (ty == "Lambert" || ty == "Phong") {
         s.type = ty == "Lambert" ? LAMBERT : PHONG;
-        if (!num(n.get("reflectance"), &s.refl) || !tex || str(tex->get("type")) != "Constant" ||
+        const std::string tt = tex ? str(tex->get("type")) : "";
+        if (!num(n.get("reflectance"), &s.refl) || (tt != "Constant" && tt != "FaceTexels") ||
             !vecn(tex->get("colour"), 3, s.col)) { *err = "shader"; return false; }
+        if (tt == "FaceTexels") {  // extension: per-face FP16 texels from a seed
+          int res = 0, sd = 0;
+          if (!inum(tex->get("resolution"), &res) || !inum(tex->get("seed"), &sd)) { *err = "texture"; return false; }
+          S->texel_res = res;
+          S->texel_seed = (uint32_t)sd;
+          s.tex = 1;
+        }
         if (s.type == PHONG && !num(n.get("exponent"), &s.ex)) { *err = "shader"; return false; }
         S->shaders.push_back(s);
       }
@@ -599,6 +610,21 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
   }
   for (auto& kv : sc.map) {  // Pathtracer.cpp:219-272
     const Node& n = kv.second;
+    if (kv.first == "light" && str(n.get("type")) == "Sphere") {  // extension: no triangle geometry
+      Light L;
+      L.type = 1;
+      if (!vecn(n.get("translation"), 3, L.c) || !num(n.get("radius"), &L.rad) || !num(n.get("intensity"), &L.inten)) {
+        *err = "light";
+        return false;
+      }
+      Shader ns;
+      ns.type = NULLSH;
+      ns.light = (int)S->lights.size();
+      S->sphere_lights.push_back(ns.light);
+      S->shaders.push_back(ns);
+      S->lights.push_back(L);
+      continue;
+    }
     if (kv.first != "light" || str(n.get("type")) != "Quad") continue;
     Light L;
     float t[3], r[3];
@@ -806,6 +832,59 @@ int trace(const oracle_scene* S, V<T> o, V<T> d, T tmin, T tmax, bool any, T* th
   return hit;
 }
 
+// ------------------------------------------------------------ sphere lights (extension)
+// First intersection of o + t d with the sphere (c, r) in (tmin, tmax), else -1.
+template <class T>
+T sphere_t(V<T> o, V<T> d, const float c[3], float r, T tmin, T tmax) {
+  const V<T> oc = sub(o, mk<T>(c[0], c[1], c[2]));
+  const T a = dot(d, d);
+  const T b = dot(oc, d);
+  const T cc = dot(oc, oc) - (T)r * (T)r;
+  const T disc = b * b - a * cc;
+  if (disc < T(0)) return T(-1);
+  const T q = std::sqrt(disc);
+  const T t0 = (-b - q) / a;
+  if (t0 > tmin && t0 < tmax) return t0;
+  const T t1 = (-b + q) / a;
+  if (t1 > tmin && t1 < tmax) return t1;
+  return T(-1);
+}
+
+// Uniform cone sampling pdf of the sphere seen from p: 1 / (2 pi (1 - cos theta_max)).
+template <class T>
+T sphere_pdf(V<T> p, const float c[3], float r) {
+  const V<T> wc = sub(mk<T>(c[0], c[1], c[2]), p);
+  const T d2 = dot(wc, wc);
+  const T r2 = (T)r * (T)r;
+  if (!(d2 > r2)) return T(0);
+  const T s2 = r2 / d2;
+  const T omc = s2 / (T(1) + std::sqrt(T(1) - s2));
+  return T(1) / ((T(2) * T(kPi)) * omc);
+}
+
+// Closest hit: triangles, then sphere lights nearer than the triangle (a
+// sphere hit is returned as -2 - sphere index).
+template <class T>
+int closest(const oracle_scene* S, V<T> o, V<T> d, T* th, T* uh, T* vh) {
+  int hit = trace<T>(S, o, d, T(kTnear), T(kTfar), false, th, uh, vh);
+  T tmax = hit >= 0 ? *th : T(kTfar);
+  for (size_t q = 0; q < S->sphere_lights.size(); ++q) {
+    const Light& L = S->lights[S->sphere_lights[q]];
+    const T t = sphere_t<T>(o, d, L.c, L.rad, T(kTnear), tmax);
+    if (t > T(0)) {
+      tmax = t;
+      *th = t; *uh = T(0); *vh = T(0);
+      hit = -2 - (int)q;
+    }
+  }
+  return hit;
+}
+
+// Face texel colour factor (extension): k / 1024 with k from the texel hash.
+inline float face_texel(uint32_t seed, uint32_t face, uint32_t texel, uint32_t ch) {
+  return (float)(pcg4d(seed, face, texel, ch).w >> 22) / 1024.0f;
+}
+
 // ------------------------------------------------------------ integrator
 template <class T>
 T misw(T a, T b, int power) {
@@ -825,10 +904,9 @@ template <class T>
 struct Eval { V<T> f; T cs, pdf; };
 
 template <class T>
-Eval<T> evaluate(const Shader& s, V<T> wi, V<T> wo, V<T> n) {  // LambertShader.cpp:27-47, NullShader.cpp:25-39
+Eval<T> evaluate(const Shader& s, V<T> col, V<T> wi, V<T> wo, V<T> n) {  // LambertShader.cpp:27-47, NullShader.cpp:25-39
   Eval<T> e;
   T ci = dot(n, wi), co = dot(n, wo);
-  V<T> col = mk<T>(s.col[0], s.col[1], s.col[2]);
   if (s.type == NULLSH) { e.f = mk<T>(0, 0, 0); e.cs = T(1); e.pdf = T(1) * T(kInvPi) * T(0.5f); return e; }
   if (s.type == PHONG) {
     V<T> r = sub(mul(n, T(2) * co), wo);
@@ -904,7 +982,22 @@ void render_path(const oracle_scene* S, uint32_t sid, uint32_t seed, T* rgb, T* 
   while (true) {
     T t = 0, hu = 0, hv = 0;
     cnt->closest++;
-    const int tri = trace<T>(S, o, d, T(kTnear), T(kTfar), false, &t, &hu, &hv);
+    const int tri = closest<T>(S, o, d, &t, &hu, &hv);
+    if (tri < -1) {  // sphere light (extension): uniform radiance on its outside
+      const Light& Lt = S->lights[S->sphere_lights[-2 - tri]];
+      const V<T> dn = normalize(d);
+      const V<T> pos = add(o, mul(dn, t));
+      const V<T> nl = mul(sub(pos, mk<T>(Lt.c[0], Lt.c[1], Lt.c[2])), T(1) / (T)Lt.rad);
+      const T le = dot(nl, neg(dn)) < T(0) ? T(0) : (T)Lt.inten;
+      T mis = T(1);
+      if (depth > 0) mis = misw(last_pdf, sphere_pdf<T>(o, Lt.c, Lt.rad) * pick, S->mis_power);
+      if (le > T(kEps)) {
+        L.x += le * mis * w.x;
+        L.y += le * mis * w.y;
+        L.z += le * mis * w.z;
+      }
+      break;
+    }
     if (tri < 0) break;  // Integrator.cpp:26-27
     const Geom& g = S->geoms[S->tgeom[tri]];
     const Shader& sh = S->shaders[g.shader];
@@ -933,22 +1026,55 @@ void render_path(const oracle_scene* S, uint32_t sid, uint32_t seed, T* rgb, T* 
     const V<T> nrm = normalize(cross(e1, e2));  // = -normalize(Ng), Integrator.cpp:121-125
     const V<T> pos = add(o, mul(dn, t));
     const V<T> wo = neg(dn);
+    V<T> colr = mk<T>(sh.col[0], sh.col[1], sh.col[2]);  // ConstantTexture.cpp:22-25
+    if (sh.tex == 1 && S->texel_res > 0) {  // face texels (extension)
+      const int res = S->texel_res;
+      const int ti = std::min(res - 1, std::max(0, (int)((float)hu * (float)res)));
+      const int tj = std::min(res - 1, std::max(0, (int)((float)hv * (float)res)));
+      const uint32_t tx = (uint32_t)(tj * res + ti);
+      colr = mk<T>(colr.x * (T)face_texel(S->texel_seed, (uint32_t)tri, tx, 0u),
+                   colr.y * (T)face_texel(S->texel_seed, (uint32_t)tri, tx, 1u),
+                   colr.z * (T)face_texel(S->texel_seed, (uint32_t)tri, tx, 2u));
+    }
     const U4 ra = pcg4d(sid, (uint32_t)depth + 1u, seed, 0u);
     if (nl > 0) {  // Integrator.cpp:103-178, QuadLight.cpp:41-67
       int li = (int)((T)nl * (T)u01(ra.x));
       if (li >= nl) li = nl - 1;
       const Light& Lt = S->lights[li];
-      const V<T> smp = xf<T>(Lt.m, mk<T>(0, (T)(u01(ra.y) - 0.5f), (T)(u01(ra.z) - 0.5f)));
-      const V<T> ln = mk<T>(Lt.n[0], Lt.n[1], Lt.n[2]);
-      T cosl = dot(normalize(sub(pos, smp)), ln);
-      const T le = cosl < T(0) ? T(0) : (T)Lt.inten;
-      cosl = cosl < T(0) ? T(0) : cosl;
-      const V<T> tol = sub(smp, pos);
-      const V<T> wi = normalize(tol);
-      const T dist = len(tol);
-      const T pdfw = (dot(tol, tol) / cosl) / ((T)Lt.scale[0] * (T)Lt.scale[1]);
+      V<T> wi;
+      T dist, pdfw, le;
+      if (Lt.type == 1) {  // sphere light (extension): uniform in its cone, distance to its near side
+        const V<T> wc = sub(mk<T>(Lt.c[0], Lt.c[1], Lt.c[2]), pos);
+        const T d2 = dot(wc, wc);
+        const T r2 = (T)Lt.rad * (T)Lt.rad;
+        le = T(0); dist = T(0); pdfw = T(1); wi = mk<T>(0, 0, 1);
+        if (d2 > r2) {
+          const T s2 = r2 / d2;
+          const T omc = s2 / (T(1) + std::sqrt(T(1) - s2));
+          const T ct = T(1) - (T)u01(ra.y) * omc;
+          const T st = std::sqrt(std::max(T(0), T(1) - ct * ct));
+          T sp, cp;
+          sincos_turns((T)u01(ra.z), &sp, &cp);
+          wi = frame_dir(mul(wc, T(1) / std::sqrt(d2)), cp * st, sp * st, ct);
+          const T b = dot(wc, wi);
+          const T disc = b * b - (d2 - r2);
+          dist = disc > T(0) ? b - std::sqrt(disc) : b;
+          pdfw = T(1) / ((T(2) * T(kPi)) * omc);
+          le = dist > T(0) ? (T)Lt.inten : T(0);
+        }
+      } else {
+        const V<T> smp = xf<T>(Lt.m, mk<T>(0, (T)(u01(ra.y) - 0.5f), (T)(u01(ra.z) - 0.5f)));
+        const V<T> ln = mk<T>(Lt.n[0], Lt.n[1], Lt.n[2]);
+        T cosl = dot(normalize(sub(pos, smp)), ln);
+        le = cosl < T(0) ? T(0) : (T)Lt.inten;
+        cosl = cosl < T(0) ? T(0) : cosl;
+        const V<T> tol = sub(smp, pos);
+        wi = normalize(tol);
+        dist = len(tol);
+        pdfw = (dot(tol, tol) / cosl) / ((T)Lt.scale[0] * (T)Lt.scale[1]);
+      }
       if (le > T(kEps)) {
-        const Eval<T> e = evaluate(sh, wi, wo, nrm);
+        const Eval<T> e = evaluate(sh, colr, wi, wo, nrm);
         if (maxc(e.f) > T(kEps)) {
           const T a = pdfw * pick;
           const T mis = misw(a, e.pdf, S->mis_power);
@@ -979,13 +1105,13 @@ void render_path(const oracle_scene* S, uint32_t sid, uint32_t seed, T* rgb, T* 
       const T sa = std::sqrt(std::max(T(0), T(1) - ca * ca));
       const V<T> rr = sub(mul(nrm, T(2) * dot(nrm, wo)), wo);
       wi = frame_dir(normalize(rr), cp * sa, sp * sa, ca);
-      e = evaluate(sh, wi, wo, nrm);
+      e = evaluate(sh, colr, wi, wo, nrm);
       ok = e.cs > T(0) && e.pdf > T(0);
     } else {  // LambertShader.cpp:49-73
       const T st = std::sqrt(T(1) - (T)u01(rb.y));
       const T ct2 = std::sqrt((T)u01(rb.y));
       wi = frame_dir(nrm, cp * st, sp * st, ct2);
-      e.f = mul(mul(mk<T>(sh.col[0], sh.col[1], sh.col[2]), (T)sh.refl), T(kInvPi));
+      e.f = mul(mul(colr, (T)sh.refl), T(kInvPi));
       e.cs = dot(nrm, wi);
       e.pdf = e.cs * T(kInvPi);
       ok = e.pdf > T(0);

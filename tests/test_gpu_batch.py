@@ -143,3 +143,65 @@ def test_serve_refuses_a_job_larger_than_the_film_pool(built, scenes):
     assert results[0]["status"] < 0 and results[1]["status"] == 0
     assert st["completed"] == 1
     b.close()
+
+
+def test_scene_info_is_the_triangle_box(built, scenes):
+    mscgpu, _ = built
+    b = mscgpu.Batch(batch_exponent=12, film_samples=1 << 12)
+    for k, y in enumerate(scenes):
+        assert b.add_scene(y) == k
+        lo, hi, n = b.scene_info(k)
+        info, tv, _ = mscgpu.scene_load_host(y)
+        p = tv.reshape(-1, 3)
+        assert n == info["triangles"]
+        assert np.array_equal(lo, p.min(0)) and np.array_equal(hi, p.max(0))
+    with pytest.raises(mscgpu.MscError):
+        b.scene_info(len(scenes))
+    b.close()
+
+
+def test_results_do_not_depend_on_the_tuning_choice(built, scenes):
+    mscgpu, _ = built
+    ref, rids = _batch(mscgpu, scenes, JOBS)
+    want = [ref.image(i) for i in rids]
+    ref.close()
+    for cfg in (dict(batch_exponent=10, trace_block=64, ray_sort=False, hit_sort=True),
+                dict(batch_exponent=12, trace_block=256, ray_sort=True, hit_sort=False),
+                dict(batch_exponent=14, trace_block=128, ray_sort=False, hit_sort=False)):
+        b = mscgpu.Batch(batch_exponent=14, film_samples=1 << 22)
+        for s in scenes:
+            b.add_scene(s)
+        b.set_tuning(**cfg)
+        t = b.tuning()
+        assert (t["batch_exponent"], t["trace_block"]) == (cfg["batch_exponent"], cfg["trace_block"])
+        ids = [b.submit(**j) for j in JOBS]
+        b.run()
+        for k, i in enumerate(ids):
+            assert np.array_equal(b.image(i).view(np.uint32), want[k].view(np.uint32)), (cfg, k)
+        b.close()
+
+
+def test_autotuner_books_samples_and_keeps_results(built, scenes):
+    mscgpu, _ = built
+    ref, rids = _batch(mscgpu, scenes, JOBS)
+    want = [ref.image(i) for i in rids]
+    ref.close()
+    b = mscgpu.Batch(batch_exponent=19, film_samples=1 << 22)
+    for s in scenes:
+        b.add_scene(s)
+    b.autotune(windows=1)
+    for _ in range(6):  # the tuner spends a window per step; keep feeding work until it is done
+        ids = [b.submit(**j) for j in JOBS]
+        b.run()
+        for k, i in enumerate(ids):
+            assert np.array_equal(b.image(i).view(np.uint32), want[k].view(np.uint32))
+            b.release(i)
+        if not b.tuning()["tuning"]:
+            break
+    log = b.tune_log()
+    assert len(log) >= 2 and all(s["mrays_per_s"] >= 0 for s in log)
+    t = b.tuning()
+    assert t["trace_block"] in (64, 128, 256) and 6 <= t["batch_exponent"] <= 19
+    with pytest.raises(mscgpu.MscError):
+        b.set_tuning(batch_exponent=20)  # above the capacity given at create
+    b.close()
