@@ -304,6 +304,46 @@ def bench_forms(args):
     return out
 
 
+def bench_stress(args):
+    """Hit-sort stress scene: sorted (64-bit hit key) against unsorted shading."""
+    import mscgpu
+    t = time.time()
+    y = make_scene_scaled(2, SEED + 2, args.stress_scale)
+    gen_s = time.time() - t
+    t = time.time()
+    pt = mscgpu.Pathtracer(y)
+    load_s = time.time() - t
+    out = {"workload": "2000 subdivided tori x 4000 tris (8 M) + floor, 4096 shader ids (Lambert/Phong) with "
+                       "per-face 16x16 FP16 RGB texels (12.3 GB), 64 sphere lights of log-uniform power; "
+                       "1024^2, 32 spp, depth 6" if args.stress_scale == 1.0 else
+                       "hit-sort stress scene at scale %g" % args.stress_scale,
+           "generate_s": gen_s, "load_s": load_s}
+    modes = {}
+    for label, hit_sort in (("sorted_64bit_key", True), ("unsorted", False)):
+        pt.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=hit_sort)
+        pt.process_device()  # warm-up (captures this choice's graph)
+        ms, rays = 0.0, 0
+        for _ in range(2):
+            pt.process_device()
+            st = pt.stats()
+            ms += st["process_ms"]
+            rays += st["closest_queries"] + st["shadow_queries"]
+        pt.set_profiling(True)
+        pt.process_device()
+        prof = pt.stats()
+        pt.set_profiling(False)
+        sm = prof["stage_ms"]
+        hits = prof["closest_queries"]
+        modes[label] = {"mrays_per_s": rays / ms / 1e3, "ms_per_pass": ms / 2,
+                        "shade_ms": round(sm["shade"], 3), "hit_sort_ms": round(sm["hit_sort"], 3),
+                        "shading_mhits_per_s": hits / sm["shade"] / 1e3 if sm["shade"] > 0 else None,
+                        "shading_incl_sort_mhits_per_s": hits / (sm["shade"] + sm["hit_sort"]) / 1e3}
+    pt.close()
+    out.update(modes)
+    log("stress: %s" % json.dumps(out))
+    return out
+
+
 def run_reference(args, yaml, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -349,6 +389,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
+    ap.add_argument("--stress-scale", type=float, default=1.0)
     ap.add_argument("--serve-rates", default="100:6,600:3",
                     help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
     ap.add_argument("--forms-scenes", type=int, default=64)
@@ -407,6 +449,8 @@ def main():
     pt.process_device()
     prof = pt.stats()
     pt.set_profiling(False)
+    tuned = pt.tuning()
+    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")}
     pt.close()
 
     total_ms = sum(dev_ms)
@@ -436,6 +480,8 @@ def main():
     out["batches_per_step"] = batches / args.steps
     if not args.no_forms:
         out["forms"] = bench_forms(args)
+    if not args.no_stress:
+        out["hit_sort_stress"] = bench_stress(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(yaml)
     print(json.dumps(out), flush=True)

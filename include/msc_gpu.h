@@ -122,6 +122,12 @@ int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys
 /* Stable LSD radix sort of (keys, vals) on bits [0, bits); sorted in place. */
 int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
 
+/* The stable order of 64-bit keys as the hit sort takes it for a 64-bit hit
+ * key (stable by the low word, then stably by the high word): perm[i] = index
+ * of the i-th smallest key.  No reference counterpart: the reference sorts
+ * hits by (geomID, primID) with tbb::parallel_sort (Pathtracer.cpp:335-339). */
+int msc_stage_sort_keys64(const uint64_t* keys, int n, uint32_t* perm);
+
 /* Device-pointer form of msc_sort_pairs on the given CUDA stream (0 = default).
  * Scratch is allocated per call. */
 int msc_sort_pairs_device(uint32_t* keys, uint32_t* vals, int n, int bits, void* stream);
@@ -192,6 +198,11 @@ typedef struct msc_tune_sample {
    counterpart. */
 int msc_batch_autotune(msc_batch* b, int windows);
 int msc_batch_get_tuning(msc_batch* b, msc_tuning* out);
+/* The plain engine's tuning point (it tunes itself during its first passes
+   unless the scene's extensions say `autotune: 0`). */
+int msc_get_tuning(msc_handle* h, msc_tuning* out);
+/* Applies a tuning point to the plain engine (stops its autotuner). */
+int msc_set_tuning(msc_handle* h, const msc_tuning* in);
 /* Applies a choice (the read-only fields are ignored); stops a running autotuner. */
 int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in);
 /* The autotuner's booked samples, at most cap; *n = how many exist. */

@@ -150,6 +150,7 @@ int plain_setup(msc_handle* h) {
   }
   h->core.ray_sort = d.ext.ray_sort != 0;
   h->core.hit_sort = d.ext.hit_sort != 0;
+  if (d.ext.autotune) h->core.start_autotune();
   int sid = 0;
   rc = h->core.add_scene(d, &sid);
   if (rc != MSC_OK) {
@@ -590,6 +591,39 @@ int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits) {
   return rc;
 }
 
+int msc_stage_sort_keys64(const uint64_t* keys, int n, uint32_t* perm) {
+  if (n < 0 || (n > 0 && (!keys || !perm))) return MSC_ERR_ARG;
+  if (n == 0) return MSC_OK;
+  std::vector<uint32_t> lo((size_t)n), hi((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    lo[i] = (uint32_t)keys[i];
+    hi[i] = (uint32_t)(keys[i] >> 32);
+  }
+  uint32_t* d = nullptr;
+  char* scratch = nullptr;
+  const size_t sb = sort_scratch_bytes(n);
+  int rc = MSC_OK;
+  if (cudaMalloc(&d, (size_t)n * 4 * 6) != cudaSuccess || cudaMalloc(&scratch, sb) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK) {
+    uint32_t *d_lo = d, *d_hi = d + n, *lo_s = d + 2 * (size_t)n, *perm1 = d + 3 * (size_t)n,
+             *hi_g = d + 4 * (size_t)n, *d_perm = d + 5 * (size_t)n;
+    SortScratch ss;
+    sort_scratch_bind(&ss, scratch, n);
+    if (cudaMemcpy(d_lo, lo.data(), (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d_hi, hi.data(), (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = MSC_ERR_CUDA;
+    if (rc == MSC_OK) {
+      sort_pairs(d_lo, nullptr, lo_s, perm1, n, 32, ss, 0);
+      launch_gather_u32(d_hi, perm1, n, hi_g, 0);
+      sort_pairs(hi_g, perm1, d_hi, d_perm, n, 32, ss, 0);
+      if (cudaMemcpy(perm, d_perm, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MSC_ERR_CUDA;
+    }
+  }
+  if (d) cudaFree(d);
+  if (scratch) cudaFree(scratch);
+  return rc;
+}
+
 int msc_trace_closest(msc_handle* h, const float* org, const float* dir, int n, float* t, float* u, float* v,
                       int32_t* geom, int32_t* prim) {
   if (!h || n < 0 || (n > 0 && (!org || !dir || !t || !u || !v || !geom || !prim))) return MSC_ERR_ARG;
@@ -832,23 +866,33 @@ int msc_batch_autotune(msc_batch* b, int windows) {
   return MSC_OK;
 }
 
+static void tuning_of(Core& c, msc_tuning* out) {
+  const TuneChoice t = c.choice();
+  out->batch_exponent = t.batch_exp;
+  out->trace_block = t.block;
+  out->ray_sort = t.ray_sort ? 1 : 0;
+  out->hit_sort = t.hit_sort ? 1 : 0;
+  out->tuning = c.tuning() ? 1 : 0;
+  out->samples = (int)c.tune_log.size();
+}
+
 int msc_batch_get_tuning(msc_batch* b, msc_tuning* out) {
   if (!b || !out) return MSC_ERR_ARG;
-  const TuneChoice c = b->core.choice();
-  out->batch_exponent = c.batch_exp;
-  out->trace_block = c.block;
-  out->ray_sort = c.ray_sort ? 1 : 0;
-  out->hit_sort = c.hit_sort ? 1 : 0;
-  out->tuning = b->core.tuning() ? 1 : 0;
-  out->samples = (int)b->core.tune_log.size();
+  tuning_of(b->core, out);
   return MSC_OK;
 }
 
-int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in) {
-  if (!b || !in) return MSC_ERR_ARG;
-  if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > b->core.batch_cap() ||
+int msc_get_tuning(msc_handle* h, msc_tuning* out) {
+  if (!h || !out) return MSC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(h->busy);
+  tuning_of(h->core, out);
+  return MSC_OK;
+}
+
+static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
+  if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > core.batch_cap() ||
       (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256)) {
-    b->err = "tuning: batch exponent above the capacity or block size not 64, 128 or 256";
+    *err = "tuning: batch exponent above the capacity or block size not 64, 128 or 256";
     return MSC_ERR_ARG;
   }
   TuneChoice c;
@@ -856,9 +900,20 @@ int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in) {
   c.block = in->trace_block;
   c.ray_sort = in->ray_sort != 0;
   c.hit_sort = in->hit_sort != 0;
-  b->core.stop_autotune();
-  b->core.apply(c);
+  core.stop_autotune();
+  core.apply(c);
   return MSC_OK;
+}
+
+int msc_batch_set_tuning(msc_batch* b, const msc_tuning* in) {
+  if (!b || !in) return MSC_ERR_ARG;
+  return set_tuning(b->core, &b->err, in);
+}
+
+int msc_set_tuning(msc_handle* h, const msc_tuning* in) {
+  if (!h || !in) return MSC_ERR_ARG;
+  std::lock_guard<std::mutex> lock(h->busy);
+  return set_tuning(h->core, &h->err, in);
 }
 
 int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {

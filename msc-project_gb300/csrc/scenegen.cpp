@@ -11,6 +11,12 @@
 //             300 instances of a subdivision-4 icosphere, 4 Lambert + 4 Phong
 //             shaders, 8 quad lights; 1024x1024, 64 spp, max depth 8,
 //             Russian roulette from depth 3, batch 2^20, power heuristic.
+//   config 2  hit-sort stress: 2000 randomly placed subdivided tori of 4000
+//             triangles each (8 M triangles, every torus two 2000-triangle
+//             halves with their own shader), a floor quad, 4096 shader ids
+//             (Lambert and Phong) whose texture is per-face 16x16 FP16 RGB
+//             texels from the seed, 64 sphere lights of log-uniform power;
+//             1024x1024, 32 spp (4 x 8 grid), max depth 6, 64-bit hit key.
 //   config 100 a tiny box scene for tests.
 // `scale` in (0,1] shrinks resolution (and for config 1 the geometry).
 #include <cmath>
@@ -196,6 +202,41 @@ std::string quad_light(V3 t, V3 r, double sx, double sy, double inten) {
          "\n  scale: " + buf + "\n  intensity: " + fmt("%.6f", inten) + "\n";
 }
 
+std::string face_texel_shader(bool glossy, double r, double g, double b, double refl, double ex, int res,
+                              uint32_t seed) {
+  std::string tex = "  texture:\n    type: FaceTexels\n    resolution: " + std::to_string(res) +
+                    "\n    seed: " + std::to_string(seed) + "\n    colour: " + vec3s(r, g, b) + "\n";
+  if (!glossy) return "shader:\n  type: Lambert\n" + tex + "  reflectance: " + fmt("%.6f", refl) + "\n";
+  return "shader:\n  type: Phong\n" + tex + "  reflectance: " + fmt("%.6f", refl) + "\n  exponent: " +
+         fmt("%.6f", ex) + "\n";
+}
+std::string sphere_light(V3 c, double radius, double inten) {
+  return "light:\n  type: Sphere\n  translation: " + vec3s(c.x, c.y, c.z) + "\n  radius: " + fmt("%.6f", radius) +
+         "\n  intensity: " + fmt("%.6f", inten) + "\n";
+}
+
+// Half of a torus of ring radius 1 and tube radius `tube`: the tube angle
+// runs over [half * pi, (half + 1) * pi); 50 x 20 quads = 2000 triangles,
+// outward winding.
+void write_torus_half(ObjWriter& o, double tube, int half) {
+  const int NU = 50, NV = 20;
+  const int base = o.nv;
+  for (int i = 0; i <= NU; ++i)
+    for (int j = 0; j <= NV; ++j) {
+      const double u = 2.0 * M_PI * i / NU, v = M_PI * (half + (double)j / NV);
+      const double rr = 1.0 + tube * std::cos(v);
+      o.vertex({rr * std::cos(u), tube * std::sin(v), rr * std::sin(u)}, (double)i / NU, (double)j / NV);
+    }
+  for (int i = 0; i < NU; ++i)
+    for (int j = 0; j < NV; ++j) {
+      const int a = base + i * (NV + 1) + j + 1;  // (i, j)
+      const int b = a + 1;                        // (i, j+1): along the tube first
+      const int c = a + (NV + 1) + 1;             // (i+1, j+1)
+      const int d = a + (NV + 1);                 // (i+1, j)
+      o.quad(a, b, c, d);
+    }
+}
+
 bool write_text(const std::string& path, const std::string& s) {
   FILE* f = fopen(path.c_str(), "wb");
   if (!f) return false;
@@ -312,6 +353,59 @@ bool gen_terrain(uint32_t seed, double scale, const std::string& dir, std::strin
   return write_text(*yaml, setup + "---\n" + scene + "---\n" + ext);
 }
 
+bool gen_stress(uint32_t seed, double scale, const std::string& dir, std::string* yaml) {
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  const int kShapes = 8;
+  double tubes[kShapes];
+  for (int k = 0; k < kShapes; ++k) {
+    tubes[k] = 0.2 + 0.3 * U(rng);
+    for (int h = 0; h < 2; ++h) {
+      ObjWriter o;
+      write_torus_half(o, tubes[k], h);
+      if (!o.save(dir + "/torus" + std::to_string(k) + "_" + std::to_string(h) + ".obj")) return false;
+    }
+  }
+  {
+    ObjWriter o;
+    o.quad_uv({0, 0, 0}, {0, 0, 120}, {120, 0, 0});  // z x x = +y
+    if (!o.save(dir + "/floor.obj")) return false;
+  }
+  const int kShaders = 4096, res = 16;
+  std::string scene;
+  for (int s = 0; s < kShaders; ++s) {
+    const bool glossy = (s & 1) != 0;
+    scene += face_texel_shader(glossy, 0.4 + 0.6 * U(rng), 0.4 + 0.6 * U(rng), 0.4 + 0.6 * U(rng), 0.9,
+                               10.0 + 190.0 * U(rng), res, seed);
+  }
+  scene += object("floor.obj", {0, 0, 0}, {0, 0, 0}, {1, 1, 1}, kShaders - 1);
+  const int meshes = scaled(2000, scale, 4);
+  for (int m = 0; m < meshes; ++m) {
+    const int k = (int)(U(rng) * kShapes) % kShapes;
+    const double r = 1.0 + 2.0 * U(rng);
+    const V3 t{(U(rng) - 0.5) * 120.0, r * (1.0 + tubes[k]) + 40.0 * U(rng), (U(rng) - 0.5) * 120.0};
+    const V3 rot{360.0 * U(rng), 360.0 * U(rng), 360.0 * U(rng)};
+    for (int h = 0; h < 2; ++h)
+      scene += object("torus" + std::to_string(k) + "_" + std::to_string(h) + ".obj", t, rot, {r, r, r},
+                      (2 * m + h) % (kShaders - 1));
+  }
+  const int lights = scaled(64, scale, 2);
+  for (int l = 0; l < lights; ++l) {
+    const double radius = 0.5 + U(rng);
+    const double power = std::exp(std::log(1.0e2) + (std::log(1.0e4) - std::log(1.0e2)) * U(rng));
+    const double inten = power / (4.0 * M_PI * M_PI * radius * radius);  // radiance of a uniform sphere emitter
+    scene += sphere_light({(U(rng) - 0.5) * 110.0, 20.0 + 45.0 * U(rng), (U(rng) - 0.5) * 110.0}, radius, inten);
+  }
+  const double focal = 36.0 / std::tan(30.0 * M_PI / 180.0);  // 60 degree field of view
+  const int img = scaled(1024, scale, 8);
+  const int spp = scale < 1.0 ? 2 : 32;
+  std::string setup = setup_doc(img, img, 8, 3, 6, 1.0, 20, {0, 45, 110}, {0, 90, -18}, focal);
+  std::string ext = "extensions:\n  mis: power\n  seed: " + std::to_string(seed) +
+                    "\n  samples per pixel: " + std::to_string(spp) + "\n  hit key bits: 64\n";
+  *yaml = dir + "/scene.yaml";
+  return write_text(*yaml, setup + "---\n" + scene + "---\n" + ext);
+}
+
 }  // namespace
 
 bool generate_scene(int config, uint32_t seed, double scale, const std::string& dir, std::string* yaml,
@@ -322,6 +416,7 @@ bool generate_scene(int config, uint32_t seed, double scale, const std::string& 
   if (config == 0) ok = gen_box(seed, scale, dir, false, yaml);
   else if (config == 100) ok = gen_box(seed, scale, dir, true, yaml);
   else if (config == 1) ok = gen_terrain(seed, scale, dir, yaml);
+  else if (config == 2) ok = gen_stress(seed, scale, dir, yaml);
   else { *err = "unknown scene config " + std::to_string(config); return false; }
   if (!ok) *err = "could not write the scene files into " + dir;
   return ok;

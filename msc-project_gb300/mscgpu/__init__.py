@@ -102,7 +102,10 @@ def load_library():
         "msc_batch_get_stats": (I, [P, C.POINTER(_Stats)]),
         "msc_batch_set_profiling": (I, [P, I]),
         "msc_batch_set_max_active": (I, [P, I]),
+        "msc_stage_sort_keys64": (I, [C.POINTER(C.c_uint64), I, U32]),
         "msc_batch_autotune": (I, [P, I]),
+        "msc_get_tuning": (I, [P, C.POINTER(_Tuning)]),
+        "msc_set_tuning": (I, [P, C.POINTER(_Tuning)]),
         "msc_batch_get_tuning": (I, [P, C.POINTER(_Tuning)]),
         "msc_batch_set_tuning": (I, [P, C.POINTER(_Tuning)]),
         "msc_batch_tune_log": (I, [P, C.POINTER(_TuneSample), I, C.POINTER(I)]),
@@ -197,6 +200,15 @@ class Pathtracer:
     def set_profiling(self, on):
         _check(self._lib.msc_set_profiling(self._h, 1 if on else 0), self._h)
 
+    def tuning(self):
+        t = _Tuning()
+        _check(self._lib.msc_get_tuning(self._h, C.byref(t)), self._h)
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}
+
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), 0, 0)
+        _check(self._lib.msc_set_tuning(self._h, C.byref(t)), self._h)
+
     def stats(self):
         s = _Stats()
         _check(self._lib.msc_get_stats(self._h, C.byref(s)), self._h)
@@ -270,6 +282,15 @@ def sort_pairs(keys, vals, bits=32):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     _check(lib.msc_sort_pairs(_ptr(k, C.c_uint32), _ptr(v, C.c_uint32), k.shape[0], bits))
     return k, v
+
+
+def sort_keys64(keys):
+    """Stable order of 64-bit keys as the 64-bit hit sort takes it."""
+    lib = load_library()
+    k = np.ascontiguousarray(keys, np.uint64)
+    perm = np.zeros(k.shape[0], np.uint32)
+    _check(lib.msc_stage_sort_keys64(_ptr(k, C.c_uint64), k.shape[0], _ptr(perm, C.c_uint32)))
+    return perm
 
 
 def generate_scene(config, seed, out_dir, scale=1.0):

@@ -153,3 +153,16 @@ def test_occlusion_matches_oracle(built, box_scene, form, tmp_path):
     want = s.occluded(org, d, tmax)
     assert (got != want).mean() < 1e-3
     assert 0.05 < want.mean() < 0.95
+
+
+def test_sort_keys64_is_the_stable_order(built):
+    """The 64-bit hit key order (low word, then high word) = a stable sort on the whole key."""
+    mscgpu, _ = built
+    rng = np.random.default_rng(64)
+    for n in (1, 1000, 70001):
+        hi = rng.integers(0, 1 << 12, n, dtype=np.uint64) << np.uint64(52)
+        mid = rng.integers(0, 1 << 23, n, dtype=np.uint64) << np.uint64(29)
+        lo = rng.integers(0, 1 << 29, n, dtype=np.uint64)
+        keys = hi | (mid if n < 5000 else (mid & np.uint64(0xF << 29))) | (lo & np.uint64(0xFF))  # many ties
+        perm = mscgpu.sort_keys64(keys)
+        assert np.array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))

@@ -74,7 +74,7 @@ def test_fan_and_dedup_semantics(built, obj_dir):
     assert pos.shape[0] == tex.shape[0]
 
 
-@pytest.mark.parametrize("cfg,scale", [(100, 1.0), (0, 0.25), (1, 0.02)])
+@pytest.mark.parametrize("cfg,scale", [(100, 1.0), (0, 0.25), (1, 0.02), (2, 0.02)])
 def test_product_scene_matches_oracle_loader(built, scene_dir, cfg, scale):
     mscgpu, oracle = built
     y = mscgpu.generate_scene(cfg, 99, str(scene_dir / ("load%d" % cfg)), scale=scale)
