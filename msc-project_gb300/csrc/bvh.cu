@@ -200,7 +200,12 @@ size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // triangles are re-emitted so that a node's leaf triangles are contiguous
 // from the node's triangle base.  Child boxes are quantised to 8 bits per
 // axis against the node box with power-of-two steps, rounded outward so the
-// decoded box always contains the child.
+// decoded box always contains the child.  Children are placed in slots by
+// direction octant (Ylitie, Karras and Laine, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017): slot s prefers
+// the child that lies farthest back along the octant-s direction, so a ray of
+// octant o that visits slots o ^ 0, o ^ 1, ..., o ^ 7 meets the children
+// roughly front to back without sorting them.
 constexpr int kWideLeafMax = 3;
 
 struct WideBuild {
@@ -290,6 +295,35 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
       ++k;
     }
     const float4 lo = nbox[2 * b], hi = nbox[2 * b + 1];
+    // octant slots: greedy assignment of (child, slot) pairs by increasing
+    // projection of the child's centre offset on the slot's direction
+    bool filled[8] = {false, false, false, false, false, false, false, false};
+    {
+      float cost[8][8];
+      const float ncx = 0.5f * (lo.x + hi.x), ncy = 0.5f * (lo.y + hi.y), ncz = 0.5f * (lo.z + hi.z);
+      for (int i = 0; i < k; ++i) {
+        const float4 cl = box_lo(C[i]), chh = box_hi(C[i]);
+        const float ox = 0.5f * (cl.x + chh.x) - ncx, oy = 0.5f * (cl.y + chh.y) - ncy, oz = 0.5f * (cl.z + chh.z) - ncz;
+        for (int sl = 0; sl < 8; ++sl)
+          cost[i][sl] = ((sl & 1) ? -ox : ox) + ((sl & 2) ? -oy : oy) + ((sl & 4) ? -oz : oz);
+      }
+      int slot_child[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      bool used[8] = {false, false, false, false, false, false, false, false};
+      for (int round = 0; round < k; ++round) {
+        int bi = -1, bs = -1;
+        float bc = 0.f;
+        for (int i = 0; i < k; ++i) {
+          if (used[i]) continue;
+          for (int sl = 0; sl < 8; ++sl)
+            if (!filled[sl] && (bi < 0 || cost[i][sl] < bc)) { bi = i; bs = sl; bc = cost[i][sl]; }
+        }
+        used[bi] = true;
+        filled[bs] = true;
+        slot_child[bs] = C[bi];
+      }
+      for (int sl = 0; sl < 8; ++sl) C[sl] = slot_child[sl];
+      k = 8;
+    }
     int e[3];
     float s[3];
     quantise_axis(lo.x, hi.x, &e[0], &s[0]);
@@ -300,6 +334,7 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
     const uint32_t tri_base = (uint32_t)out->tri_perm.size();
     for (int i = 0; i < k; ++i) {
       const int c = C[i];
+      if (!filled[i]) continue;  // an empty slot
       uint32_t m = 0;
       if (is_leafish(c)) {
         const int f = c < 0 ? ~c : first[c], cnt = c < 0 ? 1 : count[c];

@@ -141,8 +141,14 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
 //   w6, w7  one meta byte per slot: 0 empty or internal, else (count << 5) | triangle offset
 //   w8..w19 quantised child boxes, one byte per slot: lo.x, lo.y, lo.z, hi.x, hi.y, hi.z,
 //           two words each (slots 0-3, 4-7); child box = p + q * 2^e per axis.
-// Stack entries: a node index (>= 0) or ~(first triangle << 2 | count) for a leaf.
-constexpr int kWideStack = 128;
+// Traversal keeps node groups, not single children (Ylitie, Karras and Laine,
+// HPG 2017): a group is a node's child base, its internal-child mask and the
+// children still to visit, as bits in the ray's octant order (bit j = slot
+// j ^ octant).  The slots were assigned by octant at build time, so taking
+// the lowest bit first visits the children roughly front to back.  Each
+// visited node also yields a triangle group (triangle base + one bit per
+// triangle of its hit leaf slots), intersected before the next node.
+constexpr int kWideStack = 64;
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s) {
   return ((s < 4 ? lo_word : hi_word) >> (8 * (s & 3))) & 0xffu;
@@ -156,27 +162,38 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
                                            int num_nodes, int num_tris, float3 o, float3 d, float tmin, float tmax,
                                            TriHit* hit, int* overflow) {
   const float3 id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
-  int stack[kWideStack];
+  const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  uint2 stack[kWideStack];
   int sp = 0;
-  int entry = 0;
+  // the root as the only child of a virtual group: base 0, slot 0 internal
+  uint32_t g_base = 0, g_imask = 1u, g_hits = 1u << oct;
   bool found = false;
   const float widen = 1.0000004f;
   int steps = 0;
   while (true) {
-    if (entry >= 0) {
+    uint32_t t_base = 0, t_mask = 0;
+    if (g_hits != 0u) {
+      const uint32_t j = (uint32_t)(__ffs(g_hits) - 1);
+      g_hits &= g_hits - 1u;
+      const uint32_t slot = j ^ oct;
+      const int node = (int)(g_base + __popc(g_imask & ((1u << slot) - 1u)));
+      if (g_hits != 0u) {
+        if (sp < kWideStack) stack[sp++] = make_uint2(g_base, (g_imask << 8) | g_hits);
+        else *overflow = 1;
+      }
       if (++steps > kTraceStepCap) {
         *overflow = 2;
         return found;
       }
-      if (entry >= num_nodes) {
+      if (node >= num_nodes) {
         *overflow = 3;
         return found;
       }
-      const uint4 A = __ldg(&wn[5 * entry + 0]);
-      const uint4 B = __ldg(&wn[5 * entry + 1]);
-      const uint4 Q0 = __ldg(&wn[5 * entry + 2]);
-      const uint4 Q1 = __ldg(&wn[5 * entry + 3]);
-      const uint4 Q2 = __ldg(&wn[5 * entry + 4]);
+      const uint4 A = __ldg(&wn[5 * node + 0]);
+      const uint4 B = __ldg(&wn[5 * node + 1]);
+      const uint4 Q0 = __ldg(&wn[5 * node + 2]);
+      const uint4 Q1 = __ldg(&wn[5 * node + 3]);
+      const uint4 Q2 = __ldg(&wn[5 * node + 4]);
       const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
       const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
       const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
@@ -185,11 +202,11 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
       const float bx = (__uint_as_float(A.x) - o.x) * id.x;
       const float by = (__uint_as_float(A.y) - o.y) * id.y;
       const float bz = (__uint_as_float(A.z) - o.z) * id.z;
-      float dist[8];
-      uint32_t hits = 0;
+      uint32_t nh = 0u, tm = 0u;
 #pragma unroll
       for (int s = 0; s < 8; ++s) {
-        const bool valid = byte_of(B.z, B.w, s) != 0u || ((imask >> s) & 1u);
+        const uint32_t m = byte_of(B.z, B.w, s);
+        const bool inner = ((imask >> s) & 1u) != 0u;
         const float tlx = fmaf((float)byte_of(Q0.x, Q0.y, s), ax, bx);
         const float tly = fmaf((float)byte_of(Q0.z, Q0.w, s), ay, by);
         const float tlz = fmaf((float)byte_of(Q1.x, Q1.y, s), az, bz);
@@ -198,65 +215,45 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
         const float thz = fmaf((float)byte_of(Q2.z, Q2.w, s), az, bz);
         const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
         const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), tmax)) * widen;
-        dist[s] = tn;
-        if (valid && tn <= tf) hits |= 1u << s;
+        if (tn <= tf) {
+          if (inner) nh |= 1u << ((uint32_t)s ^ oct);
+          else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+        }
       }
-      if (hits == 0u) {
-        if (sp == 0) return found;
-        entry = stack[--sp];
-        continue;
-      }
-      // nearest hit child is visited next; the others go on the stack farthest first
-      int nearest = 0;
-      float nd = 3.0e38f;
-#pragma unroll
-      for (int s = 0; s < 8; ++s)
-        if (((hits >> s) & 1u) && dist[s] < nd) { nd = dist[s]; nearest = s; }
-      uint32_t rest = hits & ~(1u << nearest);
-      while (rest) {
-        int far = 0;
-        float fd = -1.0f;
-#pragma unroll
-        for (int s = 0; s < 8; ++s)
-          if (((rest >> s) & 1u) && dist[s] >= fd) { fd = dist[s]; far = s; }
-        rest &= ~(1u << far);
-        const uint32_t m = byte_of(B.z, B.w, far);
-        const int code = ((imask >> far) & 1u) ? (int)(B.x + __popc(imask & ((1u << far) - 1u)))
-                                                : ~(int)(((B.y + (m & 31u)) << 2) | (m >> 5));
-        if (sp < kWideStack) stack[sp++] = code;
-        else *overflow = 1;
-      }
-      {
-        const uint32_t m = byte_of(B.z, B.w, nearest);
-        entry = ((imask >> nearest) & 1u) ? (int)(B.x + __popc(imask & ((1u << nearest) - 1u)))
-                                          : ~(int)(((B.y + (m & 31u)) << 2) | (m >> 5));
-      }
-    } else {
-      const uint32_t code = (uint32_t)(~entry);
-      const int t0 = (int)(code >> 2);
-      const int cnt = (int)(code & 3u);
-      if (t0 + cnt > num_tris) {
+      g_base = B.x;
+      g_imask = imask;
+      g_hits = nh;
+      t_base = B.y;
+      t_mask = tm;
+    }
+    while (t_mask != 0u) {
+      const int k = (int)t_base + __ffs(t_mask) - 1;
+      t_mask &= t_mask - 1u;
+      if (k >= num_tris) {
         *overflow = 3;
         return found;
       }
-      for (int k = t0; k < t0 + cnt; ++k) {
-        const float4 a = __ldg(&tris[3 * k + 0]);
-        const float4 b = __ldg(&tris[3 * k + 1]);
-        const float4 c = __ldg(&tris[3 * k + 2]);
-        if (ANY && __float_as_int(b.w) != 0) continue;
-        float t, u, v;
-        if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
-          found = true;
-          if (ANY) return true;
-          tmax = t;
-          hit->t = t;
-          hit->u = u;
-          hit->v = v;
-          hit->tri = k;
-        }
+      const float4 a = __ldg(&tris[3 * k + 0]);
+      const float4 b = __ldg(&tris[3 * k + 1]);
+      const float4 c = __ldg(&tris[3 * k + 2]);
+      if (ANY && __float_as_int(b.w) != 0) continue;
+      float t, u, v;
+      if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
+        found = true;
+        if (ANY) return true;
+        tmax = t;
+        hit->t = t;
+        hit->u = u;
+        hit->v = v;
+        hit->tri = k;
       }
+    }
+    if (g_hits == 0u) {
       if (sp == 0) return found;
-      entry = stack[--sp];
+      const uint2 e = stack[--sp];
+      g_base = e.x;
+      g_imask = e.y >> 8;
+      g_hits = e.y & 0xffu;
     }
   }
 }
