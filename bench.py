@@ -266,8 +266,8 @@ def bench_forms(args):
         "paths": sum(job_paths(j) for j in jobs), "mrays_per_s": rate, "wall_s": wall,
         "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
         "speedup_vs_per_job_loop": rate / plain_rate if plain_rate else None,
-        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")},
-        "tune_samples": [[t["batch_exponent"], t["trace_block"], t["ray_sort"], t["hit_sort"],
+        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")},
+        "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["ray_sort"], t["hit_sort"],
                           round(t["mrays_per_s"], 1)] for t in tune_log]}
     # served: Poisson arrivals on the first 16 resident scenes, at each rate
     nres = min(16, len(scenes))
@@ -290,7 +290,7 @@ def bench_forms(args):
             if max_active:
                 b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
             else:
-                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")})
+                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")})
             _, sst = b.serve(reqs)
             row[label] = {"completed": sst["completed"], "mrays_per_s": sst["mrays_per_s"],
                           "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
@@ -390,6 +390,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
+    ap.add_argument("--tuning", default="auto",
+                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort")
     ap.add_argument("--stress-scale", type=float, default=1.0)
     ap.add_argument("--serve-rates", default="100:6,600:3",
                     help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
@@ -420,6 +422,9 @@ def main():
     t = time.time()
     pt = mscgpu.Pathtracer(yaml)
     log("scene load + device BVH build %.1f s" % (time.time() - t))
+    if args.tuning != "auto":
+        e, nb, blk, rs, hs = (int(x) for x in args.tuning.split(","))
+        pt.set_tuning(batch_exponent=e, bins=nb, trace_block=blk, ray_sort=bool(rs), hit_sort=bool(hs))
     for _ in range(args.warmup):
         pt.process_device()
     clocks = ClockSampler()
@@ -450,7 +455,7 @@ def main():
     prof = pt.stats()
     pt.set_profiling(False)
     tuned = pt.tuning()
-    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort")}
+    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")}
     pt.close()
 
     total_ms = sum(dev_ms)

@@ -114,6 +114,12 @@ int msc_stage_cardinal(const float* dirs, int n, int32_t* bins);
  * a ray whose depth word is negative is dropped.  out: 6*cap*12 floats,
  * bin b at [b*cap, (b+1)*cap); counts: 6 ints. */
 int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts);
+/* The same stable partition into 6, 26 or 98 direction bins (out holds
+ * nbins * cap rays; counts: nbins ints).  26/98 bins have no reference
+ * counterpart: they are the surface cells of a 3^3 / 5^3 direction cube. */
+int msc_stage_bin_partition_n(const float* rays, int n, int nbins, int cap, float* out, int32_t* counts);
+/* Direction bin of each of n directions (3 floats each) among 6, 26 or 98. */
+int msc_stage_ray_bins(const float* dirs, int n, int nbins, int32_t* bins);
 
 /* 32-bit ray sort keys in the origin box of the given rays (replaces the
  * median split of RaySort, src/core/RaySort.cpp:7-118). org, dir: 3*n floats. */
@@ -185,15 +191,16 @@ typedef struct msc_tuning {
   int trace_block;    /* traversal block size: 64, 128 or 256 */
   int ray_sort;       /* 1: each batch sorted on the origin/direction key (RaySort.cpp:7-118) */
   int hit_sort;       /* 1: each batch's hits sorted by (geomID, primID) (Pathtracer.cpp:335-339) */
+  int bins;           /* direction bins: 6 (DirectionalBins.cpp:37-115) or 26 / 98 (cube surface cells) */
   int tuning;         /* read only: 1 while the autotuner is still sampling */
   int samples;        /* read only: candidate samples booked by the autotuner */
 } msc_tuning;
 typedef struct msc_tune_sample {
-  int batch_exponent, trace_block, ray_sort, hit_sort;
+  int batch_exponent, trace_block, ray_sort, hit_sort, bins;
   double mrays_per_s; /* device-timed rays per second over the candidate's windows */
 } msc_tune_sample;
 /* Starts the online autotuner: the next batches are spread over candidate
-   choices (batch size, then traversal block, then the two sorts), each timed
+   choices (batch size, direction bins, traversal block, the two sorts), each timed
    over `windows` windows (0: 2), and the fastest is kept.  No reference
    counterpart. */
 int msc_batch_autotune(msc_batch* b, int windows);

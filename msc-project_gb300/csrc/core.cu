@@ -141,17 +141,28 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   free_ranges_.assign(1, std::make_pair((size_t)0, sample_cap_));
   const int B = batch_cap_, G = generation_, S = staging_cap_;
   const int part_tiles = (std::max(S, B) + kPartTile - 1) / kPartTile;
-  size_t bytes = 3 * al256((size_t)6 * G * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
+  const size_t chunks = bin_pool_chunks((size_t)G);
+  const int max_chunks = (int)(((size_t)G + kChunk - 1) / kChunk) + 1;
+  const size_t pool_rays = chunks * (size_t)kChunk;
+  size_t bytes = 3 * al256(pool_rays * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
+                 2 * al256((size_t)kMaxBins * 4) + al256((size_t)kMaxBins * max_chunks * 4) + al256(chunks * 4) +
+                 al256(4) +
                  3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(8 * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B) + al256((size_t)B * sizeof(float4)) + 3 * al256((size_t)B * sizeof(float4)) +
-                 al256((size_t)kMaxBins * part_tiles * 4) + 4096;
+                 al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
   Arena A{arena_, 0};
-  bins_.rays.o = A.take<float4>((size_t)6 * G);
-  bins_.rays.d = A.take<float4>((size_t)6 * G);
-  bins_.rays.w = A.take<float4>((size_t)6 * G);
-  bins_.cap = G;
+  bins_.rays.o = A.take<float4>(pool_rays);
+  bins_.rays.d = A.take<float4>(pool_rays);
+  bins_.rays.w = A.take<float4>(pool_rays);
+  bins_.num_chunks = (int)chunks;
+  bins_.max_chunks = max_chunks;
+  bins_.held = A.take<int>(kMaxBins);
+  bins_.table = A.take<int>((size_t)kMaxBins * max_chunks);
+  bins_.free_stack = A.take<int>(chunks);
+  bins_.free_top = A.take<int>(1);
+  A.take<int>(kMaxBins);  // spare
   staging_.o = A.take<float4>(S);
   staging_.d = A.take<float4>(S);
   staging_.w = A.take<float4>(S);
@@ -175,9 +186,10 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   shadow_.o = A.take<float4>(B);
   shadow_.d = A.take<float4>(B);
   shadow_.c = A.take<float4>(B);
-  bins_.tile_counts = A.take<uint32_t>((size_t)kMaxBins * part_tiles);
+  bins_.tile_counts = A.take<uint32_t>((size_t)(kMaxBins + 1) * part_tiles);
   bins_.max_tiles = part_tiles;
   bins_.count = ctr_->bin_count;
+  bins_.in_bins = &ctr_->in_bins;
   bins_.err = &ctr_->err;
   if (A.used > bytes) {
     err = "internal: device arena overflow";
@@ -185,6 +197,8 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   }
   CK(cudaMemset(ctr_, 0, sizeof(Counters)));
   CK(cudaMemset(plan_, 0, sizeof(BatchPlan)));
+  launch_pool_reset(bins_, stream_);
+  CK(cudaStreamSynchronize(stream_));
   CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
   memset(h_ctr_, 0, sizeof(Counters));
   return MSC_OK;
@@ -567,11 +581,15 @@ int Core::generate(bool* did) {
 }
 
 uint64_t Core::graph_key() const {
-  const uint64_t ns = scenes_.size();
+  const uint64_t ns = scenes_.size();  // <= 256
   const uint64_t k64 = (ns == 1 && scenes_[0]->rec.hit_key_bits == 64) ? 1 : 0;
-  return ns | (k64 << 15) | ((uint64_t)hit_bits_ << 16) | ((uint64_t)ray_sort << 24) | ((uint64_t)hit_sort << 25) |
-         ((uint64_t)merge_bins << 26) | ((uint64_t)wide_ << 27) | ((uint64_t)batch_size_ << 28) |
-         ((uint64_t)trace_block << 54) | (1ull << 63);
+  uint64_t bexp = 0;
+  while ((1 << (bexp + 1)) <= batch_size_) ++bexp;
+  const uint64_t block = trace_block == 64 ? 0 : (trace_block == 128 ? 1 : 2);
+  const uint64_t bins = bins_.nbins == 6 ? 0 : (bins_.nbins == 26 ? 1 : 2);
+  return ns | (k64 << 9) | ((uint64_t)hit_bits_ << 10) | ((uint64_t)ray_sort << 16) | ((uint64_t)hit_sort << 17) |
+         ((uint64_t)merge_bins << 18) | ((uint64_t)wide_ << 19) | (bexp << 20) | (block << 25) | (bins << 27) |
+         (1ull << 63);
 }
 
 void Core::drop_graph() {
@@ -600,8 +618,8 @@ int Core::enqueue_batch() {
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      int l = launch_origin_box(bins_.rays.o, plan_, B, box6_, st);
-      l += launch_ray_keys(bins_.rays.o, bins_.rays.d, plan_, B, box6_, keys_, st);
+      int l = launch_origin_box(bins_, plan_, B, box6_, st);
+      l += launch_ray_keys(bins_, plan_, B, box6_, keys_, st);
       t.done(l);
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
@@ -615,7 +633,7 @@ int Core::enqueue_batch() {
   }
   {
     StageClock t(this, MSC_STAGE_GATHER);
-    t.done(launch_gather(bins_.rays, plan_, B, perm, batch_, st));
+    t.done(launch_gather(bins_, plan_, B, perm, batch_, st));
   }
   {
     StageClock t(this, MSC_STAGE_TRACE);
@@ -756,7 +774,7 @@ int Core::step(bool* idle) {
   // enough batch bodies to take what the bins hold now (the device plans each one)
   uint64_t total = 0, need = 0;
   const uint64_t bs = (uint64_t)batch_size_;
-  for (int b = 0; b < 6; ++b) {
+  for (int b = 0; b < kMaxBins; ++b) {
     const uint64_t c = (uint64_t)std::max(0, h_ctr_->bin_count[b]);
     total += c;
     need += (c + bs - 1) / bs;
@@ -791,6 +809,7 @@ TuneChoice Core::choice() const {
   c.block = trace_block;
   c.ray_sort = ray_sort;
   c.hit_sort = hit_sort;
+  c.bins = bins_.nbins;
   return c;
 }
 
@@ -800,6 +819,7 @@ void Core::apply(const TuneChoice& c) {
   trace_block = (c.block == 64 || c.block == 256) ? c.block : 128;
   ray_sort = c.ray_sort;
   hit_sort = c.hit_sort;
+  bins_.nbins = (c.bins == 26 || c.bins == 98) ? c.bins : 6;
 }
 
 void Core::start_autotune(int windows) {
@@ -830,18 +850,24 @@ void Core::tune_begin_dim() {
           add(c);
         }
     } else if (tune_dim_ == 1) {
+      for (int nb : {6, 26, 98}) {
+        TuneChoice c = base;
+        c.bins = nb;
+        add(c);
+      }
+    } else if (tune_dim_ == 2) {
       for (int b : {64, 128, 256}) {
         TuneChoice c = base;
         c.block = b;
         add(c);
       }
-    } else if (tune_dim_ == 2) {
+    } else if (tune_dim_ == 3) {
       for (bool on : {true, false}) {
         TuneChoice c = base;
         c.ray_sort = on;
         add(c);
       }
-    } else if (tune_dim_ == 3) {
+    } else if (tune_dim_ == 4) {
       for (bool on : {true, false}) {
         TuneChoice c = base;
         c.hit_sort = on;

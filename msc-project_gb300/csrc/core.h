@@ -75,6 +75,7 @@ struct TuneChoice {
   int block = 128;      // traversal block size: 64, 128 or 256
   bool ray_sort = true; // origin/direction key sort of each batch
   bool hit_sort = true; // (geomID, primID) sort of each batch's hits
+  int bins = 6;         // direction bins: 6, 26 or 98
 };
 
 struct TuneSample {
@@ -101,9 +102,9 @@ class Core {
   int trace_block = 128;          // traversal block size
 
   // Online autotuner: while on, the next batches are spread over candidate
-  // choices (coordinate descent: batch size, then traversal block, then the
-  // two sorts), each timed on the device over a few windows; the fastest in
-  // rays per ms is kept.  Results are the same under any choice.
+  // choices (coordinate descent: batch size, direction bins, traversal
+  // block, then the two sorts), each timed on the device over a few windows;
+  // the fastest in rays per ms is kept.  Results are the same under any choice.
   void start_autotune(int windows_per_candidate = 2);
   void stop_autotune() { tune_active_ = false; tune_pending_ = -1; }
   bool tuning() const { return tune_active_; }

@@ -190,6 +190,31 @@ MSC_HD int cardinal_bin(float3 d) {
   return (da < 0.f) ? axis : axis + 3;
 }
 
+// Direction bin among 6 (cardinal_bin), 26 or 98: the surface cells of an
+// m^3 cube (m = 3 or 5) over [-1,1]^3, the direction scaled so that its
+// largest component has magnitude 1.  Cells are numbered in x-major order
+// with the (m-2)^3 interior cells skipped.
+MSC_HD int ray_bin(float3 d, int nbins) {
+  if (nbins == 6) return cardinal_bin(d);
+  const int m = nbins == 26 ? 3 : 5;
+  const float mx = fmaxf(fmaxf(fabsf(d.x), fabsf(d.y)), fabsf(d.z));
+  if (!(mx > 0.f)) return 0;
+  const float inv = 1.0f / mx;
+  const float half_m = 0.5f * (float)m;
+  int c[3];
+  const float v[3] = {d.x * inv, d.y * inv, d.z * inv};
+  for (int a = 0; a < 3; ++a) {
+    int q = (int)floorf((v[a] + 1.0f) * half_m);
+    c[a] = q < 0 ? 0 : (q > m - 1 ? m - 1 : q);
+  }
+  const int n_in = m - 2;
+  auto below = [&](int x) { return x - 1 < 0 ? 0 : (x - 1 > n_in ? n_in : x - 1); };
+  auto inner = [&](int x) { return (x >= 1 && x <= m - 2) ? 1 : 0; };
+  const int interior_before =
+      below(c[0]) * n_in * n_in + inner(c[0]) * (below(c[1]) * n_in + inner(c[1]) * below(c[2]));
+  return (c[0] * m + c[1]) * m + c[2] - interior_before;
+}
+
 MSC_HD uint32_t spread_bits_3(uint32_t v) {  // 10 bits -> every third bit
   v &= 0x3ffu;
   v = (v | (v << 16)) & 0x030000ffu;

@@ -150,6 +150,11 @@ int plain_setup(msc_handle* h) {
   }
   h->core.ray_sort = d.ext.ray_sort != 0;
   h->core.hit_sort = d.ext.hit_sort != 0;
+  {
+    TuneChoice c = h->core.choice();
+    c.bins = d.ext.bins;
+    h->core.apply(c);
+  }
   if (d.ext.autotune) h->core.start_autotune();
   int sid = 0;
   rc = h->core.add_scene(d, &sid);
@@ -469,8 +474,9 @@ int msc_stage_cardinal(const float* dirs, int n, int32_t* bins) {
   return rc;
 }
 
-int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts) {
-  if (n < 0 || cap <= 0 || !out || !counts || (n > 0 && !rays)) return MSC_ERR_ARG;
+int msc_stage_bin_partition_n(const float* rays, int n, int nbins, int cap, float* out, int32_t* counts) {
+  if (n < 0 || cap <= 0 || !out || !counts || (n > 0 && !rays) || (nbins != 6 && nbins != 26 && nbins != 98))
+    return MSC_ERR_ARG;
   RayBuf src;
   float4 *o = nullptr, *d = nullptr, *w = nullptr;
   int rc = MSC_OK;
@@ -480,11 +486,18 @@ int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32
   src.o = o;
   src.d = d;
   src.w = w;
+  // a chunked pool sized for the rays, as the render loop uses it
   BinPool pool;
+  pool.nbins = nbins;
+  const size_t chunks = bin_pool_chunks((size_t)std::max(n, 1));
+  pool.num_chunks = (int)chunks;
+  pool.max_chunks = (std::max(n, 1) + kChunk - 1) / kChunk + 1;
   char* mem = nullptr;
   const int tiles = std::max(1, (n + kPartTile - 1) / kPartTile);
-  const size_t ray_bytes = al256((size_t)6 * cap * sizeof(float4));
-  size_t bytes = 3 * ray_bytes + al256((size_t)kMaxBins * tiles * 4) + al256(8 * 4);
+  const size_t ray_bytes = al256(chunks * kChunk * sizeof(float4));
+  const size_t table_bytes = al256((size_t)kMaxBins * pool.max_chunks * 4);
+  size_t bytes = 3 * ray_bytes + al256((size_t)(kMaxBins + 1) * tiles * 4) + table_bytes + al256(chunks * 4) +
+                 al256(sizeof(Counters)) + al256((size_t)kMaxBins * 4) + al256(4);
   if (rc == MSC_OK && cudaMalloc(&mem, bytes) != cudaSuccess) rc = MSC_ERR_CUDA;
   if (rc == MSC_OK) {
     char* p = mem;
@@ -494,38 +507,76 @@ int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32
     p += ray_bytes;
     pool.rays.w = (float4*)p;
     p += ray_bytes;
-    pool.cap = cap;
     pool.tile_counts = (uint32_t*)p;
-    p += al256((size_t)kMaxBins * tiles * 4);
+    p += al256((size_t)(kMaxBins + 1) * tiles * 4);
     pool.max_tiles = tiles;
-    pool.count = (int*)p;
-    pool.err = pool.count + 7;
-    cudaMemset(pool.count, 0, 8 * 4);
-    cudaMemset(pool.rays.o, 0, 3 * ray_bytes);
+    pool.table = (int*)p;
+    p += table_bytes;
+    pool.free_stack = (int*)p;
+    p += al256(chunks * 4);
+    Counters* ctr = (Counters*)p;
+    p += al256(sizeof(Counters));
+    pool.held = (int*)p;
+    p += al256((size_t)kMaxBins * 4);
+    pool.free_top = (int*)p;
+    pool.count = ctr->bin_count;
+    pool.in_bins = &ctr->in_bins;
+    pool.err = &ctr->err;
+    cudaMemset(ctr, 0, sizeof(Counters));
+    launch_pool_reset(pool, 0);
     launch_bin_partition(src, n, pool, 0);
-    std::vector<float4> ho((size_t)6 * cap), hd((size_t)6 * cap), hw((size_t)6 * cap);
-    int hc[8];
-    if (cudaMemcpy(ho.data(), pool.rays.o, ho.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
+    Counters hc;
+    std::vector<int> table((size_t)kMaxBins * pool.max_chunks);
+    std::vector<float4> ho(chunks * kChunk), hd(chunks * kChunk), hw(chunks * kChunk);
+    if (cudaMemcpy(&hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(table.data(), pool.table, table.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(ho.data(), pool.rays.o, ho.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(hd.data(), pool.rays.d, hd.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hw.data(), pool.rays.w, hw.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hc, pool.count, 8 * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaMemcpy(hw.data(), pool.rays.w, hw.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
       rc = MSC_ERR_CUDA;
+    } else if (hc.err != 0) {
+      rc = MSC_ERR_DEVICE;
     } else {
-      for (size_t i = 0; i < ho.size(); ++i) {
-        const float4 a = ho[i], b = hd[i], c = hw[i];
-        float* r = out + 12 * i;
-        r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
-        r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
-        r[8] = c.x; r[9] = c.y; r[10] = c.z; r[11] = c.w;
+      // bin b's rays in bin order at out[(b * cap + i) * 12]
+      memset(out, 0, sizeof(float) * 12 * (size_t)nbins * cap);
+      for (int bb = 0; bb < nbins; ++bb) {
+        counts[bb] = hc.bin_count[bb];
+        for (int i = 0; i < hc.bin_count[bb] && i < cap; ++i) {
+          const int q = pool_index(table.data(), pool.max_chunks, bb, i);
+          const float4 a4 = ho[q], b4 = hd[q], c4 = hw[q];
+          float* r = out + 12 * ((size_t)bb * cap + i);
+          r[0] = a4.x; r[1] = a4.y; r[2] = a4.z; r[3] = a4.w;
+          r[4] = b4.x; r[5] = b4.y; r[6] = b4.z; r[7] = b4.w;
+          r[8] = c4.x; r[9] = c4.y; r[10] = c4.z; r[11] = c4.w;
+        }
       }
-      for (int k = 0; k < 6; ++k) counts[k] = hc[k];
-      if (hc[7] != 0) rc = MSC_ERR_DEVICE;
     }
   }
   if (mem) cudaFree(mem);
   if (o) cudaFree(o);
   if (d) cudaFree(d);
   if (w) cudaFree(w);
+  return rc;
+}
+
+int msc_stage_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts) {
+  return msc_stage_bin_partition_n(rays, n, 6, cap, out, counts);
+}
+
+int msc_stage_ray_bins(const float* dirs, int n, int nbins, int32_t* bins) {
+  if (n < 0 || (n > 0 && (!dirs || !bins)) || (nbins != 6 && nbins != 26 && nbins != 98)) return MSC_ERR_ARG;
+  if (n == 0) return MSC_OK;
+  float4* d = nullptr;
+  int* out = nullptr;
+  int rc = MSC_OK;
+  if (upload_f4(dirs, n, 3, 3, &d, 0.f)) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && cudaMalloc(&out, (size_t)n * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK) {
+    launch_ray_bins(d, n, nbins, out, 0);
+    if (cudaMemcpy(bins, out, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MSC_ERR_CUDA;
+  }
+  if (d) cudaFree(d);
+  if (out) cudaFree(out);
   return rc;
 }
 
@@ -537,26 +588,41 @@ int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys
   int rc = MSC_OK;
   if (upload_f4(org, n, 3, 3, &o, 0.f) || upload_f4(dir, n, 3, 3, &d, 0.f)) rc = MSC_ERR_CUDA;
   BatchPlan* plan = nullptr;
+  int* table = nullptr;
+  const int nchunks = (n + kChunk - 1) / kChunk;
   if (rc == MSC_OK && cudaMalloc(&mem, (size_t)(n + 8) * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
   if (rc == MSC_OK && cudaMalloc(&plan, sizeof(BatchPlan)) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && cudaMalloc(&table, (size_t)nchunks * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
   if (rc == MSC_OK) {
     uint32_t* box = mem + n;
     cudaMemset(box, 0xff, 12);
     cudaMemset(box + 3, 0, 12);
+    // the input rays as bin 0 of a pool whose chunk table is the identity
+    std::vector<int> ht((size_t)nchunks);
+    for (int k = 0; k < nchunks; ++k) ht[k] = k;
+    cudaMemcpy(table, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice);
+    BinPool pool;
+    pool.rays.o = o;
+    pool.rays.d = d;
+    pool.table = table;
+    pool.max_chunks = nchunks;
+    pool.nbins = 6;
     BatchPlan hp;
     memset(&hp, 0, sizeof(hp));
     hp.seg = one_segment(0, n);
     hp.nb = n;
     hp.prefix_bits = 0;
+    hp.bin_bits = 3;
     cudaMemcpy(plan, &hp, sizeof(hp), cudaMemcpyHostToDevice);
-    launch_origin_box(o, plan, n, box, 0);
-    launch_ray_keys(o, d, plan, n, box, mem, 0);
+    launch_origin_box(pool, plan, n, box, 0);
+    launch_ray_keys(pool, plan, n, box, mem, 0);
     if (cudaMemcpy(keys, mem, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MSC_ERR_CUDA;
   }
   if (o) cudaFree(o);
   if (d) cudaFree(d);
   if (mem) cudaFree(mem);
   if (plan) cudaFree(plan);
+  if (table) cudaFree(table);
   return rc;
 }
 
@@ -872,6 +938,7 @@ static void tuning_of(Core& c, msc_tuning* out) {
   out->trace_block = t.block;
   out->ray_sort = t.ray_sort ? 1 : 0;
   out->hit_sort = t.hit_sort ? 1 : 0;
+  out->bins = t.bins;
   out->tuning = c.tuning() ? 1 : 0;
   out->samples = (int)c.tune_log.size();
 }
@@ -891,8 +958,9 @@ int msc_get_tuning(msc_handle* h, msc_tuning* out) {
 
 static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > core.batch_cap() ||
-      (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256)) {
-    *err = "tuning: batch exponent above the capacity or block size not 64, 128 or 256";
+      (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256) ||
+      (in->bins != 6 && in->bins != 26 && in->bins != 98)) {
+    *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, or bins not 6, 26 or 98";
     return MSC_ERR_ARG;
   }
   TuneChoice c;
@@ -900,6 +968,7 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   c.block = in->trace_block;
   c.ray_sort = in->ray_sort != 0;
   c.hit_sort = in->hit_sort != 0;
+  c.bins = in->bins;
   core.stop_autotune();
   core.apply(c);
   return MSC_OK;
@@ -925,6 +994,7 @@ int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {
     out[i].trace_block = log[i].choice.block;
     out[i].ray_sort = log[i].choice.ray_sort ? 1 : 0;
     out[i].hit_sort = log[i].choice.hit_sort ? 1 : 0;
+    out[i].bins = log[i].choice.bins;
     out[i].mrays_per_s = log[i].ms > 0 ? log[i].rays / log[i].ms / 1e3 : 0.0;
   }
   return MSC_OK;

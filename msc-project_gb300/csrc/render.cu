@@ -41,13 +41,31 @@ __device__ __forceinline__ float mis_weight(float a, float b, int power) {
   return a / (a + b);  // misBalance, include/core/Common.h:45-48
 }
 
-// Position of batch ray i in the bin pool.
-__device__ __forceinline__ int seg_source(const Segments& seg, int i) {
-  int s = 0;
-#pragma unroll
-  for (int k = 1; k < 6; ++k)
-    if (k < seg.count && i >= seg.prefix[k]) s = k;
-  return seg.start[s] + (i - seg.prefix[s]);
+// The plan's runs copied into shared memory by a whole block (only the
+// runs in use).  Call from every thread of the block.
+__device__ __forceinline__ void load_segments(const BatchPlan* __restrict__ plan, Segments& sm) {
+  const int c = plan->seg.count;
+  for (int k = threadIdx.x; k <= c; k += blockDim.x) {
+    sm.prefix[k] = plan->seg.prefix[k];
+    if (k < c) {
+      sm.bin[k] = plan->seg.bin[k];
+      sm.start[k] = plan->seg.start[k];
+    }
+  }
+  if (threadIdx.x == 0) sm.count = c;
+  __syncthreads();
+}
+
+// Pool index of batch ray i: its run (binary search on the prefix), then the
+// run's bin position through the bin's chunk table.
+__device__ __forceinline__ int seg_source(const Segments& seg, const int* table, int max_chunks, int i) {
+  int lo = 0, hi = seg.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg.prefix[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return pool_index(table, max_chunks, seg.bin[lo], seg.start[lo] + (i - seg.prefix[lo]));
 }
 
 // ------------------------------------------------------------------ raygen
@@ -127,58 +145,101 @@ __global__ void __launch_bounds__(TB) k_raygen(JobRec f, int job_index, uint32_t
 
 // -------------------------------------------------------- bin partition
 // DirectionalBins::add (src/core/DirectionalBins.cpp:37-73) as a stable
-// counting partition: count digits per tile, scan, scatter.
+// counting partition: count digits per tile, scan, reserve chunks, scatter.
 constexpr int PB = 256;
 constexpr int PITEMS = kPartTile / PB;
-constexpr int PRADIX = kMaxBins;
-constexpr int kDead = 6;
+constexpr int PRADIX = kBinRadix;
 
-__device__ __forceinline__ int ray_digit(const float4& d) {
-  if (__float_as_int(d.w) < 0) return kDead;
-  return cardinal_bin(f3(d));
+__device__ __forceinline__ int ray_digit(const float4& d, int nbins) {
+  if (__float_as_int(d.w) < 0) return nbins;  // the dead bucket
+  return ray_bin(f3(d), nbins);
 }
 
 __device__ __forceinline__ int dev_count(int n_max, const int* n_dev) {
   return n_dev ? min(*n_dev, n_max) : n_max;
 }
 
+// Per-tile digit counts, digit-major: counts[digit * tiles + tile] for the
+// nbins + 1 digits (tiles past the count write zeros).
 __global__ void __launch_bounds__(PB) k_part_count(const float4* __restrict__ d, int n_max,
-                                                   const int* __restrict__ n_dev, uint32_t* __restrict__ counts,
-                                                   int tiles) {
+                                                   const int* __restrict__ n_dev, int nbins,
+                                                   uint32_t* __restrict__ counts, int tiles) {
   const int n = dev_count(n_max, n_dev);
   __shared__ int hist[PRADIX];
-  if (threadIdx.x < PRADIX) hist[threadIdx.x] = 0;
+  for (int i = threadIdx.x; i < PRADIX; i += PB) hist[i] = 0;
   __syncthreads();
   const int base = blockIdx.x * kPartTile;
   const int lane = threadIdx.x & 31;
   for (int k = 0; k < PITEMS; ++k) {
     int idx = base + k * PB + threadIdx.x;
-    int dg = idx < n ? ray_digit(d[idx]) : -1;
+    int dg = idx < n ? ray_digit(d[idx], nbins) : -1;
     unsigned peers = __match_any_sync(0xffffffffu, dg);
     if (dg >= 0 && lane == __ffs(peers) - 1) atomicAdd(&hist[dg], __popc(peers));
   }
   __syncthreads();
-  if (threadIdx.x < PRADIX) counts[threadIdx.x * tiles + blockIdx.x] = (uint32_t)hist[threadIdx.x];
+  for (int g = threadIdx.x; g <= nbins; g += PB) counts[g * tiles + blockIdx.x] = (uint32_t)hist[g];
+}
+
+// One block, one thread per bin: each bin's missing chunks, as one
+// contiguous run off the top of the free stack (an exclusive scan of the
+// needs gives each bin its part).
+__global__ void __launch_bounds__(kBinRadix) k_part_reserve(const uint32_t* __restrict__ scanned, int tiles,
+                                                            BinPool pool) {
+  __shared__ int warp_sum[kBinRadix / 32];
+  const int b = threadIdx.x, lane = b & 31, warp = b >> 5;
+  int need = 0;
+  if (b < pool.nbins) {
+    const int added = (int)(scanned[(b + 1) * tiles] - scanned[b * tiles]);
+    if (added > 0) {
+      int want = (pool.count[b] + added + kChunk - 1) >> kChunkShift;
+      if (want > pool.max_chunks) {
+        atomicOr(pool.err, ERR_BIN_OVERFLOW);
+        want = pool.max_chunks;
+      }
+      need = max(0, want - pool.held[b]);
+    }
+  }
+  int incl = need;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_sum[warp] = incl;
+  __syncthreads();
+  int before = 0, total = 0;
+  for (int w = 0; w < kBinRadix / 32; ++w) {
+    if (w < warp) before += warp_sum[w];
+    total += warp_sum[w];
+  }
+  const int ofs = before + incl - need;
+  const int top = *pool.free_top;
+  const int give = total <= top ? need : max(0, min(need, top - ofs));  // a short stack serves the lower bins
+  if (total > top && b == 0) atomicOr(pool.err, ERR_BIN_OVERFLOW);
+  const int base = top - min(total, top);
+  const int h0 = b < pool.nbins ? pool.held[b] : 0;
+  for (int i = 0; i < give; ++i) pool.table[b * pool.max_chunks + h0 + i] = pool.free_stack[base + ofs + i];
+  if (b < pool.nbins) pool.held[b] = h0 + give;
+  __syncthreads();
+  if (b == 0) *pool.free_top = base;
 }
 
 __global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, const int* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ scanned, int tiles, RayBuf dst,
-                                                     int cap, const int* __restrict__ bin_count) {
+                                                     const uint32_t* __restrict__ scanned, int tiles, BinPool pool) {
   const int n = dev_count(n_max, n_dev);
   __shared__ RankSmem<PB, PRADIX> sm;
   __shared__ uint32_t sidx[kPartTile];
   __shared__ int gofs[PRADIX];
   const int tile = blockIdx.x, base = tile * kPartTile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x < PRADIX) {
-    const int b = threadIdx.x;
-    gofs[b] = (b < kDead) ? b * cap + bin_count[b] + (int)(scanned[b * tiles + tile] - scanned[b * tiles]) : 0;
-  }
+  const int nbins = pool.nbins;
+  for (int b = threadIdx.x; b < PRADIX; b += PB)
+    gofs[b] = (b < nbins) ? pool.count[b] + (int)(scanned[b * tiles + tile] - scanned[b * tiles]) : 0;
   int dig[PITEMS], pos[PITEMS];
 #pragma unroll
   for (int k = 0; k < PITEMS; ++k) {
     int idx = base + warp * 32 * PITEMS + k * 32 + lane;
-    dig[k] = idx < n ? ray_digit(src.d[idx]) : -1;
+    dig[k] = idx < n ? ray_digit(src.d[idx], nbins) : -1;
   }
   tile_rank<PB, PITEMS, PRADIX>(dig, pos, sm);
 #pragma unroll
@@ -189,26 +250,43 @@ __global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, cons
   for (int p = threadIdx.x; p < count; p += PB) {
     uint32_t e = sidx[p];
     int b = (int)(e >> 16);
-    if (b >= kDead) continue;
+    if (b >= nbins) continue;
     int s = base + (int)(e & 0xffffu);
-    int o = gofs[b] + (p - sm.tile_start[b]);
-    if (o >= (b + 1) * cap) continue;  // overflow: reported by k_part_commit
-    dst.o[o] = src.o[s];
-    dst.d[o] = src.d[s];
-    dst.w[o] = src.w[s];
+    const int at = gofs[b] + (p - sm.tile_start[b]);
+    if ((at >> kChunkShift) >= pool.held[b]) continue;  // no chunk reserved: reported by k_part_reserve
+    const int o = pool_index(pool.table, pool.max_chunks, b, at);
+    pool.rays.o[o] = src.o[s];
+    pool.rays.d[o] = src.d[s];
+    pool.rays.w[o] = src.w[s];
   }
 }
 
-__global__ void k_part_commit(const uint32_t* __restrict__ scanned, int tiles, int* bin_count, int cap, int* err) {
-  int b = threadIdx.x;
-  if (b >= kDead) return;
-  int total = (int)(scanned[(b + 1) * tiles] - scanned[b * tiles]);
-  int c = bin_count[b] + total;
-  if (c > cap) {
-    atomicOr(err, ERR_BIN_OVERFLOW);
-    c = cap;
+__global__ void k_part_commit(const uint32_t* __restrict__ scanned, int tiles, BinPool pool) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= pool.nbins) return;
+  const int added = (int)(scanned[(b + 1) * tiles] - scanned[b * tiles]);
+  if (added == 0) return;
+  const int c = min(pool.count[b] + added, pool.held[b] << kChunkShift);
+  atomicAdd(pool.in_bins, c - pool.count[b]);
+  pool.count[b] = c;
+}
+
+__global__ void k_pool_reset(BinPool pool) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < pool.num_chunks) pool.free_stack[i] = pool.num_chunks - 1 - i;
+  if (i < kMaxBins) {
+    pool.count[i] = 0;
+    pool.held[i] = 0;
   }
-  bin_count[b] = c;
+  if (i == 0) {
+    *pool.free_top = pool.num_chunks;
+    *pool.in_bins = 0;
+  }
+}
+
+__global__ void k_ray_bins(const float4* __restrict__ d, int n, int nbins, int* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = ray_bin(f3(d[i]), nbins);
 }
 
 __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict__ out) {
@@ -221,60 +299,89 @@ __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict_
 // full batch, else flushes the fullest bin.  Here: the fullest bin's top
 // (LIFO), topped up from the next fullest bins (ties to the lower bin) while
 // `merge` is set and the batch is short.  One thread; the bins are six.
-__global__ void k_plan(int* bin_count, int cap, int batch_cap, int merge, int scene_bits, BatchPlan* plan,
-                       uint32_t* box6, Counters* ctr) {
-  if (threadIdx.x != 0) return;
-  int cnt[6], order[6];
-  for (int b = 0; b < 6; ++b) {
-    cnt[b] = bin_count[b];
-    order[b] = b;
+// One block of kBinRadix threads: thread b ranks bin b by count (descending,
+// ties to the lower bin), thread 0 then walks the ranks.  Every bin of the
+// pool is a candidate, so rays of a bin function used before a retune drain too.
+__global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap, int merge, int scene_bits,
+                                                    BatchPlan* plan, uint32_t* box6, Counters* ctr) {
+  __shared__ int cnt[kMaxBins];
+  __shared__ int by_rank[kMaxBins];
+  __shared__ int f_bin[kMaxBins], f_keep[kMaxBins], f_held[kMaxBins], f_ofs[kMaxBins + 1];
+  __shared__ int nsg_s, top_s;
+  const int t = threadIdx.x;
+  if (t < kMaxBins) cnt[t] = pool.count[t];
+  __syncthreads();
+  if (t < kMaxBins) {
+    const int c = cnt[t];
+    int r = 0;
+    for (int o = 0; o < kMaxBins; ++o) r += (cnt[o] > c || (cnt[o] == c && o < t)) ? 1 : 0;
+    by_rank[r] = t;
   }
-  for (int a = 1; a < 6; ++a) {  // stable insertion sort, count descending
-    const int o = order[a];
-    int k = a;
-    while (k > 0 && cnt[order[k - 1]] < cnt[o]) {
-      order[k] = order[k - 1];
-      --k;
+  __syncthreads();
+  if (t == 0) {
+    int nsg = 0, nb = 0, freed = 0;
+    for (int k = 0; k < kMaxBins && nb < batch_cap; ++k) {
+      const int b = by_rank[k];
+      const int c = cnt[b];
+      if (c == 0) break;
+      if (k > 0 && !merge) break;
+      const int take = min(batch_cap - nb, c);
+      const int left = c - take;
+      plan->seg.bin[nsg] = b;
+      plan->seg.start[nsg] = left;
+      plan->seg.prefix[nsg] = nb;
+      // chunks above the new top go back to the free stack; their rays are
+      // gathered before any later partition of this stream can reuse them
+      const int keep = (left + kChunk - 1) >> kChunkShift;
+      f_bin[nsg] = b;
+      f_keep[nsg] = keep;
+      f_held[nsg] = pool.held[b];
+      f_ofs[nsg] = freed;
+      freed += max(0, pool.held[b] - keep);
+      ++nsg;
+      nb += take;
+      pool.count[b] = left;
+      pool.held[b] = keep;
     }
-    order[k] = o;
+    f_ofs[nsg] = freed;
+    nsg_s = nsg;
+    top_s = *pool.free_top;
+    *pool.free_top = top_s + freed;
+    plan->seg.count = nsg;
+    plan->seg.prefix[nsg] = nb;
+    plan->nb = nb;
+    const int bb = bin_bits(pool.nbins);
+    plan->bin_bits = bb;
+    plan->prefix_bits = (nsg > 1 || scene_bits > 0) ? scene_bits + bb : 0;
+    *pool.in_bins -= nb;
+    for (int a = 0; a < 3; ++a) {
+      box6[a] = 0xffffffffu;
+      box6[3 + a] = 0u;
+    }
+    ctr->shadow_count = 0;
+    ctr->closest += (unsigned long long)nb;
+    ctr->batches += nb > 0 ? 1ull : 0ull;
   }
-  BatchPlan p;
-  p.seg.count = 0;
-  int nb = 0;
-  for (int k = 0; k < 6 && nb < batch_cap; ++k) {
-    const int b = order[k];
-    const int c = cnt[b];
-    if (c == 0) break;
-    if (k > 0 && !merge) break;
-    const int take = min(batch_cap - nb, c);
-    p.seg.start[p.seg.count] = b * cap + c - take;
-    p.seg.prefix[p.seg.count] = nb;
-    p.seg.count += 1;
-    nb += take;
-    bin_count[b] = c - take;
+  __syncthreads();
+  for (int k = 0; k < nsg_s; ++k) {
+    const int b = f_bin[k], keep = f_keep[k], nfree = f_held[k] - keep;
+    for (int h = t; h < nfree; h += blockDim.x)
+      pool.free_stack[top_s + f_ofs[k] + h] = pool.table[b * pool.max_chunks + keep + h];
   }
-  for (int k = p.seg.count; k < 6; ++k) p.seg.start[k] = 0;
-  for (int k = p.seg.count; k < 7; ++k) p.seg.prefix[k] = nb;
-  p.nb = nb;
-  p.prefix_bits = (p.seg.count > 1 || scene_bits > 0) ? scene_bits + 3 : 0;
-  *plan = p;
-  for (int a = 0; a < 3; ++a) {
-    box6[a] = 0xffffffffu;
-    box6[3 + a] = 0u;
-  }
-  ctr->shadow_count = 0;
-  ctr->closest += (unsigned long long)nb;
-  ctr->batches += nb > 0 ? 1ull : 0ull;
 }
 
 // ------------------------------------------------------------ ray keys
 // RayBoundingbox (src/core/RayBoundingbox.cpp:5-50): origin box of the batch.
-__global__ void k_origin_box(const float4* __restrict__ o, const BatchPlan* __restrict__ plan, uint32_t* box6) {
-  const Segments seg = plan->seg;
+__global__ void __launch_bounds__(TB) k_origin_box(const float4* __restrict__ o, const int* __restrict__ table,
+                                                   int max_chunks, const BatchPlan* __restrict__ plan,
+                                                   uint32_t* box6) {
+  __shared__ Segments seg;
+  __shared__ float red[TB / 32][6];
+  load_segments(plan, seg);
   const int n = plan->nb;
   float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 p = o[seg_source(seg, i)];
+    float4 p = o[seg_source(seg, table, max_chunks, i)];
     mn[0] = fminf(mn[0], p.x); mn[1] = fminf(mn[1], p.y); mn[2] = fminf(mn[2], p.z);
     mx[0] = fmaxf(mx[0], p.x); mx[1] = fmaxf(mx[1], p.y); mx[2] = fmaxf(mx[2], p.z);
   }
@@ -284,22 +391,34 @@ __global__ void k_origin_box(const float4* __restrict__ o, const BatchPlan* __re
       mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], s));
       mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], s));
     }
+  const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
     for (int a = 0; a < 3; ++a) {
-      atomicMin(&box6[a], f2ord(mn[a]));
-      atomicMax(&box6[3 + a], f2ord(mx[a]));
+      red[warp][a] = mn[a];
+      red[warp][3 + a] = mx[a];
     }
+  __syncthreads();
+  if (threadIdx.x < 6) {  // one atomic per block and component
+    const int a = threadIdx.x;
+    float v = red[0][a];
+    for (int w = 1; w < TB / 32; ++w) v = a < 3 ? fminf(v, red[w][a]) : fmaxf(v, red[w][a]);
+    if (a < 3) atomicMin(&box6[a], f2ord(v));
+    else atomicMax(&box6[a], f2ord(v));
+  }
 }
 
 __global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d,
+                                                 const int* __restrict__ table, int max_chunks, int nbins,
                                                  const BatchPlan* __restrict__ plan,
                                                  const uint32_t* __restrict__ box6, uint32_t* __restrict__ keys) {
+  __shared__ Segments seg;
   const int n = plan->nb;
+  if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole block
+  load_segments(plan, seg);
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const Segments& seg = plan->seg;
   const int prefix_bits = plan->prefix_bits;
-  const int src = seg_source(seg, i);
+  const int src = seg_source(seg, table, max_chunks, i);
   float3 lo = f3(ord2f(box6[0]), ord2f(box6[1]), ord2f(box6[2]));
   float3 hi = f3(ord2f(box6[3]), ord2f(box6[4]), ord2f(box6[5]));
   float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
@@ -307,20 +426,24 @@ __global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, c
   const float4 dd = d[src];
   uint32_t key = ray_sort_key(f3(o[src]), f3(dd), lo, sc);
   if (prefix_bits > 0) {
-    const uint32_t prefix = ((uint32_t)info_scene(__float_as_int(dd.w)) << 3) | (uint32_t)cardinal_bin(f3(dd));
+    const uint32_t prefix = ((uint32_t)info_scene(__float_as_int(dd.w)) << plan->bin_bits) |
+                            (uint32_t)ray_bin(f3(dd), nbins);
     key = (prefix << (32 - prefix_bits)) | (key >> prefix_bits);
   }
   keys[i] = key;
 }
 
 // RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
-__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const BatchPlan* __restrict__ plan,
+__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const int* __restrict__ table, int max_chunks,
+                                               const BatchPlan* __restrict__ plan,
                                                const uint32_t* __restrict__ perm, RayBuf dst) {
+  __shared__ Segments seg;
   const int n = plan->nb;
+  if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole block
+  load_segments(plan, seg);
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const Segments& seg = plan->seg;
-  const int i = seg_source(seg, perm ? (int)perm[j] : j);
+  const int i = seg_source(seg, table, max_chunks, perm ? (int)perm[j] : j);
   dst.o[j] = src.o[i];
   dst.d[j] = src.d[i];
   dst.w[j] = src.w[i];
@@ -830,13 +953,26 @@ int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBu
 int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
   const int tiles = (n + kPartTile - 1) / kPartTile;
-  k_part_count<<<tiles, PB, 0, s>>>(src.d, n, n_dev, pool.tile_counts, tiles);
-  // one extra row (the dead bucket) follows the six bins, so every bin's
-  // total is the difference of two scanned row starts
-  k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * PRADIX, nullptr);
-  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, n_dev, pool.tile_counts, tiles, pool.rays, pool.cap, pool.count);
-  k_part_commit<<<1, 32, 0, s>>>(pool.tile_counts, tiles, pool.count, pool.cap, pool.err);
-  return 4;
+  k_part_count<<<tiles, PB, 0, s>>>(src.d, n, n_dev, pool.nbins, pool.tile_counts, tiles);
+  // the dead bucket's row follows the bins', so every bin's total is the
+  // difference of two scanned row starts
+  k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * (pool.nbins + 1), nullptr);
+  k_part_reserve<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
+  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, n_dev, pool.tile_counts, tiles, pool);
+  k_part_commit<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
+  return 5;
+}
+
+int launch_pool_reset(BinPool& pool, cudaStream_t s) {
+  const int n = std::max(pool.num_chunks, kMaxBins);
+  k_pool_reset<<<grid_for(n), TB, 0, s>>>(pool);
+  return 1;
+}
+
+int launch_ray_bins(const float4* d, int n, int nbins, int* out, cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_ray_bins<<<grid_for(n), TB, 0, s>>>(d, n, nbins, out);
+  return 1;
 }
 
 int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
@@ -847,27 +983,28 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
 
 int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
                 Counters* ctr, cudaStream_t s) {
-  k_plan<<<1, 32, 0, s>>>(pool.count, pool.cap, batch_cap, merge, scene_bits, plan, box6, ctr);
+  k_plan<<<1, kBinRadix, 0, s>>>(pool, batch_cap, merge, scene_bits, plan, box6, ctr);
   return 1;
 }
 
-int launch_origin_box(const float4* o, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s) {
+int launch_origin_box(const BinPool& pool, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s) {
   if (n_max <= 0) return 0;
-  k_origin_box<<<std::min(grid_for(n_max), 512), TB, 0, s>>>(o, plan, box6);
+  k_origin_box<<<std::min(grid_for(n_max), 512), TB, 0, s>>>(pool.rays.o, pool.table, pool.max_chunks, plan, box6);
   return 1;
 }
 
-int launch_ray_keys(const float4* o, const float4* d, const BatchPlan* plan, int n_max, const uint32_t* box6,
-                    uint32_t* keys, cudaStream_t s) {
+int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* box6, uint32_t* keys,
+                    cudaStream_t s) {
   if (n_max <= 0) return 0;
-  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(o, d, plan, box6, keys);
+  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.rays.o, pool.rays.d, pool.table, pool.max_chunks, pool.nbins, plan,
+                                            box6, keys);
   return 1;
 }
 
-int launch_gather(const RayBuf& src, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
+int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
                   cudaStream_t s) {
   if (n_max <= 0) return 0;
-  k_gather<<<grid_for(n_max), TB, 0, s>>>(src, plan, perm, dst);
+  k_gather<<<grid_for(n_max), TB, 0, s>>>(pool.rays, pool.table, pool.max_chunks, plan, perm, dst);
   return 1;
 }
 

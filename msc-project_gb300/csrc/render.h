@@ -89,31 +89,44 @@ struct Film {            // per-sample radiance and film position, all jobs (Ima
 // Error bits reported through the engine's device flag word.
 enum : int { ERR_BIN_OVERFLOW = 1, ERR_STACK_OVERFLOW = 2, ERR_TRAVERSAL_CAP = 4, ERR_BVH_INDEX = 8 };
 
-constexpr int kMaxBins = 8;  // 6 cardinal bins + the dead bucket, rounded up
+// Direction bins: the reference's 6 cardinal bins (dominant axis and sign),
+// or the 26 / 98 surface cells of a 3^3 / 5^3 direction cube (extension).
+constexpr int kMaxBins = 98;
+constexpr int kBinRadix = 128;  // partition digits: bins + the dead bucket, rounded up
+// Bin pool chunks: a bin is a list of whole chunks of the pool (a chunk table
+// row), so any number of bins share one pool of about one generation of rays.
+constexpr int kChunkShift = 12;
+constexpr int kChunk = 1 << kChunkShift;
 
-// Where the rays of one batch sit: up to 6 ranges of the bin pool.
+__host__ __device__ __forceinline__ int bin_bits(int nbins) { return nbins <= 8 ? 3 : (nbins <= 32 ? 5 : 7); }
+
+// Where the rays of one batch sit: up to kMaxBins (bin, first position) runs.
 struct Segments {
-  int start[6];
-  int prefix[7];  // prefix[k] = rays in ranges before k; prefix[count] = total
   int count;
+  int prefix[kMaxBins + 1];  // prefix[k] = rays in runs before k; prefix[count] = total
+  int bin[kMaxBins];
+  int start[kMaxBins];       // first position within the bin
 };
 
-// One batch as the device chose it (k_plan): the ranges of the bin pool it
+// One batch as the device chose it (k_plan): the runs of the bin pool it
 // takes, its size and the key prefix width.  Kernels after the plan read it
 // from device memory, so a batch body needs no host decision and can be
 // replayed from a CUDA graph.
 struct BatchPlan {
-  Segments seg;
   int nb;
   int prefix_bits;
+  int bin_bits;
+  int pad;
+  Segments seg;
 };
 
 // Device counters of the wavefront, read back in one copy.
 struct Counters {
-  int bin_count[8];     // rays held per bin (6 used)
-  int shadow_count;     // shadow rays of the current batch
-  int err;              // error bits
-  int pad[6];
+  int bin_count[kBinRadix];  // rays held per bin
+  int shadow_count;          // shadow rays of the current batch
+  int err;                   // error bits
+  int in_bins;               // rays held in all bins
+  int pad[5];
   unsigned long long closest, shadow, batches;
 };
 
@@ -121,15 +134,32 @@ struct Counters {
 int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s);
 
 struct BinPool {
-  RayBuf rays;       // 6 bins of `cap` rays each, bin b at [b*cap, (b+1)*cap)
-  int cap = 0;
-  int* count = nullptr;      // device: rays held per bin
-  uint32_t* tile_counts = nullptr;  // scratch for the partition (kMaxBins * tiles)
+  RayBuf rays;               // num_chunks * kChunk rays
+  int nbins = 6;             // the bin function new rays are sorted by (6, 26 or 98)
+  int num_chunks = 0;
+  int max_chunks = 0;        // chunk-table row length
+  int* count = nullptr;      // device [kMaxBins]: rays held per bin
+  int* held = nullptr;       // device [kMaxBins]: chunks in each bin's row
+  int* table = nullptr;      // device [kMaxBins * max_chunks]: pool chunk of a bin's k-th chunk
+  int* free_stack = nullptr; // device [num_chunks]
+  int* free_top = nullptr;   // device: entries on the free stack
+  int* in_bins = nullptr;    // device: rays held in all bins
+  uint32_t* tile_counts = nullptr;  // partition scratch ((kMaxBins + 1) * tiles)
   int max_tiles = 0;
   int* err = nullptr;
 };
+__host__ __device__ __forceinline__ int pool_index(const int* table, int max_chunks, int bin, int pos) {
+  return table[bin * max_chunks + (pos >> kChunkShift)] * kChunk + (pos & (kChunk - 1));
+}
+// Chunks a pool needs so that `rays_in_flight` rays fit in any split over
+// the bins (each bin holds at most one partial chunk).
+inline size_t bin_pool_chunks(size_t rays_in_flight) {
+  return (rays_in_flight + kChunk - 1) / kChunk + 2 * (size_t)kMaxBins;
+}
+// Empties the pool: every chunk free (stream-ordered).
+int launch_pool_reset(BinPool& pool, cudaStream_t s);
 constexpr int kPartTile = 2048;
-// Stable partition of src[0, n) by cardinal bin, appended behind each bin's
+// Stable partition of src[0, n) by direction bin, appended behind each bin's
 // current content; dead rays (info < 0) are dropped.
 // n_dev (optional): the count is read on the device, n is then its upper bound.
 int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev = nullptr);
@@ -139,17 +169,19 @@ int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s
 // Also opens the batch: origin box reset, shadow count zeroed, counters.
 int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
                 Counters* ctr, cudaStream_t s);
+// Direction bin of each direction (6, 26 or 98 bins).
+int launch_ray_bins(const float4* d, int n, int nbins, int* out, cudaStream_t s);
 
 // Per-ray cardinal bin only (stage test).
 int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 
 // Origin box of the batch rays into box6 (ordered-int min xyz, max xyz; caller initialises).
 // n_max bounds the plan's batch size (grid size).
-int launch_origin_box(const float4* o, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s);
+int launch_origin_box(const BinPool& pool, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s);
 // 32-bit keys; prefix_bits > 0 puts (scene << 3 | cardinal bin) above the origin/direction code.
-int launch_ray_keys(const float4* o, const float4* d, const BatchPlan* plan, int n_max, const uint32_t* box6,
-                    uint32_t* keys, cudaStream_t s);
-int launch_gather(const RayBuf& src, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
+int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* box6, uint32_t* keys,
+                    cudaStream_t s);
+int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
                   cudaStream_t s);
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,

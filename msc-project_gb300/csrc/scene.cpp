@@ -681,6 +681,10 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
         else if (kv.first == "ray sort") { if (!as_int(&kv.second, &S.ext.ray_sort)) return c.fail("bad ray sort"); }
         else if (kv.first == "hit sort") { if (!as_int(&kv.second, &S.ext.hit_sort)) return c.fail("bad hit sort"); }
         else if (kv.first == "autotune") { if (!as_int(&kv.second, &S.ext.autotune)) return c.fail("bad autotune"); }
+        else if (kv.first == "direction bins") {
+          if (!as_int(&kv.second, &S.ext.bins) || (S.ext.bins != 6 && S.ext.bins != 26 && S.ext.bins != 98))
+            return c.fail("direction bins must be 6, 26 or 98");
+        }
         else if (kv.first == "seed") { if (!as_int(&kv.second, &iv)) return c.fail("bad seed"); S.ext.seed = (uint32_t)iv; }
         else if (kv.first == "bvh") {
           std::string m = as_str(&kv.second);

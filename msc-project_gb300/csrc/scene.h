@@ -123,6 +123,7 @@ struct Extensions {  // optional third YAML document; the reference ignores it
   int generation = 0;      // paths per camera generation (0 = automatic)
   int wide_bvh = 1;        // 1: 8-wide quantised BVH, 0: binary LBVH
   int hit_key_bits = 32;   // 32: (geomID, primID); 64: (shader 12 b, face 23 b, quantised uv 29 b)
+  int bins = 6;            // direction bins: 6 (the reference's), 26 or 98
   int autotune = 1;        // 1: the batch loop tunes itself online from the settings above
 };
 

@@ -27,17 +27,28 @@ struct TriHit {
 // Moller-Trumbore with u, v the weights of v1 and v2 (the barycentric
 // convention PolygonObject::texture relies on, src/core/PolygonObject.cpp:45-63).
 // Accepts tmin < t < tmax.
+// Before the IEEE reciprocal, candidates are rejected in det-scaled terms only
+// where the exact test below would reject them too: the signs of u and v are
+// exact, and the upper bounds keep a margin far above the rounding of the
+// scaled sums, so the accepted set and every result are unchanged.
 __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float tmin,
                                               float tmax, float* t_out, float* u_out, float* v_out) {
   float3 p = v_cross(d, e2);
   float det = v_dot(e1, p);
   if (det == 0.0f) return false;
-  float inv = 1.0f / det;
   float3 s = v_sub(o, v0);
-  float u = v_dot(s, p) * inv;
-  if (u < 0.0f || u > 1.0f) return false;
+  const float us = v_dot(s, p);  // u * det
+  const float adet = fabsf(det);
+  const float su = det > 0.0f ? us : -us;  // u * |det|
+  if (su < 0.0f || su > adet * 1.00001f) return false;
   float3 q = v_cross(s, e1);
-  float v = v_dot(d, q) * inv;
+  const float vs = v_dot(d, q);  // v * det
+  const float sv = det > 0.0f ? vs : -vs;
+  if (sv < 0.0f || su + sv > adet * 1.00001f) return false;
+  float inv = 1.0f / det;
+  float u = us * inv;
+  if (u < 0.0f || u > 1.0f) return false;
+  float v = vs * inv;
   if (v < 0.0f || u + v > 1.0f) return false;
   float t = v_dot(e2, q) * inv;
   if (!(t > tmin && t < tmax)) return false;
@@ -154,6 +165,14 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, 
   return ((s < 4 ? lo_word : hi_word) >> (8 * (s & 3))) & 0xffu;
 }
 
+// Byte s of the pair as a float, exactly: one byte permute builds the float
+// 2^23 + byte, one subtraction removes 2^23 (integer-to-float conversions run
+// on a slower pipe than these two).
+__device__ __forceinline__ float byte_float(uint32_t lo_word, uint32_t hi_word, int s) {
+  const uint32_t bits = __byte_perm(s < 4 ? lo_word : hi_word, 0x00004B00u, (uint32_t)(s & 3) | 0x5440u);
+  return __uint_as_float(bits) - 8388608.0f;
+}
+
 // Node and triangle indices are checked against num_nodes / num_tris before
 // every fetch; a bad index ends the ray with *overflow = 3 instead of reading
 // outside the arrays.
@@ -207,12 +226,12 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
       for (int s = 0; s < 8; ++s) {
         const uint32_t m = byte_of(B.z, B.w, s);
         const bool inner = ((imask >> s) & 1u) != 0u;
-        const float tlx = fmaf((float)byte_of(Q0.x, Q0.y, s), ax, bx);
-        const float tly = fmaf((float)byte_of(Q0.z, Q0.w, s), ay, by);
-        const float tlz = fmaf((float)byte_of(Q1.x, Q1.y, s), az, bz);
-        const float thx = fmaf((float)byte_of(Q1.z, Q1.w, s), ax, bx);
-        const float thy = fmaf((float)byte_of(Q2.x, Q2.y, s), ay, by);
-        const float thz = fmaf((float)byte_of(Q2.z, Q2.w, s), az, bz);
+        const float tlx = fmaf(byte_float(Q0.x, Q0.y, s), ax, bx);
+        const float tly = fmaf(byte_float(Q0.z, Q0.w, s), ay, by);
+        const float tlz = fmaf(byte_float(Q1.x, Q1.y, s), az, bz);
+        const float thx = fmaf(byte_float(Q1.z, Q1.w, s), ax, bx);
+        const float thy = fmaf(byte_float(Q2.x, Q2.y, s), ay, by);
+        const float thz = fmaf(byte_float(Q2.z, Q2.w, s), az, bz);
         const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
         const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), tmax)) * widen;
         if (tn <= tf) {

@@ -84,6 +84,8 @@ def load_library():
         "msc_get_samples": (I, [P, F, F]),
         "msc_stage_cardinal": (I, [F, I, C.POINTER(C.c_int32)]),
         "msc_stage_bin_partition": (I, [F, I, I, F, C.POINTER(C.c_int32)]),
+        "msc_stage_bin_partition_n": (I, [F, I, I, I, F, C.POINTER(C.c_int32)]),
+        "msc_stage_ray_bins": (I, [F, I, I, C.POINTER(C.c_int32)]),
         "msc_stage_ray_keys": (I, [F, F, I, U32]),
         "msc_sort_pairs": (I, [U32, U32, I, I]),
         "msc_sort_pairs_device": (I, [P, P, I, I, P]),
@@ -205,8 +207,8 @@ class Pathtracer:
         _check(self._lib.msc_get_tuning(self._h, C.byref(t)), self._h)
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, 0, 0)
         _check(self._lib.msc_set_tuning(self._h, C.byref(t)), self._h)
 
     def stats(self):
@@ -255,15 +257,24 @@ def cardinal(dirs):
     return out
 
 
-def bin_partition(rays, cap):
-    """rays: (n, 12) float32 records; returns (6*cap, 12) bins and 6 counts."""
+def bin_partition(rays, cap, nbins=6):
+    """rays: (n, 12) float32 records; returns (nbins*cap, 12) bins and nbins counts."""
     lib = load_library()
     rays = np.ascontiguousarray(rays, np.float32)
-    out = np.zeros((6 * cap, 12), np.float32)
-    counts = np.zeros(6, np.int32)
-    _check(lib.msc_stage_bin_partition(_ptr(rays, C.c_float), rays.shape[0], cap, _ptr(out, C.c_float),
-                                       _ptr(counts, C.c_int32)))
+    out = np.zeros((nbins * cap, 12), np.float32)
+    counts = np.zeros(nbins, np.int32)
+    _check(lib.msc_stage_bin_partition_n(_ptr(rays, C.c_float), rays.shape[0], nbins, cap, _ptr(out, C.c_float),
+                                         _ptr(counts, C.c_int32)))
     return out, counts
+
+
+def ray_bins(dirs, nbins):
+    """Direction bin of each direction among 6, 26 or 98."""
+    lib = load_library()
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(dirs.shape[0], np.int32)
+    _check(lib.msc_stage_ray_bins(_ptr(dirs, C.c_float), dirs.shape[0], nbins, _ptr(out, C.c_int32)))
+    return out
 
 
 def ray_keys(org, dirs):
@@ -333,12 +344,12 @@ def scene_load_host(yaml_path):
 
 class _Tuning(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("tuning", C.c_int), ("samples", C.c_int)]
+                ("bins", C.c_int), ("tuning", C.c_int), ("samples", C.c_int)]
 
 
 class _TuneSample(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("mrays_per_s", C.c_double)]
+                ("bins", C.c_int), ("mrays_per_s", C.c_double)]
 
 
 def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
@@ -429,8 +440,8 @@ class Batch:
         self._check(self._lib.msc_batch_get_tuning(self._b, C.byref(t)))
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, 0, 0)
         self._check(self._lib.msc_batch_set_tuning(self._b, C.byref(t)))
 
     def tune_log(self):

@@ -1359,19 +1359,50 @@ void oracle_stable_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits) {
   memcpy(vals, v2.data(), (size_t)n * 4);
 }
 
-void oracle_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts) {
-  for (int b = 0; b < 6; ++b) counts[b] = 0;
-  memset(out, 0, sizeof(float) * 12 * 6 * (size_t)cap);
+// 26 / 98 bins (extension, no reference counterpart): the surface cells of
+// an m^3 cube over [-1,1]^3 (m = 3 or 5), the direction scaled so its largest
+// component has magnitude 1; cells in x-major order, interior cells skipped.
+int orc_ray_bin(float x, float y, float z, int nbins) {
+  if (nbins == 6) return orc::cardinal(x, y, z);
+  const int m = nbins == 26 ? 3 : 5;
+  const float mx = std::max(std::max(std::fabs(x), std::fabs(y)), std::fabs(z));
+  if (!(mx > 0.f)) return 0;
+  const float inv = 1.0f / mx;
+  const float half_m = 0.5f * (float)m;
+  const float v[3] = {x * inv, y * inv, z * inv};
+  int c[3];
+  for (int a = 0; a < 3; ++a) c[a] = std::min(m - 1, std::max(0, (int)std::floor((v[a] + 1.0f) * half_m)));
+  const int n_in = m - 2;
+  int interior_before = 0;  // interior cells (all coordinates in [1, m-2]) with a smaller index
+  for (int i = 1; i <= m - 2; ++i)
+    for (int j = 1; j <= m - 2; ++j)
+      for (int k = 1; k <= m - 2; ++k)
+        if ((i * m + j) * m + k < (c[0] * m + c[1]) * m + c[2]) ++interior_before;
+  (void)n_in;
+  return (c[0] * m + c[1]) * m + c[2] - interior_before;
+}
+
+void oracle_ray_bins(const float* dirs, int n, int nbins, int32_t* bins) {
+  for (int i = 0; i < n; ++i) bins[i] = orc_ray_bin(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], nbins);
+}
+
+void oracle_bin_partition_n(const float* rays, int n, int nbins, int cap, float* out, int32_t* counts) {
+  for (int b = 0; b < nbins; ++b) counts[b] = 0;
+  memset(out, 0, sizeof(float) * 12 * (size_t)nbins * (size_t)cap);
   for (int i = 0; i < n; ++i) {
     const float* r = rays + 12 * i;
     int32_t depth;
     memcpy(&depth, &r[7], 4);
     if (depth < 0) continue;
-    int b = orc::cardinal(r[4], r[5], r[6]);
+    int b = orc_ray_bin(r[4], r[5], r[6], nbins);
     if (counts[b] >= cap) continue;
     memcpy(out + 12 * ((size_t)b * cap + counts[b]), r, 48);
     counts[b]++;
   }
+}
+
+void oracle_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts) {
+  oracle_bin_partition_n(rays, n, 6, cap, out, counts);
 }
 
 void oracle_tent_filter(const float* rgb, const float* xy, int w, int h, int spp, float* pixels) {

@@ -38,6 +38,8 @@ def lib():
         L.oracle_ray_keys.argtypes = [F, F, I, U32]
         L.oracle_stable_sort_pairs.argtypes = [U32, U32, I, I]
         L.oracle_bin_partition.argtypes = [F, I, I, F, I32]
+        L.oracle_ray_bins.argtypes = [F, I, I, I32]
+        L.oracle_bin_partition_n.argtypes = [F, I, I, I, F, I32]
         L.oracle_tent_filter.argtypes = [F, F, I, I, I, F]
         L.oracle_obj_load.argtypes = [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]
         _lib = L
@@ -141,6 +143,22 @@ def stable_sort_pairs(keys, vals, bits=32):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     lib().oracle_stable_sort_pairs(_p(k, C.c_uint32), _p(v, C.c_uint32), k.shape[0], bits)
     return k, v
+
+
+def ray_bins(dirs, nbins):
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(dirs.shape[0], np.int32)
+    lib().oracle_ray_bins(_p(dirs, C.c_float), dirs.shape[0], nbins, _p(out, C.c_int32))
+    return out
+
+
+def bin_partition_n(rays, nbins, cap):
+    rays = np.ascontiguousarray(rays, np.float32)
+    out = np.zeros((nbins * cap, 12), np.float32)
+    counts = np.zeros(nbins, np.int32)
+    lib().oracle_bin_partition_n(_p(rays, C.c_float), rays.shape[0], nbins, cap, _p(out, C.c_float),
+                                 _p(counts, C.c_int32))
+    return out, counts
 
 
 def bin_partition(rays, cap):

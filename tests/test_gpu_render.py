@@ -198,3 +198,16 @@ def test_hit_key_width_and_sorting_do_not_change_the_image(built, stress_scene, 
             images.append(pt.image())
     for im in images[1:]:
         assert np.array_equal(im.view(np.uint32), images[0].view(np.uint32))
+
+
+@pytest.mark.parametrize("nbins", [26, 98])
+def test_direction_bin_count_does_not_change_the_image(built, box_scene, nbins):
+    mscgpu, _ = built
+    imgs = []
+    for nb in (6, nbins):
+        with mscgpu.Pathtracer(box_scene) as pt:
+            pt.set_tuning(batch_exponent=12, trace_block=128, ray_sort=True, hit_sort=True, bins=nb)
+            assert pt.tuning()["bins"] == nb
+            pt.process()
+            imgs.append(pt.image())
+    assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))

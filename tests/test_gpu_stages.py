@@ -166,3 +166,26 @@ def test_sort_keys64_is_the_stable_order(built):
         keys = hi | (mid if n < 5000 else (mid & np.uint64(0xF << 29))) | (lo & np.uint64(0xFF))  # many ties
         perm = mscgpu.sort_keys64(keys)
         assert np.array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+
+
+@pytest.mark.parametrize("nbins", [6, 26, 98])
+def test_ray_bins_bit_exact(built, nbins):
+    mscgpu, oracle = built
+    d = _dirs(np.random.default_rng(nbins), 50000)
+    got = mscgpu.ray_bins(d, nbins)
+    assert np.array_equal(got, oracle.ray_bins(d, nbins))
+    assert got.min() >= 0 and got.max() < nbins
+    assert len(np.unique(got)) == nbins  # every cell is reached
+
+
+@pytest.mark.parametrize("nbins,n", [(26, 1), (26, 9000), (98, 2049), (98, 150000)])
+def test_bin_partition_n_bins_stable_and_bit_exact(built, nbins, n):
+    """The chunked bin pool: every bin's rays in arrival order, across chunk boundaries."""
+    mscgpu, oracle = built
+    rays = _rays(np.random.default_rng(n + nbins), n)
+    cap = max(n, 1)
+    got, gc = mscgpu.bin_partition(rays, cap, nbins)
+    want, wc = oracle.bin_partition_n(rays, nbins, cap)
+    assert np.array_equal(gc, wc)
+    for b in range(nbins):
+        assert np.array_equal(got[b * cap: b * cap + gc[b]].view(np.uint32), want[b * cap: b * cap + wc[b]].view(np.uint32))
