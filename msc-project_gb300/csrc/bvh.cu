@@ -4,7 +4,8 @@
 // 242-274).  Steps: centroid bounds -> 30-bit Morton codes -> stable radix
 // sort -> one thread per internal node finds its range and split -> one
 // thread per leaf walks to the root, the second arrival at each node
-// forming its box -> pack into the traversal layout of trace.cuh.
+// forming its box -> treelet restructuring rounds (SAH) -> pack into the
+// traversal layout of trace.cuh.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -170,6 +171,169 @@ __global__ void k_refit(const int2* __restrict__ children, const int* __restrict
   }
 }
 
+// ------------------------------------------------------------ treelet restructuring
+// Karras and Aila, "Fast Parallel Construction of High-Quality Bounding Volume
+// Hierarchies" (HPG 2013): bottom-up over the LBVH, every node with at least
+// 7 leaves below roots a treelet of 7 leaves (grown by opening the treelet leaf
+// of largest surface area); the SAH-optimal binary tree over those 7 leaves is
+// found by dynamic programming over their 127 subsets and replaces the
+// treelet when it is cheaper, reusing the treelet's 6 internal nodes.  One
+// thread per treelet; a round is one bottom-up pass.
+constexpr int kTreeletRounds = 3;
+constexpr float kCostNode = 1.2f;  // SAH cost of a node visit relative to a triangle test
+constexpr float kCostTri = 1.0f;
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+  const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+  return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ void box_of(int c, const float4* leaf_box, const float4* node_box, float4* lo, float4* hi) {
+  if (c < 0) {
+    *lo = __ldcg(&leaf_box[2 * (~c) + 0]);
+    *hi = __ldcg(&leaf_box[2 * (~c) + 1]);
+  } else {
+    *lo = __ldcg(&node_box[2 * c + 0]);
+    *hi = __ldcg(&node_box[2 * c + 1]);
+  }
+}
+
+__global__ void k_treelet(int2* children, int* parent, int n, const float4* __restrict__ leaf_box, float4* node_box,
+                          float* cost, int* leaves, int* flags, int* err) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int p = parent[(n - 1) + k];
+  int level = 0;
+  float s_area[128], s_cost[128];
+  uint8_t s_best[128];
+  while (p >= 0) {
+    if (++level > n) {
+      atomicOr(err, 1);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(&flags[p], 1) == 0) return;
+    __threadfence();
+    const int2 ch = __ldcg(&children[p]);
+    float4 l0, h0, l1, h1;
+    box_of(ch.x, leaf_box, node_box, &l0, &h0);
+    box_of(ch.y, leaf_box, node_box, &l1, &h1);
+    const float4 lo = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f);
+    const float4 hi = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f);
+    const int nl = (ch.x < 0 ? 1 : __ldcg(&leaves[ch.x])) + (ch.y < 0 ? 1 : __ldcg(&leaves[ch.y]));
+    const float cl = ch.x < 0 ? kCostTri * half_area(l0, h0) : __ldcg(&cost[ch.x]);
+    const float cr = ch.y < 0 ? kCostTri * half_area(l1, h1) : __ldcg(&cost[ch.y]);
+    float cp = kCostNode * half_area(lo, hi) + cl + cr;
+    if (nl >= 7) {
+      // grow the treelet: open the internal treelet leaf of largest area until 7 leaves
+      int tl[7], inner[6];
+      tl[0] = ch.x;
+      tl[1] = ch.y;
+      int ntl = 2, ninner = 0;
+      while (ntl < 7) {
+        int bi = -1;
+        float ba = -1.f;
+        for (int i = 0; i < ntl; ++i) {
+          if (tl[i] < 0) continue;
+          float4 a, b;
+          box_of(tl[i], leaf_box, node_box, &a, &b);
+          const float ar = half_area(a, b);
+          if (ar > ba) { ba = ar; bi = i; }
+        }
+        if (bi < 0) break;
+        const int2 c2 = __ldcg(&children[tl[bi]]);
+        inner[ninner++] = tl[bi];
+        tl[bi] = c2.x;
+        tl[ntl++] = c2.y;
+      }
+      if (ntl == 7) {
+        // subset areas and optimal costs
+        for (int S = 1; S < 128; ++S) {
+          float4 a = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), b = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+          for (int i = 0; i < 7; ++i) {
+            if (!((S >> i) & 1)) continue;
+            float4 x, y;
+            box_of(tl[i], leaf_box, node_box, &x, &y);
+            a = make_float4(fminf(a.x, x.x), fminf(a.y, x.y), fminf(a.z, x.z), 0.f);
+            b = make_float4(fmaxf(b.x, y.x), fmaxf(b.y, y.y), fmaxf(b.z, y.z), 0.f);
+          }
+          s_area[S] = half_area(a, b);
+        }
+        for (int i = 0; i < 7; ++i) {
+          const int S = 1 << i;
+          s_cost[S] = tl[i] < 0 ? kCostTri * s_area[S] : __ldcg(&cost[tl[i]]);
+          s_best[S] = 0;
+        }
+        for (int S = 1; S < 128; ++S) {
+          if ((S & (S - 1)) == 0) continue;
+          const int low = S & -S;
+          float best = 3.0e38f;
+          int bp = 0;
+          // partitions (P, S \ P) with the lowest element in P
+          const int rest = S ^ low;
+          for (int Q = rest;; Q = (Q - 1) & rest) {
+            const int P = low | Q;
+            if (P != S) {
+              const float c = s_cost[P] + s_cost[S ^ P];
+              if (c < best) { best = c; bp = P; }
+            }
+            if (Q == 0) break;
+          }
+          s_cost[S] = kCostNode * s_area[S] + best;
+          s_best[S] = (uint8_t)bp;
+        }
+        if (s_cost[127] < cp * 0.9999f) {
+          // rebuild: subsets in creation order, the treelet root keeps node p
+          int sets[6], ids[6], nsets = 1, next = 0;
+          sets[0] = 127;
+          ids[0] = p;
+          for (int q = 0; q < nsets; ++q) {
+            const int S = sets[q], P = s_best[S];
+            int cid[2];
+            const int part[2] = {P, S ^ P};
+            for (int h = 0; h < 2; ++h) {
+              const int X = part[h];
+              if ((X & (X - 1)) == 0) {
+                cid[h] = tl[__ffs(X) - 1];
+              } else {
+                cid[h] = inner[next++];
+                sets[nsets] = X;
+                ids[nsets] = cid[h];
+                ++nsets;
+              }
+              const int c = cid[h];
+              if (c < 0) parent[(n - 1) + ~c] = ids[q];
+              else parent[c] = ids[q];
+            }
+            __stcg(&children[ids[q]], make_int2(cid[0], cid[1]));
+          }
+          // boxes, costs and leaf counts bottom-up (children were created after their parents)
+          for (int q = nsets - 1; q >= 0; --q) {
+            const int id = ids[q];
+            const int2 cc = __ldcg(&children[id]);
+            float4 a0, b0, a1, b1;
+            box_of(cc.x, leaf_box, node_box, &a0, &b0);
+            box_of(cc.y, leaf_box, node_box, &a1, &b1);
+            const float4 bl = make_float4(fminf(a0.x, a1.x), fminf(a0.y, a1.y), fminf(a0.z, a1.z), 0.f);
+            const float4 bh = make_float4(fmaxf(b0.x, b1.x), fmaxf(b0.y, b1.y), fmaxf(b0.z, b1.z), 0.f);
+            __stcg(&node_box[2 * id + 0], bl);
+            __stcg(&node_box[2 * id + 1], bh);
+            __stcg(&cost[id], s_cost[sets[q]]);
+            __stcg(&leaves[id], __popc(sets[q]) == 7 ? nl : (cc.x < 0 ? 1 : __ldcg(&leaves[cc.x])) +
+                                                               (cc.y < 0 ? 1 : __ldcg(&leaves[cc.y])));
+          }
+          cp = s_cost[127];
+        }
+      }
+    }
+    __stcg(&node_box[2 * p + 0], lo);  // a restructured treelet keeps its leaf set, so its box
+    __stcg(&node_box[2 * p + 1], hi);
+    __stcg(&cost[p], cp);
+    __stcg(&leaves[p], nl);
+    p = __ldcg(&parent[p]);
+  }
+}
+
 __global__ void k_pack(const int2* __restrict__ children, int n, const float4* __restrict__ leaf_box,
                        const float4* __restrict__ node_box, float4* __restrict__ nodes) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -247,8 +411,8 @@ uint32_t q_hi(float p, float s, float v) {
 
 void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>& nbox, const std::vector<float4>& lbox,
                    WideBuild* out) {
-  // leaf range [first, first + count) of every internal node, children before parents
-  std::vector<int> first(n - 1), count(n - 1), bfs;
+  // leaf count of every internal node, children before parents
+  std::vector<int> count(n - 1), bfs;
   bfs.reserve(n - 1);
   bfs.push_back(0);
   for (size_t i = 0; i < bfs.size(); ++i) {
@@ -259,9 +423,7 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
   for (size_t i = bfs.size(); i-- > 0;) {
     int b = bfs[i];
     int2 c = ch[b];
-    int fl = c.x < 0 ? ~c.x : first[c.x], cl = c.x < 0 ? 1 : count[c.x];
-    int fr = c.y < 0 ? ~c.y : first[c.y], cr = c.y < 0 ? 1 : count[c.y];
-    first[b] = std::min(fl, fr);
+    const int cl = c.x < 0 ? 1 : count[c.x], cr = c.y < 0 ? 1 : count[c.y];
     count[b] = cl + cr;
   }
   auto is_leafish = [&](int c) { return c < 0 || count[c] <= kWideLeafMax; };
@@ -337,9 +499,21 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
       if (!filled[i]) continue;  // an empty slot
       uint32_t m = 0;
       if (is_leafish(c)) {
-        const int f = c < 0 ? ~c : first[c], cnt = c < 0 ? 1 : count[c];
+        // the subtree's leaves (restructured treelets need not hold a
+        // contiguous leaf range, so they are collected by a walk)
         const uint32_t off = (uint32_t)out->tri_perm.size() - tri_base;
-        for (int t = 0; t < cnt; ++t) out->tri_perm.push_back(f + t);
+        int walk[2 * kWideLeafMax], nw = 0, cnt = 0;
+        walk[nw++] = c;
+        while (nw > 0) {
+          const int x = walk[--nw];
+          if (x < 0) {
+            out->tri_perm.push_back(~x);
+            ++cnt;
+          } else {
+            walk[nw++] = ch[x].y;
+            walk[nw++] = ch[x].x;
+          }
+        }
         m = ((uint32_t)cnt << 5) | off;
       } else {
         imask |= 1u << i;
@@ -389,7 +563,7 @@ int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n
   }
   // build scratch
   size_t bytes = al(6 * 4) + al((size_t)n * 4) * 2 + al((size_t)(n - 1) * sizeof(int2)) + al((size_t)(2 * n) * 4) +
-                 al((size_t)n * 2 * sizeof(float4)) + al((size_t)(n - 1) * 2 * sizeof(float4)) + al((size_t)n * 4) +
+                 al((size_t)n * 2 * sizeof(float4)) + al((size_t)(n - 1) * 2 * sizeof(float4)) + 3 * al((size_t)n * 4) +
                  sort_scratch_bytes(n);
   char* scratch = nullptr;
   if (cudaMalloc(&scratch, bytes) != cudaSuccess) { *err = "out of device memory for the BVH build"; return -1; }
@@ -402,6 +576,8 @@ int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n
   float4* leaf_box = (float4*)p; p += al((size_t)n * 2 * sizeof(float4));
   float4* node_box = (float4*)p; p += al((size_t)(n - 1) * 2 * sizeof(float4));
   int* flags = (int*)p; p += al((size_t)n * 4);
+  float* tcost = (float*)p; p += al((size_t)n * 4);
+  int* tleaves = (int*)p; p += al((size_t)n * 4);
   SortScratch ss;
   sort_scratch_bind(&ss, p, n);
 
@@ -417,6 +593,12 @@ int bvh_build(const float* d_v, const int* d_geom, const uint8_t* d_light, int n
   k_karras<<<(n - 1 + tb - 1) / tb, tb, 0, stream>>>(codes, n, children, parent);
   k_leaves<<<g, tb, 0, stream>>>(d_v, d_geom, d_light, order, n, out->tris, out->tri_orig, leaf_box);
   k_refit<<<g, tb, 0, stream>>>(children, parent, n, leaf_box, node_box, flags, (int*)(bounds + 7));
+  for (int round = 0; round < kTreeletRounds && n >= 7; ++round) {
+    cudaMemsetAsync(flags, 0, (size_t)n * 4, stream);
+    k_treelet<<<g, tb, 0, stream>>>(children, parent, n, leaf_box, node_box, tcost, tleaves, flags,
+                                    (int*)(bounds + 7));
+    ++launches;
+  }
   k_pack<<<(n - 1 + tb - 1) / tb, tb, 0, stream>>>(children, n, leaf_box, node_box, out->nodes);
   k_scene_bounds<<<1, 1, 0, stream>>>(node_box, out->bounds_dev);
   launches += 5;

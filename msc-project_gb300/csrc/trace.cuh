@@ -182,6 +182,10 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
                                            TriHit* hit, int* overflow) {
   const float3 id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
   const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  // per axis, the entry plane of a child box is its low plane when the
+  // inverse direction is positive and its high plane otherwise (the step
+  // scale is positive), so the slab min/max reduce to a choice per node
+  const bool nx = id.x < 0.f, ny = id.y < 0.f, nz = id.z < 0.f;
   uint2 stack[kWideStack];
   int sp = 0;
   // the root as the only child of a virtual group: base 0, slot 0 internal
@@ -221,19 +225,24 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
       const float bx = (__uint_as_float(A.x) - o.x) * id.x;
       const float by = (__uint_as_float(A.y) - o.y) * id.y;
       const float bz = (__uint_as_float(A.z) - o.z) * id.z;
+      // quantised planes: lo x (Q0.x, Q0.y), lo y (Q0.z, Q0.w), lo z (Q1.x, Q1.y),
+      // hi x (Q1.z, Q1.w), hi y (Q2.x, Q2.y), hi z (Q2.z, Q2.w); words for slots 0-3, 4-7
+      const uint32_t enx0 = nx ? Q1.z : Q0.x, enx1 = nx ? Q1.w : Q0.y, exx0 = nx ? Q0.x : Q1.z, exx1 = nx ? Q0.y : Q1.w;
+      const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
+      const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
       uint32_t nh = 0u, tm = 0u;
 #pragma unroll
       for (int s = 0; s < 8; ++s) {
         const uint32_t m = byte_of(B.z, B.w, s);
         const bool inner = ((imask >> s) & 1u) != 0u;
-        const float tlx = fmaf(byte_float(Q0.x, Q0.y, s), ax, bx);
-        const float tly = fmaf(byte_float(Q0.z, Q0.w, s), ay, by);
-        const float tlz = fmaf(byte_float(Q1.x, Q1.y, s), az, bz);
-        const float thx = fmaf(byte_float(Q1.z, Q1.w, s), ax, bx);
-        const float thy = fmaf(byte_float(Q2.x, Q2.y, s), ay, by);
-        const float thz = fmaf(byte_float(Q2.z, Q2.w, s), az, bz);
-        const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fmaxf(fminf(tlz, thz), tmin));
-        const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fminf(fmaxf(tlz, thz), tmax)) * widen;
+        const float tnx = fmaf(byte_float(enx0, enx1, s), ax, bx);
+        const float tny = fmaf(byte_float(eny0, eny1, s), ay, by);
+        const float tnz = fmaf(byte_float(enz0, enz1, s), az, bz);
+        const float tfx = fmaf(byte_float(exx0, exx1, s), ax, bx);
+        const float tfy = fmaf(byte_float(exy0, exy1, s), ay, by);
+        const float tfz = fmaf(byte_float(exz0, exz1, s), az, bz);
+        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax)) * widen;
         if (tn <= tf) {
           if (inner) nh |= 1u << ((uint32_t)s ^ oct);
           else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
