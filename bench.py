@@ -266,9 +266,9 @@ def bench_forms(args):
         "paths": sum(job_paths(j) for j in jobs), "mrays_per_s": rate, "wall_s": wall,
         "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
         "speedup_vs_per_job_loop": rate / plain_rate if plain_rate else None,
-        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")},
-        "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["ray_sort"], t["hit_sort"],
-                          round(t["mrays_per_s"], 1)] for t in tune_log]}
+        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")},
+        "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["persistent"], t["ray_sort"],
+                          t["hit_sort"], round(t["mrays_per_s"], 1)] for t in tune_log]}
     # served: Poisson arrivals on the first 16 resident scenes, at each rate
     nres = min(16, len(scenes))
     out["served"] = {"workload": "Poisson arrivals on %d resident scenes, 128^2-512^2, 4-64 spp log-uniform, "
@@ -290,7 +290,7 @@ def bench_forms(args):
             if max_active:
                 b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
             else:
-                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")})
+                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")})
             _, sst = b.serve(reqs)
             row[label] = {"completed": sst["completed"], "mrays_per_s": sst["mrays_per_s"],
                           "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
@@ -391,7 +391,7 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
     ap.add_argument("--tuning", default="auto",
-                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort")
+                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort[,persistent]")
     ap.add_argument("--stress-scale", type=float, default=1.0)
     ap.add_argument("--serve-rates", default="100:6,600:3",
                     help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
@@ -423,8 +423,9 @@ def main():
     pt = mscgpu.Pathtracer(yaml)
     log("scene load + device BVH build %.1f s" % (time.time() - t))
     if args.tuning != "auto":
-        e, nb, blk, rs, hs = (int(x) for x in args.tuning.split(","))
-        pt.set_tuning(batch_exponent=e, bins=nb, trace_block=blk, ray_sort=bool(rs), hit_sort=bool(hs))
+        v = [int(x) for x in args.tuning.split(",")] + [0]
+        pt.set_tuning(batch_exponent=v[0], bins=v[1], trace_block=v[2], ray_sort=bool(v[3]), hit_sort=bool(v[4]),
+                      persistent=bool(v[5]))
     for _ in range(args.warmup):
         pt.process_device()
     clocks = ClockSampler()
@@ -455,7 +456,7 @@ def main():
     prof = pt.stats()
     pt.set_profiling(False)
     tuned = pt.tuning()
-    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins")}
+    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")}
     pt.close()
 
     total_ms = sum(dev_ms)

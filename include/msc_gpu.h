@@ -192,11 +192,12 @@ typedef struct msc_tuning {
   int ray_sort;       /* 1: each batch sorted on the origin/direction key (RaySort.cpp:7-118) */
   int hit_sort;       /* 1: each batch's hits sorted by (geomID, primID) (Pathtracer.cpp:335-339) */
   int bins;           /* direction bins: 6 (DirectionalBins.cpp:37-115) or 26 / 98 (cube surface cells) */
+  int persistent;     /* 1: persistent traversal kernels with per-lane ray refill (8-wide BVH) */
   int tuning;         /* read only: 1 while the autotuner is still sampling */
   int samples;        /* read only: candidate samples booked by the autotuner */
 } msc_tuning;
 typedef struct msc_tune_sample {
-  int batch_exponent, trace_block, ray_sort, hit_sort, bins;
+  int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent;
   double mrays_per_s; /* device-timed rays per second over the candidate's windows */
 } msc_tune_sample;
 /* Starts the online autotuner: the next batches are spread over candidate

@@ -370,7 +370,7 @@ size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // the child that lies farthest back along the octant-s direction, so a ray of
 // octant o that visits slots o ^ 0, o ^ 1, ..., o ^ 7 meets the children
 // roughly front to back without sorting them.
-constexpr int kWideLeafMax = 3;
+constexpr int kWideLeafMax = 2;
 
 struct WideBuild {
   std::vector<uint32_t> words;  // 20 words per node

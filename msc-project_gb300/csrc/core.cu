@@ -56,7 +56,27 @@ SceneGPU::~SceneGPU() {
   if (d_spheres) cudaFree(d_spheres);
   if (d_sphere_light) cudaFree(d_sphere_light);
   if (d_texels) cudaFree(d_texels);
+  if (d_tex_nodes) cudaFree(d_tex_nodes);
+  if (d_tex_ops) cudaFree(d_tex_ops);
+  if (d_tex_images) cudaFree(d_tex_images);
+  if (d_tex_texels) cudaFree(d_tex_texels);
+  if (d_tri_uv) cudaFree(d_tri_uv);
 }
+
+namespace {
+// Post-order program of the texture tree rooted at `node`.
+void emit_tex_program(const std::vector<TexNode>& nodes, int node, std::vector<int2>* ops) {
+  const TexNode& t = nodes[node];
+  if (t.type == TEXNODE_LAYERED) {
+    emit_tex_program(nodes, t.upper, ops);
+    emit_tex_program(nodes, t.lower, ops);
+    emit_tex_program(nodes, t.mask, ops);
+    ops->push_back(make_int2(2, node));
+  } else {
+    ops->push_back(make_int2(t.type == TEXNODE_STANDARD ? 1 : 0, node));
+  }
+}
+}  // namespace
 
 JobRec job_record(const SceneDesc& d, const JobSpec& spec, int scene_id) {
   JobRec f;
@@ -179,6 +199,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   hhi_g_ = A.take<uint32_t>(B);
   hperm1_ = A.take<uint32_t>(B);
   ctr_ = A.take<Counters>(1);
+  trace_counter_ = A.take<int>(2);
   box6_ = A.take<uint32_t>(8);
   plan_ = A.take<BatchPlan>(1);
   sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B)), B);
@@ -197,6 +218,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   }
   CK(cudaMemset(ctr_, 0, sizeof(Counters)));
   CK(cudaMemset(plan_, 0, sizeof(BatchPlan)));
+  persistent_grids_init();
   launch_pool_reset(bins_, stream_);
   CK(cudaStreamSynchronize(stream_));
   CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
@@ -270,6 +292,37 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
   }
   sg->h_tri_orig.resize(T);
   CK(cudaMemcpy(sg->h_tri_orig.data(), sg->bvh.tri_orig, T * sizeof(int), cudaMemcpyDeviceToHost));
+  // image textures: programs into the shader records, nodes, images, texcoords
+  std::vector<int2> tex_ops;
+  for (auto& sh : d.shaders) {
+    if (sh.texture != TEXTURE_TREE) continue;
+    sh.tex_prog = (int)tex_ops.size();
+    emit_tex_program(d.tex_nodes, sh.tex_root, &tex_ops);
+    sh.tex_len = (int)tex_ops.size() - sh.tex_prog;
+  }
+  if (!tex_ops.empty()) {
+    std::vector<int4> ims;
+    std::vector<float4> tx;
+    for (const auto& im : d.images) {
+      ims.push_back(make_int4((int)tx.size(), im.width, im.height, 0));
+      for (size_t i = 0; i < (size_t)im.width * im.height; ++i)
+        tx.push_back(make_float4(im.rgb[3 * i], im.rgb[3 * i + 1], im.rgb[3 * i + 2], 0.f));
+    }
+    if (ims.empty()) ims.push_back(make_int4(0, 1, 1, 0));
+    if (tx.empty()) tx.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float> uv(d.tri_uv);
+    uv.resize((size_t)6 * T, 0.f);
+    CK(cudaMalloc(&sg->d_tex_nodes, d.tex_nodes.size() * sizeof(TexNode)));
+    CK(cudaMalloc(&sg->d_tex_ops, tex_ops.size() * sizeof(int2)));
+    CK(cudaMalloc(&sg->d_tex_images, ims.size() * sizeof(int4)));
+    CK(cudaMalloc(&sg->d_tex_texels, tx.size() * sizeof(float4)));
+    CK(cudaMalloc(&sg->d_tri_uv, uv.size() * sizeof(float)));
+    CK(cudaMemcpy(sg->d_tex_nodes, d.tex_nodes.data(), d.tex_nodes.size() * sizeof(TexNode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg->d_tex_ops, tex_ops.data(), tex_ops.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg->d_tex_images, ims.data(), ims.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg->d_tex_texels, tx.data(), tx.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(sg->d_tri_uv, uv.data(), uv.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&sg->d_shaders, std::max<size_t>(1, d.shaders.size()) * sizeof(ShaderRec)));
   CK(cudaMalloc(&sg->d_geoms, std::max<size_t>(1, geoms.size()) * sizeof(GeomRec)));
   CK(cudaMalloc(&sg->d_lights, std::max<size_t>(1, d.lights.size()) * sizeof(LightRec)));
@@ -293,6 +346,11 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
   r.light_pick = r.num_lights > 0 ? 1.f / (float)r.num_lights : 0.f;
   r.tri_base = total_tris_;
   r.hit_key_bits = d.ext.hit_key_bits;
+  r.tex_nodes = sg->d_tex_nodes;
+  r.tex_ops = sg->d_tex_ops;
+  r.tex_images = sg->d_tex_images;
+  r.tex_texels = sg->d_tex_texels;
+  r.tri_uv = sg->d_tri_uv;
   if (!d.sphere_lights.empty()) {
     std::vector<float4> sp;
     for (int li : d.sphere_lights) {
@@ -587,9 +645,10 @@ uint64_t Core::graph_key() const {
   while ((1 << (bexp + 1)) <= batch_size_) ++bexp;
   const uint64_t block = trace_block == 64 ? 0 : (trace_block == 128 ? 1 : 2);
   const uint64_t bins = bins_.nbins == 6 ? 0 : (bins_.nbins == 26 ? 1 : 2);
+  const uint64_t pers = persistent_trace ? 1 : 0;
   return ns | (k64 << 9) | ((uint64_t)hit_bits_ << 10) | ((uint64_t)ray_sort << 16) | ((uint64_t)hit_sort << 17) |
          ((uint64_t)merge_bins << 18) | ((uint64_t)wide_ << 19) | (bexp << 20) | (block << 25) | (bins << 27) |
-         (1ull << 63);
+         (pers << 29) | (1ull << 63);
 }
 
 void Core::drop_graph() {
@@ -637,7 +696,8 @@ int Core::enqueue_batch() {
   }
   {
     StageClock t(this, MSC_STAGE_TRACE);
-    t.done(launch_trace_closest(d_scenes_, ns, s0, batch_.o, batch_.d, B, hits_, errw, st, nb, trace_block));
+    t.done(launch_trace_closest(d_scenes_, ns, s0, batch_.o, batch_.d, B, hits_, errw, st, nb, trace_block,
+                                persistent_trace ? trace_counter_ : nullptr));
   }
   const uint32_t* order = nullptr;
   if (hit_sort && ns == 1 && s0.hit_key_bits == 64) {
@@ -672,7 +732,7 @@ int Core::enqueue_batch() {
   {
     StageClock t(this, MSC_STAGE_SHADOW);
     t.done(launch_trace_shadow(d_scenes_, ns, s0, shadow_, shc, B, film_.rgb, errw, st, &ctr_->shadow,
-                               trace_block));
+                               trace_block, persistent_trace ? trace_counter_ + 1 : nullptr));
   }
   {
     StageClock t(this, MSC_STAGE_BINS);
@@ -810,6 +870,7 @@ TuneChoice Core::choice() const {
   c.ray_sort = ray_sort;
   c.hit_sort = hit_sort;
   c.bins = bins_.nbins;
+  c.persistent = persistent_trace;
   return c;
 }
 
@@ -820,6 +881,7 @@ void Core::apply(const TuneChoice& c) {
   ray_sort = c.ray_sort;
   hit_sort = c.hit_sort;
   bins_.nbins = (c.bins == 26 || c.bins == 98) ? c.bins : 6;
+  persistent_trace = c.persistent;
 }
 
 void Core::start_autotune(int windows) {
@@ -859,6 +921,11 @@ void Core::tune_begin_dim() {
       for (int b : {64, 128, 256}) {
         TuneChoice c = base;
         c.block = b;
+        add(c);
+      }
+      if (wide_) {
+        TuneChoice c = base;
+        c.persistent = true;
         add(c);
       }
     } else if (tune_dim_ == 3) {

@@ -38,6 +38,11 @@ struct SceneGPU {
   float4* d_spheres = nullptr;        // sphere lights: centre, radius
   int* d_sphere_light = nullptr;
   unsigned short* d_texels = nullptr; // face texels (FP16 bits)
+  TexNode* d_tex_nodes = nullptr;     // image textures
+  int2* d_tex_ops = nullptr;
+  int4* d_tex_images = nullptr;
+  float4* d_tex_texels = nullptr;
+  float* d_tri_uv = nullptr;
   std::vector<int> h_tri_orig;  // leaf order -> global triangle index
   SceneRec rec;
   ~SceneGPU();
@@ -76,6 +81,7 @@ struct TuneChoice {
   bool ray_sort = true; // origin/direction key sort of each batch
   bool hit_sort = true; // (geomID, primID) sort of each batch's hits
   int bins = 6;         // direction bins: 6, 26 or 98
+  bool persistent = false;  // persistent traversal with per-lane ray refill
 };
 
 struct TuneSample {
@@ -100,6 +106,7 @@ class Core {
   bool use_graph = true;   // replay the batch body from a captured CUDA graph (eager launches when profiling)
   int max_batches_per_step = 16;  // batch bodies enqueued between two host looks at the counters
   int trace_block = 128;          // traversal block size
+  bool persistent_trace = false;  // persistent traversal kernels (8-wide BVH)
 
   // Online autotuner: while on, the next batches are spread over candidate
   // choices (coordinate descent: batch size, direction bins, traversal
@@ -193,6 +200,7 @@ class Core {
   float4* hits_ = nullptr;
   ShadowBuf shadow_;
   Counters* ctr_ = nullptr;    // device counters
+  int* trace_counter_ = nullptr;  // ray counters of the persistent traversal (closest, shadow)
   Counters* h_ctr_ = nullptr;  // pinned copy
   BatchPlan* plan_ = nullptr;
   cudaGraphExec_t graph_ = nullptr;

@@ -939,6 +939,7 @@ static void tuning_of(Core& c, msc_tuning* out) {
   out->ray_sort = t.ray_sort ? 1 : 0;
   out->hit_sort = t.hit_sort ? 1 : 0;
   out->bins = t.bins;
+  out->persistent = t.persistent ? 1 : 0;
   out->tuning = c.tuning() ? 1 : 0;
   out->samples = (int)c.tune_log.size();
 }
@@ -969,6 +970,7 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   c.ray_sort = in->ray_sort != 0;
   c.hit_sort = in->hit_sort != 0;
   c.bins = in->bins;
+  c.persistent = in->persistent != 0;
   core.stop_autotune();
   core.apply(c);
   return MSC_OK;
@@ -995,6 +997,7 @@ int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {
     out[i].ray_sort = log[i].choice.ray_sort ? 1 : 0;
     out[i].hit_sort = log[i].choice.hit_sort ? 1 : 0;
     out[i].bins = log[i].choice.bins;
+    out[i].persistent = log[i].choice.persistent ? 1 : 0;
     out[i].mrays_per_s = log[i].ms > 0 ? log[i].rays / log[i].ms / 1e3 : 0.0;
   }
   return MSC_OK;

@@ -648,6 +648,52 @@ __device__ __forceinline__ BsdfEval bsdf_evaluate(const ShaderRec& s, float3 col
   return e;
 }
 
+// ------------------------------------------------------- image textures
+// StandardTexture::initialize (src/core/StandardTexture.cpp:11-43) looks the
+// image up through OpenImageIO with periodic wrap and zero derivatives; this
+// build wraps (s, t) into [0, 1) and interpolates bilinearly between texel
+// centres, t = 0 being the image's top row.
+__device__ __forceinline__ float3 image_lookup(const float4* __restrict__ texels, int4 im, float s, float t) {
+  const int w = im.y, h = im.z;
+  s = s - floorf(s);
+  t = t - floorf(t);
+  const float x = s * (float)w - 0.5f, y = t * (float)h - 0.5f;
+  const float fx0 = floorf(x), fy0 = floorf(y);
+  const float fx = x - fx0, fy = y - fy0;
+  int x0 = (int)fx0, y0 = (int)fy0;
+  x0 = x0 < 0 ? x0 + w : (x0 >= w ? x0 - w : x0);
+  y0 = y0 < 0 ? y0 + h : (y0 >= h ? y0 - h : y0);
+  const int x1 = x0 + 1 == w ? 0 : x0 + 1, y1 = y0 + 1 == h ? 0 : y0 + 1;
+  const float4 c00 = __ldg(&texels[im.x + y0 * w + x0]), c10 = __ldg(&texels[im.x + y0 * w + x1]);
+  const float4 c01 = __ldg(&texels[im.x + y1 * w + x0]), c11 = __ldg(&texels[im.x + y1 * w + x1]);
+  const float gx = 1.f - fx, gy = 1.f - fy;
+  return f3((c00.x * gx + c10.x * fx) * gy + (c01.x * gx + c11.x * fx) * fy,
+            (c00.y * gx + c10.y * fx) * gy + (c01.y * gx + c11.y * fx) * fy,
+            (c00.z * gx + c10.z * fx) * gy + (c01.z * gx + c11.z * fx) * fy);
+}
+
+// A texture tree as a post-order program on a small value stack;
+// LayeredTexture::initialize (src/core/LayeredTexture.cpp:14-37):
+// upper * mask + lower * (1 - mask).
+constexpr int kTexStack = 34;
+__device__ __noinline__ float3 texture_eval(const SceneRec& sc, int prog, int len, float s, float t) {
+  float3 st[kTexStack];
+  int sp = 0;
+  for (int k = 0; k < len; ++k) {
+    const int2 op = __ldg(&sc.tex_ops[prog + k]);
+    const TexNode& nd = sc.tex_nodes[op.y];
+    if (op.x == 0) {
+      if (sp < kTexStack) st[sp++] = f3(nd.colour[0], nd.colour[1], nd.colour[2]);
+    } else if (op.x == 1) {
+      if (sp < kTexStack) st[sp++] = image_lookup(sc.tex_texels, __ldg(&sc.tex_images[nd.image]), s, t);
+    } else if (sp >= 3) {
+      const float3 m = st[--sp], lo = st[--sp], up = st[--sp];
+      st[sp++] = f3(up.x * m.x + lo.x * (1.f - m.x), up.y * m.y + lo.y * (1.f - m.y), up.z * m.z + lo.z * (1.f - m.z));
+    }
+  }
+  return sp > 0 ? st[sp - 1] : f3(0.f, 0.f, 0.f);
+}
+
 // Orthonormal frame around axis a as in LambertShader::sample
 // (src/core/LambertShader.cpp:63-65): tmp = a.x > 0.99 ? Y : X, s = |tmp x a|, t = |a x s|.
 __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z) {
@@ -723,7 +769,12 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
         const float3 wo = v_neg(dn);
         // texture colour (ConstantTexture.cpp:22-25; face texels: extension)
         float3 col = f3(s.colour[0], s.colour[1], s.colour[2]);
-        if (s.texture == TEXTURE_FACE && sc.texel_res > 0) {
+        if (s.texture == TEXTURE_TREE && sc.tex_ops) {
+          const int o = __ldg(&sc.tri_orig[k]);
+          const float* uv = sc.tri_uv + 6 * (size_t)o;
+          col = texture_eval(sc, s.tex_prog, s.tex_len, uv_interp(uv[0], uv[2], uv[4], h.y, h.z),
+                             uv_interp(uv[1], uv[3], uv[5], h.y, h.z));
+        } else if (s.texture == TEXTURE_FACE && sc.texel_res > 0) {
           const int res = sc.texel_res;
           const int ti = min(res - 1, max(0, (int)(h.y * (float)res)));
           const int tj = min(res - 1, max(0, (int)(h.z * (float)res)));
@@ -875,6 +926,127 @@ __global__ void __launch_bounds__(BLOCK) k_trace_shadow(const SceneRec* __restri
   const bool blocked = scene_trace<WIDE, true>(b, f3(o), f3(d), MSC_TNEAR, o.w, &h, &ovf);
   if (ovf) atomicOr(err, ovf_bits(ovf));
   if (!blocked) add_rgb(&sample_rgb[__float_as_int(d.w)], f3(c));
+}
+
+// Persistent traversal with per-lane ray refill (8-wide BVH only): every lane
+// holds one ray; when at least kRefill lanes of a warp are idle, the warp
+// takes that many new rays from `counter` in one atomic.
+constexpr int kRefill = 8;
+constexpr int kPersistBlock = 128;
+
+template <bool MULTI>
+__global__ void __launch_bounds__(kPersistBlock) k_trace_closest_pt(const SceneRec* __restrict__ scenes,
+                                                                    BvhRef scene0, const float4* __restrict__ o,
+                                                                    const float4* __restrict__ d, int n_max,
+                                                                    const int* __restrict__ n_dev,
+                                                                    float4* __restrict__ hits, int* err,
+                                                                    int* counter) {
+  const int n = dev_count(n_max, n_dev);
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  Trav8 st;
+  TriHit h;
+  uint2 stack[kWideStack];
+  BvhRef b = scene0;
+  int ray = -1, sc = 0, ovf = 0;
+  bool exhausted = false;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, ray < 0);
+    if (!exhausted && __popc(idle) >= kRefill) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(counter, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      exhausted = base + __popc(idle) >= n;
+      if (ray < 0) {
+        const int my = base + __popc(idle & lt);
+        if (my < n) {
+          ray = my;
+          const float4 ro = o[my], rd = d[my];
+          sc = MULTI ? info_scene(__float_as_int(rd.w)) : 0;
+          b = MULTI ? bvh_of(scenes[sc], true) : scene0;
+          trav8_init(st, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR);
+          h.t = MSC_TFAR; h.u = 0.f; h.v = 0.f; h.tri = -1;
+          ovf = 0;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, ray >= 0) == 0u) {
+      if (exhausted) break;
+      continue;  // all idle and more rays left: refill on the next turn
+    }
+    if (ray >= 0 &&
+        trav8_step<false>(st, stack, (const uint4*)b.nodes, b.tris, b.num_nodes, b.num_tris, &h, &ovf)) {
+      if (scenes[sc].num_spheres > 0) trace_spheres(scenes[sc], st.o, st.d, &h);
+      if (ovf) atomicOr(err, ovf_bits(ovf));
+      hits[ray] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+      ray = -1;
+    }
+  }
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(kPersistBlock) k_trace_shadow_pt(const SceneRec* __restrict__ scenes,
+                                                                   BvhRef scene0, ShadowBuf sh,
+                                                                   const int* __restrict__ count, float4* sample_rgb,
+                                                                   int* err, unsigned long long* shadow_total,
+                                                                   int* counter) {
+  const int n = *count;
+  if (shadow_total && blockIdx.x == 0 && threadIdx.x == 0) *shadow_total += (unsigned long long)n;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  Trav8 st;
+  TriHit h;
+  uint2 stack[kWideStack];
+  BvhRef b = scene0;
+  int ray = -1, ovf = 0;
+  float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
+  int target = 0;
+  bool exhausted = false;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xffffffffu, ray < 0);
+    if (!exhausted && __popc(idle) >= kRefill) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(counter, __popc(idle));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      exhausted = base + __popc(idle) >= n;
+      if (ray < 0) {
+        const int my = base + __popc(idle & lt);
+        if (my < n) {
+          ray = my;
+          const float4 so = sh.o[my], sd = sh.d[my];
+          col = sh.c[my];
+          target = __float_as_int(sd.w);
+          b = MULTI ? bvh_of(scenes[__float_as_int(col.w)], true) : scene0;
+          trav8_init(st, f3(so), f3(sd), MSC_TNEAR, so.w);
+          ovf = 0;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, ray >= 0) == 0u) {
+      if (exhausted) break;
+      continue;
+    }
+    if (ray >= 0 &&
+        trav8_step<true>(st, stack, (const uint4*)b.nodes, b.tris, b.num_nodes, b.num_tris, &h, &ovf)) {
+      if (ovf) atomicOr(err, ovf_bits(ovf));
+      if (!st.found) add_rgb(&sample_rgb[target], f3(col));
+      ray = -1;
+    }
+  }
+}
+
+// Resident blocks of a persistent kernel on this device (cached per kernel).
+template <class K>
+int persistent_grid(K kernel) {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistBlock, 0);
+    grid = std::max(1, sms * std::max(1, per_sm));
+  }
+  return grid;
 }
 
 template <bool WIDE>
@@ -1032,12 +1204,30 @@ int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const u
   } while (0)
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
-                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev, int block) {
+                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev, int block,
+                         int* counter) {
   if (n <= 0) return 0;
   const bool wide = scene0.wnodes != nullptr;
   const BvhRef b0 = bvh_of(scene0, wide);
+  if (counter && wide) {
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    if (num_scenes > 1)
+      k_trace_closest_pt<true><<<persistent_grid(k_trace_closest_pt<true>), kPersistBlock, 0, s>>>(
+          scenes, b0, o, d, n, n_dev, hits, err, counter);
+    else
+      k_trace_closest_pt<false><<<persistent_grid(k_trace_closest_pt<false>), kPersistBlock, 0, s>>>(
+          scenes, b0, o, d, n, n_dev, hits, err, counter);
+    return 1;
+  }
   MSC_TRACE_DISPATCH(k_trace_closest, block, wide, num_scenes > 1, n, s, scenes, b0, o, d, n, n_dev, hits, err);
   return 1;
+}
+
+void persistent_grids_init() {
+  persistent_grid(k_trace_closest_pt<true>);
+  persistent_grid(k_trace_closest_pt<false>);
+  persistent_grid(k_trace_shadow_pt<true>);
+  persistent_grid(k_trace_shadow_pt<false>);
 }
 
 int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
@@ -1079,10 +1269,20 @@ int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const Ra
 
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
                         const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
-                        unsigned long long* shadow_total, int block) {
+                        unsigned long long* shadow_total, int block, int* counter) {
   if (max_n <= 0) return 0;
   const bool wide = scene0.wnodes != nullptr;
   const BvhRef b0 = bvh_of(scene0, wide);
+  if (counter && wide) {
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    if (num_scenes > 1)
+      k_trace_shadow_pt<true><<<persistent_grid(k_trace_shadow_pt<true>), kPersistBlock, 0, s>>>(
+          scenes, b0, sh, sh_count, sample_rgb, err, shadow_total, counter);
+    else
+      k_trace_shadow_pt<false><<<persistent_grid(k_trace_shadow_pt<false>), kPersistBlock, 0, s>>>(
+          scenes, b0, sh, sh_count, sample_rgb, err, shadow_total, counter);
+    return 1;
+  }
   MSC_TRACE_DISPATCH(k_trace_shadow, block, wide, num_scenes > 1, max_n, s, scenes, b0, sh, sh_count, sample_rgb,
                      err, shadow_total);
   return 1;

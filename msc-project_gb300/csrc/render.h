@@ -61,7 +61,19 @@ struct SceneRec {        // one resident scene
   int num_spheres;
   int texel_res;         // face texels per side (0: none)
   const unsigned short* texels;  // FP16 bits, [face][j][i][rgb], face = original triangle index
+  // image textures (Standard / Layered): post-order programs of (op, node),
+  // op 0 constant, 1 image, 2 layer; images as (first texel, width, height)
+  const TexNode* tex_nodes;
+  const int2* tex_ops;
+  const int4* tex_images;
+  const float4* tex_texels;
+  const float* tri_uv;   // 6 per original triangle: uv of v0, v1, v2
 };
+
+// Texture coordinate of a hit (PolygonObject::texture, src/core/PolygonObject.cpp:45-63).
+__host__ __device__ __forceinline__ float uv_interp(float a0, float a1, float a2, float s, float t) {
+  return (((1.f - s) - t) * a0 + s * a1) + t * a2;
+}
 
 // A closest hit on sphere light s is recorded as triangle -2 - s.
 __host__ __device__ __forceinline__ int sphere_hit_code(int s) { return -2 - s; }
@@ -186,7 +198,7 @@ int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const u
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
                          const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev = nullptr,
-                         int block = 128);
+                         int block = 128, int* counter = nullptr);
 int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
                     cudaStream_t s, const int* n_dev = nullptr);
 // The 64-bit hit key of one scene (shader id 12 b, face 23 b, quantised u 15 b, v 14 b; misses and
@@ -203,7 +215,11 @@ int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const Ra
 // shadow_total (optional): the batch's shadow count is added to it.
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
                         const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
-                        unsigned long long* shadow_total = nullptr, int block = 128);
+                        unsigned long long* shadow_total = nullptr, int block = 128, int* counter = nullptr);
+// Sizes the persistent traversal grids (call before any stream capture).
+void persistent_grids_init();
+// counter (optional, 8-wide BVH only): a device int for the persistent
+// traversal with per-lane ray refill; null selects one thread per ray.
 // Occlusion for explicit rays of scene 0 (stage test): occluded[i] = 1 if blocked in (tnear, tmax).
 int launch_occluded(const SceneRec& scene, const float4* o, const float4* d, int n, int* occluded, int* err,
                     cudaStream_t s);

@@ -561,9 +561,58 @@ struct Ctx {
   bool fail(const std::string& m) { *err = m; return false; }
 };
 
-bool decode_texture(const YNode* n, ShaderRec* sh, FaceTexels* ft, Ctx& c) {
+// One texture node (Constant / Standard / Layered, recursively), appended to
+// the scene's node table; returns its index or -1 after c.fail.
+int decode_tex_node(const YNode* n, SceneDesc* S, const std::string& dir, Ctx& c, int depth) {
+  if (depth > 16) { c.fail("texture layers nest deeper than 16"); return -1; }
+  std::string ty = as_str(n ? n->get("type") : nullptr);
+  TexNode t;
+  memset(&t, 0, sizeof(t));
+  t.image = t.upper = t.lower = t.mask = -1;
+  if (ty == "Constant") {  // ConstantTexture.h:74-85
+    t.type = TEXNODE_CONSTANT;
+    if (n->size() != 2 || !as_vec(n->get("colour"), 3, t.colour)) { c.fail("bad Constant texture"); return -1; }
+  } else if (ty == "Standard") {  // StandardTexture.h:69-81: the path is relative to the scene's folder
+    t.type = TEXNODE_STANDARD;
+    std::string rel = as_str(n->get("string"));
+    if (n->size() != 2 || rel.empty()) { c.fail("bad Standard texture (needs string)"); return -1; }
+    const std::string path = dir + "/" + rel;
+    int found = -1;
+    for (size_t i = 0; i < S->image_paths.size(); ++i)
+      if (S->image_paths[i] == path) found = (int)i;
+    if (found < 0) {
+      TexImage img;
+      if (!image_load(path, &img, c.err)) return -1;
+      S->images.push_back(std::move(img));
+      S->image_paths.push_back(path);
+      found = (int)S->images.size() - 1;
+    }
+    t.image = found;
+  } else if (ty == "Layered") {  // LayeredTexture.h:101-178
+    t.type = TEXNODE_LAYERED;
+    if (n->size() != 4) { c.fail("bad Layered texture (needs upper, lower, mask)"); return -1; }
+    const int u = decode_tex_node(n->get("upper"), S, dir, c, depth + 1);
+    if (u < 0) return -1;
+    const int l = decode_tex_node(n->get("lower"), S, dir, c, depth + 1);
+    if (l < 0) return -1;
+    const int m = decode_tex_node(n->get("mask"), S, dir, c, depth + 1);
+    if (m < 0) return -1;
+    t.upper = u;
+    t.lower = l;
+    t.mask = m;
+  } else {
+    c.fail("unknown texture type '" + ty + "'");
+    return -1;
+  }
+  S->tex_nodes.push_back(t);
+  return (int)S->tex_nodes.size() - 1;
+}
+
+bool decode_texture(const YNode* n, ShaderRec* sh, SceneDesc* S, const std::string& dir, Ctx& c) {
+  FaceTexels* ft = &S->texels;
   std::string ty = as_str(n ? n->get("type") : nullptr);
   sh->texture = TEXTURE_CONSTANT;
+  sh->tex_root = -1;
   if (ty == "Constant") {  // include/core/ConstantTexture.h:74-85
     if (n->size() != 2 || !as_vec(n->get("colour"), 3, sh->colour)) return c.fail("bad Constant texture");
     return true;
@@ -580,12 +629,77 @@ bool decode_texture(const YNode* n, ShaderRec* sh, FaceTexels* ft, Ctx& c) {
     sh->texture = TEXTURE_FACE;
     return true;
   }
-  if (ty == "Standard" || ty == "Layered")
-    return c.fail("texture type '" + ty + "' needs an image reader that this build does not have yet");
+  if (ty == "Standard" || ty == "Layered") {
+    const int root = decode_tex_node(n, S, dir, c, 0);
+    if (root < 0) return false;
+    sh->texture = TEXTURE_TREE;
+    sh->tex_root = root;
+    return true;
+  }
   return c.fail("unknown texture type '" + ty + "'");
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------- images
+// PFM: "PF" (RGB) or "Pf" (grey), width height, scale (< 0: little endian),
+// rows bottom first.  PPM: "P6", width height, maxval (< 256: 8 bit, else 16
+// bit big endian), rows top first, values / maxval.  Both end up top first.
+bool image_load(const std::string& path, TexImage* out, std::string* err) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) { *err = "cannot open texture image [" + path + "]"; return false; }
+  std::string data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  size_t p = 0;
+  auto token = [&]() {
+    while (p < data.size()) {
+      if (data[p] == '#') { while (p < data.size() && data[p] != '\n') ++p; }
+      else if (isspace((unsigned char)data[p])) ++p;
+      else break;
+    }
+    size_t b = p;
+    while (p < data.size() && !isspace((unsigned char)data[p])) ++p;
+    return data.substr(b, p - b);
+  };
+  const std::string magic = token();
+  const long w = atol(token().c_str()), h = atol(token().c_str());
+  const std::string third = token();
+  if (p < data.size()) ++p;  // the single whitespace before the raster
+  if (w <= 0 || h <= 0 || w > 65536 || h > 65536) { *err = "bad image size in [" + path + "]"; return false; }
+  out->width = (int)w;
+  out->height = (int)h;
+  out->rgb.assign((size_t)w * h * 3, 0.f);
+  const unsigned char* r = (const unsigned char*)data.data() + p;
+  const size_t left = data.size() - p;
+  if (magic == "PF" || magic == "Pf") {
+    const int ch = magic == "PF" ? 3 : 1;
+    const bool little = atof(third.c_str()) < 0.0;
+    if (left < (size_t)w * h * ch * 4) { *err = "truncated PFM [" + path + "]"; return false; }
+    for (long y = 0; y < h; ++y)
+      for (long x = 0; x < w; ++x)
+        for (int k = 0; k < 3; ++k) {
+          const unsigned char* q = r + 4 * (((size_t)y * w + x) * ch + (ch == 3 ? k : 0));
+          uint32_t u = little ? (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24)
+                              : (uint32_t)q[3] | ((uint32_t)q[2] << 8) | ((uint32_t)q[1] << 16) | ((uint32_t)q[0] << 24);
+          float v;
+          memcpy(&v, &u, 4);
+          out->rgb[(((size_t)(h - 1 - y)) * w + x) * 3 + k] = v;  // bottom row first in the file
+        }
+    return true;
+  }
+  if (magic == "P6") {
+    const long maxv = atol(third.c_str());
+    if (maxv <= 0 || maxv > 65535) { *err = "bad PPM maxval in [" + path + "]"; return false; }
+    const int bps = maxv < 256 ? 1 : 2;
+    if (left < (size_t)w * h * 3 * bps) { *err = "truncated PPM [" + path + "]"; return false; }
+    for (size_t i = 0; i < (size_t)w * h * 3; ++i) {
+      const uint32_t v = bps == 1 ? r[i] : ((uint32_t)r[2 * i] << 8) | r[2 * i + 1];
+      out->rgb[i] = (float)v / (float)maxv;
+    }
+    return true;
+  }
+  *err = "texture image [" + path + "] is not PFM or binary PPM";
+  return false;
+}
 
 bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) {
   std::ifstream f(yaml_path, std::ios::binary);
@@ -761,13 +875,13 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
       if (ty == "Lambert") {  // LambertShader.h:140-174
         sh.type = SHADER_LAMBERT;
         if (n.size() != 3 || !as_float(n.get("reflectance"), &sh.reflectance)) return c.fail("bad Lambert shader");
-        if (!decode_texture(n.get("texture"), &sh, &S.texels, c)) return false;
+        if (!decode_texture(n.get("texture"), &sh, &S, dir, c)) return false;
       } else if (ty == "Phong") {  // extension: modified Phong lobe
         sh.type = SHADER_PHONG;
         if (n.size() != 4 || !as_float(n.get("reflectance"), &sh.reflectance) ||
             !as_float(n.get("exponent"), &sh.exponent) || sh.exponent < 0.f)
           return c.fail("bad Phong shader");
-        if (!decode_texture(n.get("texture"), &sh, &S.texels, c)) return false;
+        if (!decode_texture(n.get("texture"), &sh, &S, dir, c)) return false;
       } else {
         continue;
       }

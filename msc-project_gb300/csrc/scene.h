@@ -49,7 +49,25 @@ double obj_parse_number(const char* s, const char* end);  // tinyobj tryParseDou
 
 // ------------------------------------------------------------------ device tables
 enum ShaderType : int { SHADER_LAMBERT = 0, SHADER_NULL = 1, SHADER_PHONG = 2 };
-enum TextureType : int { TEXTURE_CONSTANT = 0, TEXTURE_FACE = 1 };
+enum TextureType : int { TEXTURE_CONSTANT = 0, TEXTURE_FACE = 1, TEXTURE_TREE = 2 };
+enum TexNodeType : int { TEXNODE_CONSTANT = 0, TEXNODE_STANDARD = 1, TEXNODE_LAYERED = 2 };
+
+// A node of a texture tree (ConstantTexture, StandardTexture, LayeredTexture;
+// include/core/*Texture.h): Layered = upper * mask + lower * (1 - mask).
+struct TexNode {
+  int type;          // TexNodeType
+  int image;         // Standard: index into the scene's images
+  int upper, lower, mask;  // Layered: node indices
+  float colour[3];   // Constant
+};
+
+// An RGB image, rows top first (image row 0 is texture coordinate t = 0).
+struct TexImage {
+  int width = 0, height = 0;
+  std::vector<float> rgb;  // 3 per texel
+};
+// Reads PFM (PF/Pf), PPM (P6, 8 or 16 bit) images.
+bool image_load(const std::string& path, TexImage* out, std::string* err);
 enum LightType : int { LIGHT_QUAD = 0, LIGHT_SPHERE = 1 };
 enum CameraType : int { CAMERA_PINHOLE = 0, CAMERA_THINLENS = 1 };
 enum SamplerType : int { SAMPLER_STRATIFIED = 0, SAMPLER_INDEPENDENT = 1, SAMPLER_GRID = 2 };
@@ -62,6 +80,10 @@ struct ShaderRec {
   float exponent;    // Phong exponent (extension)
   float colour[3];   // ConstantTexture colour (ConstantTexture.cpp:22-25); tint of face texels
   int texture;       // TextureType
+  int tex_root;      // TEXTURE_TREE: root node of the shader's texture tree
+  int tex_prog;      // TEXTURE_TREE: first op of its post-order program (device)
+  int tex_len;       // and the number of ops
+  int pad;
 };
 
 // Per-face texels (extension): every triangle of the scene owns res x res RGB
@@ -141,6 +163,9 @@ struct SceneDesc {
   std::vector<LightRec> lights;
   std::vector<int> sphere_lights;    // light index of each sphere light, in light order
   FaceTexels texels;
+  std::vector<TexNode> tex_nodes;    // texture trees of Standard / Layered textures
+  std::vector<TexImage> images;
+  std::vector<std::string> image_paths;
   // flattened triangles in geomID order, positions after the object transform
   std::vector<float> tri_v;          // 9 per triangle: v0, v1, v2
   std::vector<float> tri_uv;         // 6 per triangle: uv0, uv1, uv2 (0 when absent)

@@ -286,4 +286,134 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
   }
 }
 
+// ------------------------------------------------- stepwise 8-wide traversal
+// The same traversal as bvh8_trace, one step at a time: a step tests one
+// triangle, visits one node, or pops one node group.  A persistent kernel
+// keeps one ray per lane and, when a lane's ray ends, hands the lane a new ray
+// (Aila and Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
+// HPG 2009), so warps stay full instead of waiting for their slowest ray.
+// The per-ray order of steps is that of bvh8_trace, so hits are identical.
+struct Trav8 {
+  float3 o, d, id;
+  float tmin, tmax;
+  uint32_t oct;
+  uint32_t g_base, g_imask, g_hits, t_base, t_mask;
+  int sp, steps;
+  bool found;
+};
+
+__device__ __forceinline__ void trav8_init(Trav8& s, float3 o, float3 d, float tmin, float tmax) {
+  s.o = o;
+  s.d = d;
+  s.id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  s.tmin = tmin;
+  s.tmax = tmax;
+  s.oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+  s.g_base = 0;
+  s.g_imask = 1u;
+  s.g_hits = 1u << s.oct;
+  s.t_base = 0;
+  s.t_mask = 0;
+  s.sp = 0;
+  s.steps = 0;
+  s.found = false;
+}
+
+// One step; returns true when the ray is finished (*overflow set on errors).
+template <bool ANY>
+__device__ __forceinline__ bool trav8_step(Trav8& s, uint2* stack, const uint4* __restrict__ wn,
+                                           const float4* __restrict__ tris, int num_nodes, int num_tris, TriHit* hit,
+                                           int* overflow) {
+  if (s.t_mask != 0u) {
+    const int k = (int)s.t_base + __ffs(s.t_mask) - 1;
+    s.t_mask &= s.t_mask - 1u;
+    if (k >= num_tris) {
+      *overflow = 3;
+      return true;
+    }
+    const float4 a = __ldg(&tris[3 * k + 0]);
+    const float4 b = __ldg(&tris[3 * k + 1]);
+    const float4 c = __ldg(&tris[3 * k + 2]);
+    if (ANY && __float_as_int(b.w) != 0) return false;
+    float t, u, v;
+    if (tri_intersect(s.o, s.d, f3(a), f3(b), f3(c), s.tmin, s.tmax, &t, &u, &v)) {
+      s.found = true;
+      if (ANY) return true;
+      s.tmax = t;
+      hit->t = t;
+      hit->u = u;
+      hit->v = v;
+      hit->tri = k;
+    }
+    return false;
+  }
+  if (s.g_hits != 0u) {
+    const uint32_t j = (uint32_t)(__ffs(s.g_hits) - 1);
+    s.g_hits &= s.g_hits - 1u;
+    const uint32_t slot = j ^ s.oct;
+    const int node = (int)(s.g_base + __popc(s.g_imask & ((1u << slot) - 1u)));
+    if (s.g_hits != 0u) {
+      if (s.sp < kWideStack) stack[s.sp++] = make_uint2(s.g_base, (s.g_imask << 8) | s.g_hits);
+      else *overflow = 1;
+    }
+    if (++s.steps > kTraceStepCap) {
+      *overflow = 2;
+      return true;
+    }
+    if (node >= num_nodes) {
+      *overflow = 3;
+      return true;
+    }
+    const uint4 A = __ldg(&wn[5 * node + 0]);
+    const uint4 B = __ldg(&wn[5 * node + 1]);
+    const uint4 Q0 = __ldg(&wn[5 * node + 2]);
+    const uint4 Q1 = __ldg(&wn[5 * node + 3]);
+    const uint4 Q2 = __ldg(&wn[5 * node + 4]);
+    const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
+    const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
+    const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
+    const uint32_t imask = A.w >> 24;
+    const float3 id = s.id, o = s.o;
+    const float ax = sx * id.x, ay = sy * id.y, az = sz * id.z;
+    const float bx = (__uint_as_float(A.x) - o.x) * id.x;
+    const float by = (__uint_as_float(A.y) - o.y) * id.y;
+    const float bz = (__uint_as_float(A.z) - o.z) * id.z;
+    const bool nx = id.x < 0.f, ny = id.y < 0.f, nz = id.z < 0.f;
+    const uint32_t enx0 = nx ? Q1.z : Q0.x, enx1 = nx ? Q1.w : Q0.y, exx0 = nx ? Q0.x : Q1.z, exx1 = nx ? Q0.y : Q1.w;
+    const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
+    const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
+    const float widen = 1.0000004f;
+    uint32_t nh = 0u, tm = 0u;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t m = byte_of(B.z, B.w, q);
+      const bool inner = ((imask >> q) & 1u) != 0u;
+      const float tnx = fmaf(byte_float(enx0, enx1, q), ax, bx);
+      const float tny = fmaf(byte_float(eny0, eny1, q), ay, by);
+      const float tnz = fmaf(byte_float(enz0, enz1, q), az, bz);
+      const float tfx = fmaf(byte_float(exx0, exx1, q), ax, bx);
+      const float tfy = fmaf(byte_float(exy0, exy1, q), ay, by);
+      const float tfz = fmaf(byte_float(exz0, exz1, q), az, bz);
+      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
+      const float tf = fminf(fminf(tfx, tfy), fminf(tfz, s.tmax)) * widen;
+      if (tn <= tf) {
+        if (inner) nh |= 1u << ((uint32_t)q ^ s.oct);
+        else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+      }
+    }
+    s.g_base = B.x;
+    s.g_imask = imask;
+    s.g_hits = nh;
+    s.t_base = B.y;
+    s.t_mask = tm;
+    return false;
+  }
+  if (s.sp == 0) return true;
+  const uint2 e = stack[--s.sp];
+  s.g_base = e.x;
+  s.g_imask = e.y >> 8;
+  s.g_hits = e.y & 0xffu;
+  return false;
+}
+
 }  // namespace mscg

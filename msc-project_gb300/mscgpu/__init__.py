@@ -207,8 +207,8 @@ class Pathtracer:
         _check(self._lib.msc_get_tuning(self._h, C.byref(t)), self._h)
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), 0, 0)
         _check(self._lib.msc_set_tuning(self._h, C.byref(t)), self._h)
 
     def stats(self):
@@ -344,12 +344,12 @@ def scene_load_host(yaml_path):
 
 class _Tuning(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("bins", C.c_int), ("tuning", C.c_int), ("samples", C.c_int)]
+                ("bins", C.c_int), ("persistent", C.c_int), ("tuning", C.c_int), ("samples", C.c_int)]
 
 
 class _TuneSample(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("bins", C.c_int), ("mrays_per_s", C.c_double)]
+                ("bins", C.c_int), ("persistent", C.c_int), ("mrays_per_s", C.c_double)]
 
 
 def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
@@ -440,8 +440,8 @@ class Batch:
         self._check(self._lib.msc_batch_get_tuning(self._b, C.byref(t)))
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), 0, 0)
         self._check(self._lib.msc_batch_set_tuning(self._b, C.byref(t)))
 
     def tune_log(self):

@@ -464,7 +464,10 @@ void point(const Aff& a, const float p[3], float o[3]) {
 }
 
 enum { LAMBERT = 0, NULLSH = 1, PHONG = 2 };
-struct Shader { int type = LAMBERT; int light = -1; float refl = 1.f, ex = 0.f; float col[3] = {0, 0, 0}; int tex = 0; };
+struct Shader { int type = LAMBERT; int light = -1; float refl = 1.f, ex = 0.f; float col[3] = {0, 0, 0}; int tex = 0; int tex_root = -1; };
+// Texture trees (ConstantTexture / StandardTexture / LayeredTexture, include/core/*Texture.h).
+struct TNode { int type = 0; int image = -1, upper = -1, lower = -1, mask = -1; float col[3] = {0, 0, 0}; };
+struct OImage { int w = 0, h = 0; std::vector<float> rgb; };  // rows top first
 struct Geom { int shader = 0, first = 0, count = 0, light = -1; };
 struct Light { int type = 0; float inten = 100.f; float scale[2] = {1, 1}; Aff m; float n[3]; float c[3]; float rad = 0.f; };
 
@@ -490,6 +493,10 @@ struct oracle_scene {
   std::vector<int> sphere_lights;  // light index of each sphere light (extension)
   int texel_res = 0;           // per-face texels (extension)
   uint32_t texel_seed = 0;
+  std::vector<TNode> tnodes;   // image textures
+  std::vector<OImage> images;
+  std::vector<std::string> image_paths;
+  std::vector<float> tuv;      // 6 per triangle: texcoords of v0, v1, v2
   std::vector<float> tv;       // 9 per triangle
   std::vector<int> tgeom;
   std::vector<uint8_t> tlight;
@@ -499,6 +506,121 @@ struct oracle_scene {
 };
 
 namespace orc {
+
+// PFM ("PF"/"Pf", rows bottom first, scale < 0 little endian) and binary PPM
+// ("P6", maxval < 256: bytes, else 16-bit big endian), both stored top first.
+bool read_image(const std::string& path, OImage* im) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  std::string d((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  size_t p = 0;
+  auto tok = [&]() {
+    while (p < d.size() && (isspace((unsigned char)d[p]) || d[p] == '#')) {
+      if (d[p] == '#') while (p < d.size() && d[p] != '\n') ++p;
+      else ++p;
+    }
+    size_t b = p;
+    while (p < d.size() && !isspace((unsigned char)d[p])) ++p;
+    return d.substr(b, p - b);
+  };
+  std::string mg = tok();
+  long w = atol(tok().c_str()), h = atol(tok().c_str());
+  std::string third = tok();
+  ++p;
+  if (w <= 0 || h <= 0) return false;
+  im->w = (int)w; im->h = (int)h;
+  im->rgb.assign((size_t)w * h * 3, 0.f);
+  const unsigned char* r = (const unsigned char*)d.data() + p;
+  if (mg == "PF" || mg == "Pf") {
+    int ch = mg == "PF" ? 3 : 1;
+    bool le = atof(third.c_str()) < 0;
+    if (d.size() - p < (size_t)w * h * ch * 4) return false;
+    for (long y = 0; y < h; ++y)
+      for (long x = 0; x < w; ++x)
+        for (int k = 0; k < 3; ++k) {
+          const unsigned char* q = r + 4 * ((y * w + x) * ch + (ch == 3 ? k : 0));
+          uint32_t u = le ? (q[0] | (q[1] << 8) | (q[2] << 16) | ((uint32_t)q[3] << 24))
+                          : (q[3] | (q[2] << 8) | (q[1] << 16) | ((uint32_t)q[0] << 24));
+          float v; memcpy(&v, &u, 4);
+          im->rgb[((h - 1 - y) * w + x) * 3 + k] = v;
+        }
+    return true;
+  }
+  if (mg == "P6") {
+    long mv = atol(third.c_str());
+    int bps = mv < 256 ? 1 : 2;
+    if (mv <= 0 || d.size() - p < (size_t)w * h * 3 * bps) return false;
+    for (size_t i = 0; i < (size_t)w * h * 3; ++i) {
+      uint32_t v = bps == 1 ? r[i] : ((uint32_t)r[2 * i] << 8) | r[2 * i + 1];
+      im->rgb[i] = (float)v / (float)mv;
+    }
+    return true;
+  }
+  return false;
+}
+
+int tex_node(const Node* n, oracle_scene* S, const std::string& dir) {
+  if (!n) return -1;
+  std::string ty = str(n->get("type"));
+  TNode t;
+  if (ty == "Constant") {
+    if (!vecn(n->get("colour"), 3, t.col)) return -1;
+  } else if (ty == "Standard") {
+    t.type = 1;
+    std::string path = dir + "/" + str(n->get("string"));
+    for (size_t i = 0; i < S->image_paths.size(); ++i) if (S->image_paths[i] == path) t.image = (int)i;
+    if (t.image < 0) {
+      OImage im;
+      if (!read_image(path, &im)) return -1;
+      S->images.push_back(im);
+      S->image_paths.push_back(path);
+      t.image = (int)S->images.size() - 1;
+    }
+  } else if (ty == "Layered") {
+    t.type = 2;
+    t.upper = tex_node(n->get("upper"), S, dir);
+    t.lower = tex_node(n->get("lower"), S, dir);
+    t.mask = tex_node(n->get("mask"), S, dir);
+    if (t.upper < 0 || t.lower < 0 || t.mask < 0) return -1;
+  } else {
+    return -1;
+  }
+  S->tnodes.push_back(t);
+  return (int)S->tnodes.size() - 1;
+}
+
+// Periodic bilinear lookup between texel centres, t = 0 on the top row (the
+// stand-in for OpenImageIO's texture() with periodic wrap, StandardTexture.cpp:18-34).
+void image_lookup(const OImage& im, float s, float t, float out[3]) {
+  const int w = im.w, h = im.h;
+  s = s - std::floor(s);
+  t = t - std::floor(t);
+  const float x = s * (float)w - 0.5f, y = t * (float)h - 0.5f;
+  const float fx0 = std::floor(x), fy0 = std::floor(y);
+  const float fx = x - fx0, fy = y - fy0;
+  int x0 = (int)fx0, y0 = (int)fy0;
+  x0 = x0 < 0 ? x0 + w : (x0 >= w ? x0 - w : x0);
+  y0 = y0 < 0 ? y0 + h : (y0 >= h ? y0 - h : y0);
+  const int x1 = x0 + 1 == w ? 0 : x0 + 1, y1 = y0 + 1 == h ? 0 : y0 + 1;
+  const float gx = 1.f - fx, gy = 1.f - fy;
+  for (int k = 0; k < 3; ++k) {
+    const float c00 = im.rgb[((size_t)y0 * w + x0) * 3 + k], c10 = im.rgb[((size_t)y0 * w + x1) * 3 + k];
+    const float c01 = im.rgb[((size_t)y1 * w + x0) * 3 + k], c11 = im.rgb[((size_t)y1 * w + x1) * 3 + k];
+    out[k] = (c00 * gx + c10 * fx) * gy + (c01 * gx + c11 * fx) * fy;
+  }
+}
+
+// LayeredTexture.cpp:14-37: upper * mask + lower * (1 - mask).
+void tex_eval(const oracle_scene* S, int node, float s, float t, float out[3]) {
+  const TNode& n = S->tnodes[node];
+  if (n.type == 0) { out[0] = n.col[0]; out[1] = n.col[1]; out[2] = n.col[2]; return; }
+  if (n.type == 1) { image_lookup(S->images[n.image], s, t, out); return; }
+  float u[3], l[3], m[3];
+  tex_eval(S, n.upper, s, t, u);
+  tex_eval(S, n.lower, s, t, l);
+  tex_eval(S, n.mask, s, t, m);
+  for (int k = 0; k < 3; ++k) out[k] = u[k] * m[k] + l[k] * (1.f - m[k]);
+}
 
 bool load(const std::string& path, oracle_scene* S, std::string* err) {
   std::ifstream f(path, std::ios::binary);
@@ -561,10 +683,16 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
     S->spp = S->base * S->base;
     S->gx = S->gy = S->base;
   }
-  auto add_tris = [&](const std::vector<float>& p, const std::vector<uint32_t>& idx, int g, bool light) {
+  auto add_tris = [&](const std::vector<float>& p, const std::vector<uint32_t>& idx, int g, bool light,
+                      const std::vector<float>& uv) {
     for (size_t t = 0; t + 2 < idx.size(); t += 3) {
-      for (int k = 0; k < 3; ++k)
+      for (int k = 0; k < 3; ++k) {
         for (int a = 0; a < 3; ++a) S->tv.push_back(p[3 * idx[t + k] + a]);
+        const size_t vi = idx[t + k];
+        const bool has = 2 * vi + 1 < uv.size();
+        S->tuv.push_back(has ? uv[2 * vi] : 0.f);
+        S->tuv.push_back(has ? uv[2 * vi + 1] : 0.f);
+      }
       S->tgeom.push_back(g);
       S->tlight.push_back(light ? 1 : 0);
     }
@@ -586,7 +714,7 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
       g.first = (int)S->tgeom.size();
       g.count = (int)(o.idx.size() / 3);
       S->geoms.push_back(g);
-      add_tris(p, o.idx, (int)S->geoms.size() - 1, false);
+      add_tris(p, o.idx, (int)S->geoms.size() - 1, false, o.tex);
     } else if (kv.first == "shader") {
       std::string ty = str(n.get("type"));
       Shader s;
@@ -594,8 +722,15 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
       if (ty == "Lambert" || ty == "Phong") {
         s.type = ty == "Lambert" ? LAMBERT : PHONG;
         const std::string tt = tex ? str(tex->get("type")) : "";
-        if (!num(n.get("reflectance"), &s.refl) || (tt != "Constant" && tt != "FaceTexels") ||
-            !vecn(tex->get("colour"), 3, s.col)) { *err = "shader"; return false; }
+        if (!num(n.get("reflectance"), &s.refl)) { *err = "shader"; return false; }
+        if (tt == "Standard" || tt == "Layered") {
+          s.tex = 2;
+          s.tex_root = tex_node(tex, S, dir);
+          if (s.tex_root < 0) { *err = "texture"; return false; }
+        } else if ((tt != "Constant" && tt != "FaceTexels") || !vecn(tex->get("colour"), 3, s.col)) {
+          *err = "shader";
+          return false;
+        }
         if (tt == "FaceTexels") {  // extension: per-face FP16 texels from a seed
           int res = 0, sd = 0;
           if (!inum(tex->get("resolution"), &res) || !inum(tex->get("seed"), &sd)) { *err = "texture"; return false; }
@@ -648,7 +783,7 @@ bool load(const std::string& path, oracle_scene* S, std::string* err) {
                            {0.f, 0.5f, 0.5f}, {0.f, -0.5f, 0.5f}, {0.f, -0.5f, -0.5f}};
     std::vector<float> p(18);
     for (int i = 0; i < 6; ++i) point(L.m, q[i], &p[3 * i]);
-    add_tris(p, {0, 1, 2, 3, 4, 5}, (int)S->geoms.size() - 1, true);
+    add_tris(p, {0, 1, 2, 3, 4, 5}, (int)S->geoms.size() - 1, true, std::vector<float>());
   }
   for (auto& g : S->geoms)
     if (g.shader < 0 || g.shader >= (int)S->shaders.size()) { *err = "object shader index"; return false; }
@@ -1027,7 +1162,15 @@ void render_path(const oracle_scene* S, uint32_t sid, uint32_t seed, T* rgb, T* 
     const V<T> pos = add(o, mul(dn, t));
     const V<T> wo = neg(dn);
     V<T> colr = mk<T>(sh.col[0], sh.col[1], sh.col[2]);  // ConstantTexture.cpp:22-25
-    if (sh.tex == 1 && S->texel_res > 0) {  // face texels (extension)
+    if (sh.tex == 2) {  // Standard / Layered (PolygonObject.cpp:45-63 texture coordinates)
+      const float* uv = &S->tuv[6 * (size_t)tri];
+      const float fs = (float)hu, ft = (float)hv;
+      const float su = (((1.f - fs) - ft) * uv[0] + fs * uv[2]) + ft * uv[4];
+      const float sv = (((1.f - fs) - ft) * uv[1] + fs * uv[3]) + ft * uv[5];
+      float c3[3];
+      tex_eval(S, sh.tex_root, su, sv, c3);
+      colr = mk<T>(c3[0], c3[1], c3[2]);
+    } else if (sh.tex == 1 && S->texel_res > 0) {  // face texels (extension)
       const int res = S->texel_res;
       const int ti = std::min(res - 1, std::max(0, (int)((float)hu * (float)res)));
       const int tj = std::min(res - 1, std::max(0, (int)((float)hv * (float)res)));
@@ -1380,6 +1523,13 @@ int orc_ray_bin(float x, float y, float z, int nbins) {
         if ((i * m + j) * m + k < (c[0] * m + c[1]) * m + c[2]) ++interior_before;
   (void)n_in;
   return (c[0] * m + c[1]) * m + c[2] - interior_before;
+}
+
+int oracle_image_lookup(const char* path, int n, const float* s, const float* t, float* rgb) {
+  OImage im;
+  if (!read_image(path, &im)) return -1;
+  for (int i = 0; i < n; ++i) image_lookup(im, s[i], t[i], rgb + 3 * i);
+  return 0;
 }
 
 void oracle_ray_bins(const float* dirs, int n, int nbins, int32_t* bins) {

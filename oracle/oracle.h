@@ -64,6 +64,8 @@ void oracle_ray_keys(const float* org, const float* dir, int n, uint32_t* keys);
 void oracle_stable_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
 void oracle_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts);
 void oracle_ray_bins(const float* dirs, int n, int nbins, int32_t* bins);
+// Periodic bilinear lookups of a PFM / PPM image at (s[i], t[i]); -1 if unreadable.
+int oracle_image_lookup(const char* path, int n, const float* s, const float* t, float* rgb);
 void oracle_bin_partition_n(const float* rays, int n, int nbins, int cap, float* out, int32_t* counts);
 void oracle_tent_filter(const float* sample_rgb, const float* sample_xy, int w, int h, int spp, float* pixels);
 

@@ -39,6 +39,7 @@ def lib():
         L.oracle_stable_sort_pairs.argtypes = [U32, U32, I, I]
         L.oracle_bin_partition.argtypes = [F, I, I, F, I32]
         L.oracle_ray_bins.argtypes = [F, I, I, I32]
+        L.oracle_image_lookup.argtypes = [C.c_char_p, I, F, F, F]
         L.oracle_bin_partition_n.argtypes = [F, I, I, I, F, I32]
         L.oracle_tent_filter.argtypes = [F, F, I, I, I, F]
         L.oracle_obj_load.argtypes = [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]
@@ -143,6 +144,17 @@ def stable_sort_pairs(keys, vals, bits=32):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     lib().oracle_stable_sort_pairs(_p(k, C.c_uint32), _p(v, C.c_uint32), k.shape[0], bits)
     return k, v
+
+
+def image_lookup(path, s, t):
+    s = np.ascontiguousarray(s, np.float32)
+    t = np.ascontiguousarray(t, np.float32)
+    out = np.zeros((s.shape[0], 3), np.float32)
+    rc = lib().oracle_image_lookup(os.fsencode(path), s.shape[0], _p(s, C.c_float), _p(t, C.c_float),
+                                   _p(out, C.c_float))
+    if rc != 0:
+        raise ValueError("unreadable image " + path)
+    return out
 
 
 def ray_bins(dirs, nbins):

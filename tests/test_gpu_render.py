@@ -211,3 +211,36 @@ def test_direction_bin_count_does_not_change_the_image(built, box_scene, nbins):
             pt.process()
             imgs.append(pt.image())
     assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
+
+
+def test_image_textures_match_oracle(built, tmp_path):
+    """Standard and (nested) Layered textures from PFM / PPM images."""
+    from texture_scene import make_texture_scene
+    mscgpu, oracle = built
+    y = make_texture_scene(mscgpu, str(tmp_path))
+    with mscgpu.Pathtracer(y) as pt:
+        pt.process()
+        img = pt.image()
+        rgb, _ = pt.samples()
+    ref, wrgb, _, _ = oracle.Scene(y).render(0)
+    same = (rgb.view(np.uint32) == wrgb.view(np.uint32)).all(axis=1)
+    assert same.mean() > 0.99, same.mean()
+    _close(img, ref)
+
+
+@pytest.mark.parametrize("which", ["box", "terrain"])
+def test_persistent_traversal_gives_the_same_image(built, box_scene, scene_dir, which):
+    """Per-lane ray refill changes only the scheduling: every ray's steps and hit are the same."""
+    mscgpu, _ = built
+    y = box_scene if which == "box" else mscgpu.generate_scene(1, 77, str(scene_dir / "terrain_small"), scale=0.05)
+    imgs = []
+    for pers in (False, True):
+        with mscgpu.Pathtracer(y) as pt:
+            e = pt.tuning()["batch_exponent"]
+            pt.set_tuning(batch_exponent=e, trace_block=128, ray_sort=True, hit_sort=False, bins=6, persistent=pers)
+            assert pt.tuning()["persistent"] == int(pers)
+            pt.process()
+            imgs.append(pt.image())
+            st = pt.stats()
+            assert st["closest_queries"] > 0
+    assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
