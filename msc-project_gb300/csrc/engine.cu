@@ -143,7 +143,8 @@ int plain_setup(msc_handle* h) {
   const int e = std::min(d.settings.bin_exponent, 24);
   uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(16ull << e, 1ull << 22);
   gen = std::max<uint64_t>(std::min<uint64_t>(gen, paths), 1);
-  int rc = h->core.init(e, (int)gen, paths, d.ext.wide_bvh != 0);
+  // capacity for twice the scene's batch so the autotuner can also try a larger one
+  int rc = h->core.init(std::min(e + 1, 22), (int)gen, paths, d.ext.wide_bvh != 0);
   if (rc != MSC_OK) {
     h->err = h->core.err;
     return rc;
@@ -152,6 +153,7 @@ int plain_setup(msc_handle* h) {
   h->core.hit_sort = d.ext.hit_sort != 0;
   {
     TuneChoice c = h->core.choice();
+    c.batch_exp = std::max(6, e);  // the scene's bin exponent (Settings.h:16-24) is the starting batch size
     c.bins = d.ext.bins;
     h->core.apply(c);
   }
