@@ -209,7 +209,7 @@ def bench_forms(args):
     gen_s = time.time() - t
     film_cap = 1_800_000_000  # the film pool indexes samples with 31 bits
     t = time.time()
-    b = mscgpu.Batch(batch_exponent=21, film_samples=film_cap)
+    b = mscgpu.Batch(batch_exponent=22, film_samples=film_cap)
     bboxes, tris = [], []
     for y in scenes:
         k = b.add_scene(y)

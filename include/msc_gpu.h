@@ -202,7 +202,7 @@ typedef struct msc_tune_sample {
 } msc_tune_sample;
 /* Starts the online autotuner: the next batches are spread over candidate
    choices (batch size, direction bins, traversal block, the two sorts), each timed
-   over `windows` windows (0: 2), and the fastest is kept.  No reference
+   over `windows` windows (0: 3), and the fastest is kept.  No reference
    counterpart. */
 int msc_batch_autotune(msc_batch* b, int windows);
 int msc_batch_get_tuning(msc_batch* b, msc_tuning* out);

@@ -125,6 +125,11 @@ Core::~Core() {
   if (h_ctr_) cudaFreeHost(h_ctr_);
   for (auto e : tune_ev_)
     if (e) cudaEventDestroy(e);
+  for (int i = 0; i < kGraphBodies; ++i) {
+    if (fork_ev_[i]) cudaEventDestroy(fork_ev_[i]);
+    if (join_ev_[i]) cudaEventDestroy(join_ev_[i]);
+  }
+  if (side_) cudaStreamDestroy(side_);
   for (auto e : event_pool_) cudaEventDestroy(e);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -147,6 +152,11 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
     return MSC_ERR_ARG;
   }
   CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
+  for (int i = 0; i < kGraphBodies; ++i) {
+    CK(cudaEventCreateWithFlags(&fork_ev_[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&join_ev_[i], cudaEventDisableTiming));
+  }
   CK(cudaEventCreate(&tune_ev_[0]));
   CK(cudaEventCreate(&tune_ev_[1]));
   CK(cudaMalloc(&d_scenes_, kMaxScenes * sizeof(SceneRec)));
@@ -169,7 +179,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
                  al256(4) +
                  3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(8 * 4) + al256(sizeof(BatchPlan)) +
-                 sort_scratch_bytes(B) + al256((size_t)B * sizeof(float4)) + 3 * al256((size_t)B * sizeof(float4)) +
+                 sort_scratch_bytes(B) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
   Arena A{arena_, 0};
@@ -204,9 +214,11 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   plan_ = A.take<BatchPlan>(1);
   sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B)), B);
   hits_ = A.take<float4>(B);
-  shadow_.o = A.take<float4>(B);
-  shadow_.d = A.take<float4>(B);
-  shadow_.c = A.take<float4>(B);
+  for (int q = 0; q < 2; ++q) {
+    shadow_[q].o = A.take<float4>(B);
+    shadow_[q].d = A.take<float4>(B);
+    shadow_[q].c = A.take<float4>(B);
+  }
   bins_.tile_counts = A.take<uint32_t>((size_t)(kMaxBins + 1) * part_tiles);
   bins_.max_tiles = part_tiles;
   bins_.count = ctr_->bin_count;
@@ -659,14 +671,15 @@ void Core::drop_graph() {
 
 // One batch body.  Every size is read on the device from the plan, so the
 // same launches serve any batch and can be captured once.
-int Core::enqueue_batch() {
+int Core::enqueue_batch(int index, bool overlap) {
   cudaStream_t st = stream_;
   const SceneRec& s0 = scenes_[0]->rec;
   const int ns = (int)scenes_.size();
   const int B = batch_size_;
   const int* nb = &plan_->nb;
   int* errw = &ctr_->err;
-  int* shc = &ctr_->shadow_count;
+  const int q = index & 1;
+  int* shc = &ctr_->shadow_count[q];
   int scene_bits = 0;
   while ((1 << scene_bits) < ns) ++scene_bits;
   {
@@ -724,15 +737,24 @@ int Core::enqueue_batch() {
     t.done(l + ls);
     order = hperm_;
   }
+  if (overlap && index > 0) CK(cudaStreamWaitEvent(st, join_ev_[index - 1], 0));  // the previous occlusion
   {
     StageClock t(this, MSC_STAGE_SHADE);
-    t.done(launch_shade(d_scenes_, d_jobs_, film_, batch_, hits_, order, B, staging_, shadow_, shc, d_job_done_, st,
-                        nb));
+    CK(cudaMemsetAsync(shc, 0, sizeof(int), st));
+    t.done(launch_shade(d_scenes_, d_jobs_, film_, batch_, hits_, order, B, staging_, shadow_[q], shc, d_job_done_,
+                        st, nb));
   }
   {
     StageClock t(this, MSC_STAGE_SHADOW);
-    t.done(launch_trace_shadow(d_scenes_, ns, s0, shadow_, shc, B, film_.rgb, errw, st, &ctr_->shadow,
+    cudaStream_t ss = st;
+    if (overlap) {
+      CK(cudaEventRecord(fork_ev_[index], st));
+      CK(cudaStreamWaitEvent(side_, fork_ev_[index], 0));
+      ss = side_;
+    }
+    t.done(launch_trace_shadow(d_scenes_, ns, s0, shadow_[q], shc, B, film_.rgb, errw, ss, &ctr_->shadow,
                                trace_block, persistent_trace ? trace_counter_ + 1 : nullptr));
+    if (overlap) CK(cudaEventRecord(join_ev_[index], side_));
   }
   {
     StageClock t(this, MSC_STAGE_BINS);
@@ -744,7 +766,7 @@ int Core::enqueue_batch() {
 int Core::run_batches(int k) {
   if (profiling || !use_graph) {
     for (int i = 0; i < k; ++i) {
-      int rc = enqueue_batch();
+      int rc = enqueue_batch(i, false);
       if (rc != MSC_OK) return rc;
     }
     CK(cudaGetLastError());
@@ -758,7 +780,12 @@ int Core::run_batches(int k) {
     uint64_t stage0[12];
     memcpy(stage0, stats.stage_launches, sizeof(stage0));
     CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_batch();
+    int rc = MSC_OK;
+    for (int i = 0; i < kGraphBodies && rc == MSC_OK; ++i) rc = enqueue_batch(i, true);
+    if (rc == MSC_OK && cudaStreamWaitEvent(stream_, join_ev_[kGraphBodies - 1], 0) != cudaSuccess) {
+      err = "joining the occlusion stream in the batch graph";
+      rc = MSC_ERR_CUDA;
+    }
     cudaError_t ce = cudaStreamEndCapture(stream_, &g);
     if (rc != MSC_OK) {
       if (g) cudaGraphDestroy(g);
@@ -780,9 +807,10 @@ int Core::run_batches(int k) {
     memcpy(stats.stage_launches, stage0, sizeof(stage0));
     graph_key_ = key;
   }
-  for (int i = 0; i < k; ++i) CK(cudaGraphLaunch(graph_, stream_));
-  stats.launches += (uint64_t)graph_launches_ * (uint64_t)k;
-  stats.graph_replays += (uint64_t)k;
+  const int replays = (k + kGraphBodies - 1) / kGraphBodies;  // bodies past the work plan empty batches
+  for (int i = 0; i < replays; ++i) CK(cudaGraphLaunch(graph_, stream_));
+  stats.launches += (uint64_t)graph_launches_ * (uint64_t)replays;
+  stats.graph_replays += (uint64_t)replays;
   return MSC_OK;
 }
 
@@ -905,7 +933,7 @@ void Core::tune_begin_dim() {
       tune_cands_.push_back(t);
     };
     if (tune_dim_ == 0) {
-      for (int e = 18; e <= 21; ++e)
+      for (int e = 18; e <= 22; ++e)
         if ((1 << e) <= batch_cap_) {
           TuneChoice c = base;
           c.batch_exp = e;

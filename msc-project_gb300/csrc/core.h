@@ -112,7 +112,7 @@ class Core {
   // choices (coordinate descent: batch size, direction bins, traversal
   // block, then the two sorts), each timed on the device over a few windows;
   // the fastest in rays per ms is kept.  Results are the same under any choice.
-  void start_autotune(int windows_per_candidate = 2);
+  void start_autotune(int windows_per_candidate = 3);
   void stop_autotune() { tune_active_ = false; tune_pending_ = -1; }
   bool tuning() const { return tune_active_; }
   TuneChoice choice() const;
@@ -151,7 +151,12 @@ class Core {
   int trace_occluded(const float* org, const float* dir, const float* tmax, int n, int* occluded);
 
  private:
-  int enqueue_batch();            // one batch body: plan, sort, trace, shade, shadow, re-bin
+  // One batch body: plan, sort, trace, shade, shadow, re-bin.  In a captured
+  // graph of several bodies (`overlap`), body i's occlusion runs on the side
+  // stream beside body i+1's plan, gather and closest-hit traversal; body
+  // i+1's shading waits for it, so every path still adds to its sample in
+  // bounce order.
+  int enqueue_batch(int index, bool overlap);
   int run_batches(int k);         // k batch bodies (graph replays or eager)
   void drop_graph();
   int finish_job(JobState& j);
@@ -198,7 +203,10 @@ class Core {
            *hperm_ = nullptr, *box6_ = nullptr, *hhi_ = nullptr, *hhi_g_ = nullptr, *hperm1_ = nullptr;
   SortScratch ss_;
   float4* hits_ = nullptr;
-  ShadowBuf shadow_;
+  ShadowBuf shadow_[2];          // shadow queues, alternating between batches
+  cudaStream_t side_ = nullptr;  // occlusion of batch k runs here beside batch k+1's front part
+  static constexpr int kGraphBodies = 4;
+  cudaEvent_t fork_ev_[kGraphBodies] = {}, join_ev_[kGraphBodies] = {};
   Counters* ctr_ = nullptr;    // device counters
   int* trace_counter_ = nullptr;  // ray counters of the persistent traversal (closest, shadow)
   Counters* h_ctr_ = nullptr;  // pinned copy

@@ -143,8 +143,8 @@ int plain_setup(msc_handle* h) {
   const int e = std::min(d.settings.bin_exponent, 24);
   uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(16ull << e, 1ull << 22);
   gen = std::max<uint64_t>(std::min<uint64_t>(gen, paths), 1);
-  // capacity for twice the scene's batch so the autotuner can also try a larger one
-  int rc = h->core.init(std::min(e + 1, 22), (int)gen, paths, d.ext.wide_bvh != 0);
+  // capacity for four times the scene's batch so the autotuner can also try larger ones
+  int rc = h->core.init(std::min(e + 2, 22), (int)gen, paths, d.ext.wide_bvh != 0);
   if (rc != MSC_OK) {
     h->err = h->core.err;
     return rc;
@@ -930,7 +930,7 @@ int msc_batch_get_stats(msc_batch* b, msc_stats* out) {
 
 int msc_batch_autotune(msc_batch* b, int windows) {
   if (!b || windows < 0) return MSC_ERR_ARG;
-  b->core.start_autotune(windows == 0 ? 2 : windows);
+  b->core.start_autotune(windows == 0 ? 3 : windows);
   return MSC_OK;
 }
 

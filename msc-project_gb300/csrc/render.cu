@@ -358,7 +358,6 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
       box6[a] = 0xffffffffu;
       box6[3 + a] = 0u;
     }
-    ctr->shadow_count = 0;
     ctr->closest += (unsigned long long)nb;
     ctr->batches += nb > 0 ? 1ull : 0ull;
   }

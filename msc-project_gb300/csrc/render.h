@@ -135,10 +135,10 @@ struct BatchPlan {
 // Device counters of the wavefront, read back in one copy.
 struct Counters {
   int bin_count[kBinRadix];  // rays held per bin
-  int shadow_count;          // shadow rays of the current batch
+  int shadow_count[2];       // shadow rays of the current batch, per shadow queue
   int err;                   // error bits
   int in_bins;               // rays held in all bins
-  int pad[5];
+  int pad[4];
   unsigned long long closest, shadow, batches;
 };
 

@@ -41,19 +41,17 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __
   __shared__ uint32_t sh[kSortMaxPasses][RADIX];
   for (int i = threadIdx.x; i < kSortMaxPasses * RADIX; i += kSortBlock) (&sh[0][0])[i] = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
   const int stride = gridDim.x * kSortBlock;
   for (int base = blockIdx.x * kSortBlock; base < n; base += stride) {
     const int idx = base + threadIdx.x;
     const bool ok = idx < n;
     const uint32_t key = ok ? keys[idx] : 0u;
-    for (int p = 0; p < passes; ++p) {
-      const int shift = p * kSortRadixBits;
-      const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
-      const int d = ok ? (int)((key >> shift) & ((1u << width) - 1u)) : -1;
-      const unsigned peers = __match_any_sync(0xffffffffu, d);
-      if (d >= 0 && lane == __ffs(peers) - 1) atomicAdd(&sh[p][d], (uint32_t)__popc(peers));
-    }
+    if (ok)  // shared-memory atomics: cheaper than grouping equal digits first
+      for (int p = 0; p < passes; ++p) {
+        const int shift = p * kSortRadixBits;
+        const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
+        atomicAdd(&sh[p][(key >> shift) & ((1u << width) - 1u)], 1u);
+      }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * RADIX; i += kSortBlock) {
