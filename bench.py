@@ -253,8 +253,9 @@ def bench_forms(args):
     for i in ids:
         b.release(i)
     # the per-job loop on the same jobs: one job in flight at a time, with the
-    # plain engine's settings (2^20 rays per batch, 128-thread traversal, both sorts)
-    b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
+    # same tuned settings, so the difference is only the merging of jobs
+    tuned_kw = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")}
+    b.set_tuning(**tuned_kw)
     b.set_max_active(1)
     _, pst = b.serve([(0.0, j) for j in jobs])
     plain_rate = rays_of(pst) / pst["wall_s"] / 1e6
@@ -266,9 +267,9 @@ def bench_forms(args):
         "paths": sum(job_paths(j) for j in jobs), "mrays_per_s": rate, "wall_s": wall,
         "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
         "speedup_vs_per_job_loop": rate / plain_rate if plain_rate else None,
-        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")},
-        "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["persistent"], t["ray_sort"],
-                          t["hit_sort"], round(t["mrays_per_s"], 1)] for t in tune_log]}
+        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")},
+        "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["persistent"], t["digit_bits"],
+                          t["ray_sort"], t["hit_sort"], round(t["mrays_per_s"], 1)] for t in tune_log]}
     # served: Poisson arrivals on the first 16 resident scenes, at each rate
     nres = min(16, len(scenes))
     out["served"] = {"workload": "Poisson arrivals on %d resident scenes, 128^2-512^2, 4-64 spp log-uniform, "
@@ -287,10 +288,7 @@ def bench_forms(args):
         row = {"rate_per_s": rrate, "seconds": dur, "requests": len(reqs)}
         for label, max_active in (("served", 0), ("per_job_loop", 1)):
             b.set_max_active(max_active)
-            if max_active:
-                b.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True)
-            else:
-                b.set_tuning(**{k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")})
+            b.set_tuning(**tuned_kw)
             _, sst = b.serve(reqs)
             row[label] = {"completed": sst["completed"], "mrays_per_s": sst["mrays_per_s"],
                           "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
@@ -320,7 +318,7 @@ def bench_stress(args):
            "generate_s": gen_s, "load_s": load_s}
     modes = {}
     for label, hit_sort in (("sorted_64bit_key", True), ("unsorted", False)):
-        pt.set_tuning(batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=hit_sort)
+        pt.set_tuning(batch_exponent=22, trace_block=64, ray_sort=False, hit_sort=hit_sort)
         pt.process_device()  # warm-up (captures this choice's graph)
         ms, rays = 0.0, 0
         for _ in range(2):
@@ -391,7 +389,8 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
     ap.add_argument("--tuning", default="auto",
-                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort[,persistent]")
+                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort"
+                         "[,persistent[,digit_bits]]")
     ap.add_argument("--stress-scale", type=float, default=1.0)
     ap.add_argument("--serve-rates", default="100:6,600:3",
                     help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
@@ -412,7 +411,8 @@ def main():
            "scale": args.scale, "width": info["width"], "height": info["height"], "spp": info["spp"],
            "triangles": info["triangles"], "lights": info["lights"],
            "batch": 1 << (20 if args.config == 1 else 16), "seed": SEED + args.config,
-           "l2": "inputs larger than L2: BVH + triangles ~0.4 GB, sample film 1.6 GB, ray pools 1.2 GB per step"}
+           "l2": "inputs larger than L2 (129 MB): BVH + triangles ~0.25 GB, sample film 1.6 GB, ray pool up to "
+                 "1.6 GB, batch buffers ~1.7 GB, all read or written every step"}
     if args.impl == "reference":
         run_reference(args, yaml, cfg)
         return
@@ -422,10 +422,18 @@ def main():
     t = time.time()
     pt = mscgpu.Pathtracer(yaml)
     log("scene load + device BVH build %.1f s" % (time.time() - t))
+    tuning_passes = 0
     if args.tuning != "auto":
-        v = [int(x) for x in args.tuning.split(",")] + [0]
+        v = [int(x) for x in args.tuning.split(",")]
+        v += [0, 8][len(v) - 5:]
         pt.set_tuning(batch_exponent=v[0], bins=v[1], trace_block=v[2], ray_sort=bool(v[3]), hit_sort=bool(v[4]),
-                      persistent=bool(v[5]))
+                      persistent=bool(v[5]), digit_bits=v[6])
+    else:
+        # the engine tunes itself during its first passes: let it finish before the warm-up
+        while pt.tuning()["tuning"] and tuning_passes < 16:
+            pt.process_device()
+            tuning_passes += 1
+        log("autotuner settled after %d passes: %s" % (tuning_passes, pt.tuning()))
     for _ in range(args.warmup):
         pt.process_device()
     clocks = ClockSampler()
@@ -456,7 +464,8 @@ def main():
     prof = pt.stats()
     pt.set_profiling(False)
     tuned = pt.tuning()
-    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent")}
+    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")}
+    cfg["tuning_passes"] = tuning_passes
     pt.close()
 
     total_ms = sum(dev_ms)

@@ -127,6 +127,8 @@ int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys
 
 /* Stable LSD radix sort of (keys, vals) on bits [0, bits); sorted in place. */
 int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
+/* The same with 4-, 8- or 11-bit digits (the autotuner's digit widths). */
+int msc_stage_sort_pairs_digits(uint32_t* keys, uint32_t* vals, int n, int bits, int digit_bits);
 
 /* The stable order of 64-bit keys as the hit sort takes it for a 64-bit hit
  * key (stable by the low word, then stably by the high word): perm[i] = index
@@ -193,15 +195,16 @@ typedef struct msc_tuning {
   int hit_sort;       /* 1: each batch's hits sorted by (geomID, primID) (Pathtracer.cpp:335-339) */
   int bins;           /* direction bins: 6 (DirectionalBins.cpp:37-115) or 26 / 98 (cube surface cells) */
   int persistent;     /* 1: persistent traversal kernels with per-lane ray refill (8-wide BVH) */
+  int digit_bits;     /* radix sort digit width: 4, 8 or 11 */
   int tuning;         /* read only: 1 while the autotuner is still sampling */
   int samples;        /* read only: candidate samples booked by the autotuner */
 } msc_tuning;
 typedef struct msc_tune_sample {
-  int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent;
+  int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent, digit_bits;
   double mrays_per_s; /* device-timed rays per second over the candidate's windows */
 } msc_tune_sample;
 /* Starts the online autotuner: the next batches are spread over candidate
-   choices (batch size, direction bins, traversal block, the two sorts), each timed
+   choices (batch size, direction bins, traversal block, sort digit width, the two sorts), each timed
    over `windows` windows (0: 3), and the fastest is kept.  No reference
    counterpart. */
 int msc_batch_autotune(msc_batch* b, int windows);

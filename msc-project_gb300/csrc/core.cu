@@ -179,7 +179,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
                  al256(4) +
                  3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(8 * 4) + al256(sizeof(BatchPlan)) +
-                 sort_scratch_bytes(B) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
+                 sort_scratch_bytes(B, 11) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
   Arena A{arena_, 0};
@@ -212,7 +212,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   trace_counter_ = A.take<int>(2);
   box6_ = A.take<uint32_t>(8);
   plan_ = A.take<BatchPlan>(1);
-  sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B)), B);
+  sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B, 11)), B, 11);
   hits_ = A.take<float4>(B);
   for (int q = 0; q < 2; ++q) {
     shadow_[q].o = A.take<float4>(B);
@@ -231,6 +231,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   CK(cudaMemset(ctr_, 0, sizeof(Counters)));
   CK(cudaMemset(plan_, 0, sizeof(BatchPlan)));
   persistent_grids_init();
+  sort_init();
   launch_pool_reset(bins_, stream_);
   CK(cudaStreamSynchronize(stream_));
   CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
@@ -658,9 +659,10 @@ uint64_t Core::graph_key() const {
   const uint64_t block = trace_block == 64 ? 0 : (trace_block == 128 ? 1 : 2);
   const uint64_t bins = bins_.nbins == 6 ? 0 : (bins_.nbins == 26 ? 1 : 2);
   const uint64_t pers = persistent_trace ? 1 : 0;
+  const uint64_t dig = sort_digits == 4 ? 0 : (sort_digits == 8 ? 1 : 2);
   return ns | (k64 << 9) | ((uint64_t)hit_bits_ << 10) | ((uint64_t)ray_sort << 16) | ((uint64_t)hit_sort << 17) |
          ((uint64_t)merge_bins << 18) | ((uint64_t)wide_ << 19) | (bexp << 20) | (block << 25) | (bins << 27) |
-         (pers << 29) | (1ull << 63);
+         (pers << 29) | (dig << 30) | (1ull << 63);
 }
 
 void Core::drop_graph() {
@@ -695,7 +697,7 @@ int Core::enqueue_batch(int index, bool overlap) {
       t.done(l);
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, 32, ss_, st, errw, nb);
+    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, 32, ss_, st, errw, nb, sort_digits);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;
@@ -717,9 +719,9 @@ int Core::enqueue_batch(int index, bool overlap) {
     // 64-bit key: stable by the low word, then stable by the high word
     StageClock t(this, MSC_STAGE_HITSORT);
     int l = launch_hit_keys64(d_scenes_, hits_, B, hkeys_, hhi_, st, nb);
-    const int l1 = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm1_, B, 32, ss_, st, errw, nb);
+    const int l1 = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm1_, B, 32, ss_, st, errw, nb, sort_digits);
     l += launch_gather_u32(hhi_, hperm1_, B, hhi_g_, st, nb);
-    const int l2 = sort_pairs(hhi_g_, hperm1_, hhi_, hperm_, B, 32, ss_, st, errw, nb);
+    const int l2 = sort_pairs(hhi_g_, hperm1_, hhi_, hperm_, B, 32, ss_, st, errw, nb, sort_digits);
     if (l1 < 0 || l2 < 0) {
       err = "internal: hit sort without distinct outputs";
       return MSC_ERR_CUDA;
@@ -729,7 +731,7 @@ int Core::enqueue_batch(int index, bool overlap) {
   } else if (hit_sort) {
     StageClock t(this, MSC_STAGE_HITSORT);
     int l = launch_hit_keys(d_scenes_, batch_.d, hits_, B, hkeys_, st, nb);
-    const int ls = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, B, hit_bits_, ss_, st, errw, nb);
+    const int ls = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, B, hit_bits_, ss_, st, errw, nb, sort_digits);
     if (ls < 0) {
       err = "internal: hit sort without distinct outputs";
       return MSC_ERR_CUDA;
@@ -763,15 +765,9 @@ int Core::enqueue_batch(int index, bool overlap) {
   return MSC_OK;
 }
 
-int Core::run_batches(int k) {
-  if (profiling || !use_graph) {
-    for (int i = 0; i < k; ++i) {
-      int rc = enqueue_batch(i, false);
-      if (rc != MSC_OK) return rc;
-    }
-    CK(cudaGetLastError());
-    return MSC_OK;
-  }
+// Captures and instantiates the batch graph for the current choice if needed.
+int Core::ensure_graph() {
+  if (profiling || !use_graph) return MSC_OK;
   const uint64_t key = graph_key();
   if (!graph_ || graph_key_ != key) {
     drop_graph();
@@ -807,6 +803,20 @@ int Core::run_batches(int k) {
     memcpy(stats.stage_launches, stage0, sizeof(stage0));
     graph_key_ = key;
   }
+  return MSC_OK;
+}
+
+int Core::run_batches(int k) {
+  if (profiling || !use_graph) {
+    for (int i = 0; i < k; ++i) {
+      int rc = enqueue_batch(i, false);
+      if (rc != MSC_OK) return rc;
+    }
+    CK(cudaGetLastError());
+    return MSC_OK;
+  }
+  const int grc = ensure_graph();
+  if (grc != MSC_OK) return grc;
   const int replays = (k + kGraphBodies - 1) / kGraphBodies;  // bodies past the work plan empty batches
   for (int i = 0; i < replays; ++i) CK(cudaGraphLaunch(graph_, stream_));
   stats.launches += (uint64_t)graph_launches_ * (uint64_t)replays;
@@ -880,6 +890,10 @@ int Core::step(bool* idle) {
   apply(tune_cands_[c].choice);
   k = std::min(k, 2);
   tune_rays0_ = (double)(h_ctr_->closest + h_ctr_->shadow);
+  {
+    const int grc = ensure_graph();  // graph construction stays outside the timed window
+    if (grc != MSC_OK) return grc;
+  }
   CK(cudaEventRecord(tune_ev_[0], stream_));
   int rc2 = run_batches(k);
   if (rc2 != MSC_OK) return rc2;
@@ -899,6 +913,7 @@ TuneChoice Core::choice() const {
   c.hit_sort = hit_sort;
   c.bins = bins_.nbins;
   c.persistent = persistent_trace;
+  c.digit_bits = sort_digits;
   return c;
 }
 
@@ -910,6 +925,7 @@ void Core::apply(const TuneChoice& c) {
   hit_sort = c.hit_sort;
   bins_.nbins = (c.bins == 26 || c.bins == 98) ? c.bins : 6;
   persistent_trace = c.persistent;
+  sort_digits = (c.digit_bits == 4 || c.digit_bits == 11) ? c.digit_bits : 8;
 }
 
 void Core::start_autotune(int windows) {
@@ -933,7 +949,7 @@ void Core::tune_begin_dim() {
       tune_cands_.push_back(t);
     };
     if (tune_dim_ == 0) {
-      for (int e = 18; e <= 22; ++e)
+      for (int e = 18; e <= 23; ++e)
         if ((1 << e) <= batch_cap_) {
           TuneChoice c = base;
           c.batch_exp = e;
@@ -957,12 +973,19 @@ void Core::tune_begin_dim() {
         add(c);
       }
     } else if (tune_dim_ == 3) {
+      if (base.ray_sort || base.hit_sort)
+        for (int db : {4, 8, 11}) {
+          TuneChoice c = base;
+          c.digit_bits = db;
+          add(c);
+        }
+    } else if (tune_dim_ == 4) {
       for (bool on : {true, false}) {
         TuneChoice c = base;
         c.ray_sort = on;
         add(c);
       }
-    } else if (tune_dim_ == 4) {
+    } else if (tune_dim_ == 5) {
       for (bool on : {true, false}) {
         TuneChoice c = base;
         c.hit_sort = on;

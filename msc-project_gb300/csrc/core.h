@@ -82,6 +82,7 @@ struct TuneChoice {
   bool hit_sort = true; // (geomID, primID) sort of each batch's hits
   int bins = 6;         // direction bins: 6, 26 or 98
   bool persistent = false;  // persistent traversal with per-lane ray refill
+  int digit_bits = 8;       // radix sort digit width: 4, 8 or 11
 };
 
 struct TuneSample {
@@ -107,10 +108,12 @@ class Core {
   int max_batches_per_step = 16;  // batch bodies enqueued between two host looks at the counters
   int trace_block = 128;          // traversal block size
   bool persistent_trace = false;  // persistent traversal kernels (8-wide BVH)
+  int sort_digits = 8;            // radix sort digit width (4, 8 or 11)
 
   // Online autotuner: while on, the next batches are spread over candidate
   // choices (coordinate descent: batch size, direction bins, traversal
-  // block, then the two sorts), each timed on the device over a few windows;
+  // block and form, sort digit width, then the two sorts), each timed on the
+  // device over a few windows;
   // the fastest in rays per ms is kept.  Results are the same under any choice.
   void start_autotune(int windows_per_candidate = 3);
   void stop_autotune() { tune_active_ = false; tune_pending_ = -1; }
@@ -158,6 +161,7 @@ class Core {
   // bounce order.
   int enqueue_batch(int index, bool overlap);
   int run_batches(int k);         // k batch bodies (graph replays or eager)
+  int ensure_graph();
   void drop_graph();
   int finish_job(JobState& j);
   int generate(bool* did);

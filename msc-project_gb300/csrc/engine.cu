@@ -141,10 +141,10 @@ int plain_setup(msc_handle* h) {
     return MSC_ERR_ARG;
   }
   const int e = std::min(d.settings.bin_exponent, 24);
-  uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(16ull << e, 1ull << 22);
+  uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(32ull << e, 1ull << 22);
   gen = std::max<uint64_t>(std::min<uint64_t>(gen, paths), 1);
-  // capacity for four times the scene's batch so the autotuner can also try larger ones
-  int rc = h->core.init(std::min(e + 2, 22), (int)gen, paths, d.ext.wide_bvh != 0);
+  // capacity for eight times the scene's batch so the autotuner can also try larger ones
+  int rc = h->core.init(std::min(e + 3, 23), (int)gen, paths, d.ext.wide_bvh != 0);
   if (rc != MSC_OK) {
     h->err = h->core.err;
     return rc;
@@ -659,6 +659,32 @@ int msc_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits) {
   return rc;
 }
 
+int msc_stage_sort_pairs_digits(uint32_t* keys, uint32_t* vals, int n, int bits, int digit_bits) {
+  if (n < 0 || bits < 0 || bits > 32 || (n > 0 && (!keys || !vals)) ||
+      (digit_bits != 4 && digit_bits != 8 && digit_bits != 11))
+    return MSC_ERR_ARG;
+  if (n == 0) return MSC_OK;
+  uint32_t* d = nullptr;
+  char* scratch = nullptr;
+  const size_t sb = sort_scratch_bytes(n, 11);
+  int rc = MSC_OK;
+  if (cudaMalloc(&d, (size_t)n * 16) != cudaSuccess || cudaMalloc(&scratch, sb) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && (cudaMemcpy(d, keys, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMemcpy(d + n, vals, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK) {
+    SortScratch ss;
+    sort_scratch_bind(&ss, scratch, n, 11);
+    sort_pairs(d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, n, bits, ss, 0, nullptr, nullptr, digit_bits);
+    if (cudaMemcpy(keys, d + 2 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(vals, d + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = MSC_ERR_CUDA;
+  }
+  if (d) cudaFree(d);
+  if (scratch) cudaFree(scratch);
+  return rc;
+}
+
 int msc_stage_sort_keys64(const uint64_t* keys, int n, uint32_t* perm) {
   if (n < 0 || (n > 0 && (!keys || !perm))) return MSC_ERR_ARG;
   if (n == 0) return MSC_OK;
@@ -942,6 +968,7 @@ static void tuning_of(Core& c, msc_tuning* out) {
   out->hit_sort = t.hit_sort ? 1 : 0;
   out->bins = t.bins;
   out->persistent = t.persistent ? 1 : 0;
+  out->digit_bits = t.digit_bits;
   out->tuning = c.tuning() ? 1 : 0;
   out->samples = (int)c.tune_log.size();
 }
@@ -962,8 +989,10 @@ int msc_get_tuning(msc_handle* h, msc_tuning* out) {
 static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > core.batch_cap() ||
       (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256) ||
-      (in->bins != 6 && in->bins != 26 && in->bins != 98)) {
-    *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, or bins not 6, 26 or 98";
+      (in->bins != 6 && in->bins != 26 && in->bins != 98) ||
+      (in->digit_bits != 4 && in->digit_bits != 8 && in->digit_bits != 11)) {
+    *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, bins not 6, 26 or 98, or "
+           "digit width not 4, 8 or 11";
     return MSC_ERR_ARG;
   }
   TuneChoice c;
@@ -973,6 +1002,7 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   c.hit_sort = in->hit_sort != 0;
   c.bins = in->bins;
   c.persistent = in->persistent != 0;
+  c.digit_bits = in->digit_bits;
   core.stop_autotune();
   core.apply(c);
   return MSC_OK;
@@ -1000,6 +1030,7 @@ int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {
     out[i].hit_sort = log[i].choice.hit_sort ? 1 : 0;
     out[i].bins = log[i].choice.bins;
     out[i].persistent = log[i].choice.persistent ? 1 : 0;
+    out[i].digit_bits = log[i].choice.digit_bits;
     out[i].mrays_per_s = log[i].ms > 0 ? log[i].rays / log[i].ms / 1e3 : 0.0;
   }
   return MSC_OK;

@@ -108,40 +108,59 @@ constexpr int kSortTile = kSortBlock * kSortItems;
 constexpr int kSortRadixBits = 8;
 constexpr int kSortMaxPasses = 4;
 
+// Histogram words for any digit width (4: 8 x 16, 8: 4 x 256, 11: 3 x 2048)
+// and tile counters for up to 8 passes.
+constexpr int kSortHistWords = 3 * 2048;
+constexpr int kSortMaxPassesAny = 8;
+
 struct SortScratch {
   uint32_t* keys_alt = nullptr;
   uint32_t* vals_alt = nullptr;
   uint32_t* counts = nullptr;   // reduce-then-scan: RADIX * tiles (aliases the first half of `status`)
   uint32_t* status = nullptr;   // look-back words: 2 arrays of RADIX * tiles
-  uint32_t* hist = nullptr;     // kSortMaxPasses * RADIX global digit counts
-  uint32_t* ctl = nullptr;      // kSortMaxPasses tile counters, then the error word
+  uint32_t* hist = nullptr;     // global digit counts of every pass (kSortHistWords)
+  uint32_t* ctl = nullptr;      // kSortMaxPassesAny tile counters, then the error word
   int capacity = 0;
+  int max_digit_bits = 8;       // widest digit the status arrays were sized for (8 or 11)
 };
 
 constexpr size_t sort_align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t sort_tiles(int capacity) {
   return capacity <= 0 ? 1 : ((size_t)capacity + kSortTile - 1) / kSortTile;
 }
-// Scratch bytes for sorts of up to `capacity` pairs.
-constexpr size_t sort_scratch_bytes(int capacity) {
-  return 2 * sort_align256((size_t)(capacity > 0 ? capacity : 1) * 4) +
-         sort_align256(2 * sort_tiles(capacity) * (1u << kSortRadixBits) * 4) +
-         sort_align256((size_t)kSortMaxPasses * (1u << kSortRadixBits) * 4 + 64);
+// Look-back words per status array: tiles x radix, the largest over the digit
+// widths up to max_digit_bits (11-bit digits use tiles of 2048 keys).
+constexpr size_t sort_status_words(int capacity, int max_digit_bits) {
+  return max_digit_bits >= 11 ? ((size_t)(capacity > 0 ? capacity : 1) + 2047) / 2048 * 2048
+                              : sort_tiles(capacity) * 256;
 }
-// Carves the scratch buffers out of `base` (sort_scratch_bytes(capacity) bytes, 256-aligned).
-void sort_scratch_bind(SortScratch* s, void* base, int capacity);
+// Scratch bytes for sorts of up to `capacity` pairs with digits of up to
+// max_digit_bits (8 or 11) bits.
+constexpr size_t sort_scratch_bytes(int capacity, int max_digit_bits = 8) {
+  return 2 * sort_align256((size_t)(capacity > 0 ? capacity : 1) * 4) +
+         sort_align256(2 * sort_status_words(capacity, max_digit_bits) * 4) +
+         sort_align256((size_t)kSortHistWords * 4 + 64);
+}
+// Carves the scratch buffers out of `base` (sort_scratch_bytes(capacity, max_digit_bits) bytes, 256-aligned).
+void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_bits = 8);
+// Opts the pass kernels into the shared memory they need (idempotent; call
+// before any stream capture).
+void sort_init();
 
 // Stable LSD sort of (keys_in, vals_in) on bits [0, bits) into (keys_out, vals_out).
 // vals_in == nullptr means vals_in[i] = i.  Input buffers are left unchanged
 // unless they alias the outputs.  One histogram kernel for all passes, then
-// one kernel per 8-bit pass with a decoupled look-back across tiles.  Spin
+// one kernel per digit pass with a decoupled look-back across tiles.  Spin
 // waits are capped; a cap that runs out sets bit 8 of *err (when err is not
 // null).  Returns the number of kernel launches.  n_dev (optional): the pair
 // count is read on the device when the kernels run and n is its upper bound
 // (sizes the grids); this form needs outputs distinct from the inputs when
 // the pass count is odd, and returns -1 otherwise.
+// digit_bits: 4, 8 or 11 (an 11-bit sort needs scratch bound for 11 bits,
+// else it falls back to 8).
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr);
+               int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr,
+               int digit_bits = 8);
 
 // The same order with three kernels per pass (upsweep count, one-block scan,
 // downsweep scatter) and no inter-block waiting.

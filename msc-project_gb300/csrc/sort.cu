@@ -34,28 +34,40 @@ __device__ __forceinline__ int sort_count(int n_max, const int* n_dev) {
   return n_dev ? min(*n_dev, n_max) : n_max;
 }
 
+// Digit width RB (4, 8 or 11 bits): radix, keys per thread, tile and passes.
+template <int RB>
+struct SortShape {
+  static constexpr int RADIX = 1 << RB;
+  static constexpr int ITEMS = RB > 8 ? 8 : kSortItems;
+  static constexpr int TILE = kSortBlock * ITEMS;
+  static constexpr int MAXP = (32 + RB - 1) / RB;
+  static constexpr int DPT = RADIX > kSortBlock ? RADIX / kSortBlock : 1;  // digits per thread
+};
+
+template <int RB>
 __global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __restrict__ keys, int n_max,
                                                               const int* __restrict__ n_dev, int passes, int bits,
                                                               uint32_t* __restrict__ hist) {
+  using S = SortShape<RB>;
   const int n = sort_count(n_max, n_dev);
-  __shared__ uint32_t sh[kSortMaxPasses][RADIX];
-  for (int i = threadIdx.x; i < kSortMaxPasses * RADIX; i += kSortBlock) (&sh[0][0])[i] = 0;
+  __shared__ uint32_t sh[S::MAXP * S::RADIX];
+  for (int i = threadIdx.x; i < S::MAXP * S::RADIX; i += kSortBlock) sh[i] = 0;
   __syncthreads();
   const int stride = gridDim.x * kSortBlock;
   for (int base = blockIdx.x * kSortBlock; base < n; base += stride) {
     const int idx = base + threadIdx.x;
-    const bool ok = idx < n;
-    const uint32_t key = ok ? keys[idx] : 0u;
-    if (ok)  // shared-memory atomics: cheaper than grouping equal digits first
+    if (idx < n) {  // shared-memory atomics: cheaper than grouping equal digits first
+      const uint32_t key = keys[idx];
       for (int p = 0; p < passes; ++p) {
-        const int shift = p * kSortRadixBits;
-        const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
-        atomicAdd(&sh[p][(key >> shift) & ((1u << width) - 1u)], 1u);
+        const int shift = p * RB;
+        const int width = bits - shift < RB ? bits - shift : RB;
+        atomicAdd(&sh[p * S::RADIX + ((key >> shift) & ((1u << width) - 1u))], 1u);
       }
+    }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < passes * RADIX; i += kSortBlock) {
-    const uint32_t c = (&sh[0][0])[i];
+  for (int i = threadIdx.x; i < passes * S::RADIX; i += kSortBlock) {
+    const uint32_t c = sh[i];
     if (c) atomicAdd(&hist[i], c);
   }
 }
@@ -77,6 +89,20 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_t
   return before + incl - v;
 }
 
+template <int RB>
+struct PassSmem {
+  using S = SortShape<RB>;
+  RankSmem<kSortBlock, S::RADIX> rank;
+  uint32_t skey[S::TILE];
+  uint32_t sval[S::TILE];
+  uint32_t gofs[S::RADIX];
+  uint32_t warp_tmp[kSortBlock / 32];
+  int tile;
+};
+
+// One pass: thread t owns digits [t*DPT, (t+1)*DPT) (the first RADIX threads
+// when the radix is smaller than the block) for the scan and the look-back.
+template <int RB>
 __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
@@ -85,89 +111,109 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
                                                               uint32_t mask, int pass,
                                                               const uint32_t* __restrict__ hist, uint32_t* status_cur,
                                                               uint32_t* status_next, uint32_t* ctl, int* err) {
-  static_assert(RADIX == kSortBlock, "one digit per thread");
-  __shared__ RankSmem<kSortBlock, RADIX> sm;
-  __shared__ uint32_t skey[kSortTile];
-  __shared__ uint32_t sval[kSortTile];
-  __shared__ uint32_t gofs[RADIX];
-  __shared__ uint32_t warp_tmp[kSortBlock / 32];
-  __shared__ int s_tile;
-  if (threadIdx.x == 0) s_tile = (int)atomicAdd(&ctl[pass], 1u);
-  const uint32_t dstart = block_excl_scan(hist[pass * RADIX + threadIdx.x], warp_tmp);  // syncs inside
-  const int tile = s_tile;
-  const int base = tile * kSortTile;
+  using S = SortShape<RB>;
+  constexpr int RADIX = S::RADIX, DPT = S::DPT, ITEMS = S::ITEMS, TILE = S::TILE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassSmem<RB>& sm = *reinterpret_cast<PassSmem<RB>*>(smem_raw);
+  const int d0 = threadIdx.x * DPT;
+  const bool owns = d0 < RADIX;
+  if (threadIdx.x == 0) sm.tile = (int)atomicAdd(&ctl[pass], 1u);
+  // global start of each owned digit: exclusive scan of the pass histogram
+  uint32_t hv[DPT], own = 0;
+#pragma unroll
+  for (int k = 0; k < DPT; ++k) {
+    hv[k] = owns ? hist[pass * RADIX + d0 + k] : 0u;
+    own += hv[k];
+  }
+  uint32_t run = block_excl_scan(own, sm.warp_tmp);  // syncs inside
+  uint32_t dstart[DPT];
+#pragma unroll
+  for (int k = 0; k < DPT; ++k) {
+    dstart[k] = run;
+    run += hv[k];
+  }
+  const int tile = sm.tile;
+  const int base = tile * TILE;
   const int n = sort_count(n_max, n_dev);
   if (base >= n) return;  // the whole block: past a batch smaller than the launch
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // the next pass reads status_next from zero; the pass that last used it has finished
-  if (status_next) status_next[tile * RADIX + threadIdx.x] = 0u;
-  uint32_t key[kSortItems], val[kSortItems];
-  int dig[kSortItems], pos[kSortItems];
+  if (status_next && owns)
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    const int idx = base + warp * 32 * kSortItems + k * 32 + lane;
+    for (int k = 0; k < DPT; ++k) status_next[tile * RADIX + d0 + k] = 0u;
+  uint32_t key[ITEMS], val[ITEMS];
+  int dig[ITEMS], pos[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; ++k) {
+    const int idx = base + warp * 32 * ITEMS + k * 32 + lane;
     const bool ok = idx < n;
     key[k] = ok ? keys_in[idx] : 0u;
     val[k] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
     dig[k] = ok ? (int)((key[k] >> shift) & mask) : -1;
   }
-  tile_rank<kSortBlock, kSortItems, RADIX>(dig, pos, sm);
-  {
-    const int d = threadIdx.x;
-    const uint32_t cnt = (uint32_t)sm.tile_count[d];
-    uint32_t excl = 0;
-    if (tile == 0) {
-      st_volatile(&status_cur[d], (cnt << 2) | kFlagPrefix);
-    } else {
-      st_volatile(&status_cur[tile * RADIX + d], (cnt << 2) | kFlagAggregate);
-      // Look back a window of kLookbackWindow predecessors per step (independent
-      // loads), summing aggregates up to the first inclusive prefix.
-      int t = tile - 1;
-      int spins = 0;
-      while (t >= 0) {
-        uint32_t v[kLookbackWindow];
+  tile_rank<kSortBlock, ITEMS, RADIX>(dig, pos, sm.rank);
+  if (owns) {
+    uint32_t cnt[DPT];
+    // post every owned aggregate first, so successors can sum past this tile
 #pragma unroll
-        for (int k = 0; k < kLookbackWindow; ++k)
-          v[k] = (t - k >= 0) ? ld_volatile(&status_cur[(t - k) * RADIX + d]) : kFlagPrefix;
-        int used = 0;
-        bool done = false;
+    for (int k = 0; k < DPT; ++k) {
+      cnt[k] = (uint32_t)sm.rank.tile_count[d0 + k];
+      st_volatile(&status_cur[tile * RADIX + d0 + k], (cnt[k] << 2) | (tile == 0 ? kFlagPrefix : kFlagAggregate));
+    }
 #pragma unroll
-        for (int k = 0; k < kLookbackWindow; ++k) {
-          if (done || used < k) continue;       // stop at the first prefix or the first unposted tile
-          const uint32_t f = v[k] & 3u;
-          if (f == 0u) continue;                // not posted yet: re-read from here
-          excl += v[k] >> 2;
-          used = k + 1;
-          if (f == kFlagPrefix) done = true;
-        }
-        if (done) break;
-        t -= used;
-        if (used < kLookbackWindow) {  // a predecessor has not posted yet; it is running, so this ends
-          if (++spins > kLookbackSpinCap) {
-            atomicOr(err, kSortErrLookback);
-            break;
+    for (int k = 0; k < DPT; ++k) {
+      const int d = d0 + k;
+      uint32_t excl = 0;
+      if (tile > 0) {
+        // Look back a window of kLookbackWindow predecessors per step (independent
+        // loads), summing aggregates up to the first inclusive prefix.
+        int t = tile - 1;
+        int spins = 0;
+        while (t >= 0) {
+          uint32_t v[kLookbackWindow];
+#pragma unroll
+          for (int w = 0; w < kLookbackWindow; ++w)
+            v[w] = (t - w >= 0) ? ld_volatile(&status_cur[(t - w) * RADIX + d]) : kFlagPrefix;
+          int used = 0;
+          bool done = false;
+#pragma unroll
+          for (int w = 0; w < kLookbackWindow; ++w) {
+            if (done || used < w) continue;  // stop at the first prefix or the first unposted tile
+            const uint32_t f = v[w] & 3u;
+            if (f == 0u) continue;           // not posted yet: re-read from here
+            excl += v[w] >> 2;
+            used = w + 1;
+            if (f == kFlagPrefix) done = true;
+          }
+          if (done) break;
+          t -= used;
+          if (used < kLookbackWindow) {  // a predecessor has not posted yet; it is running, so this ends
+            if (++spins > kLookbackSpinCap) {
+              atomicOr(err, kSortErrLookback);
+              break;
+            }
           }
         }
+        st_volatile(&status_cur[tile * RADIX + d], ((excl + cnt[k]) << 2) | kFlagPrefix);
       }
-      st_volatile(&status_cur[tile * RADIX + d], ((excl + cnt) << 2) | kFlagPrefix);
+      sm.gofs[d] = dstart[k] + excl;
     }
-    gofs[d] = dstart + excl;
   }
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < ITEMS; ++k) {
     if (pos[k] >= 0) {
-      skey[pos[k]] = key[k];
-      sval[pos[k]] = val[k];
+      sm.skey[pos[k]] = key[k];
+      sm.sval[pos[k]] = val[k];
     }
   }
   __syncthreads();
-  const int count = min(kSortTile, n - base);
+  const int count = min(TILE, n - base);
   for (int p = threadIdx.x; p < count; p += kSortBlock) {
-    const uint32_t k = skey[p];
+    const uint32_t k = sm.skey[p];
     const int d = (int)((k >> shift) & mask);
-    const uint32_t o = gofs[d] + (uint32_t)(p - sm.tile_start[d]);
+    const uint32_t o = sm.gofs[d] + (uint32_t)(p - sm.rank.tile_start[d]);
     keys_out[o] = k;
-    vals_out[o] = sval[p];
+    vals_out[o] = sm.sval[p];
   }
 }
 
@@ -307,7 +353,7 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, int len
   }
 }
 
-void sort_scratch_bind(SortScratch* s, void* base, int capacity) {
+void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_bits) {
   const size_t cap = (size_t)(capacity > 0 ? capacity : 1);
   char* p = (char*)base;
   s->keys_alt = (uint32_t*)p;
@@ -316,16 +362,19 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity) {
   p += sort_align256(cap * 4);
   s->status = (uint32_t*)p;
   s->counts = s->status;
-  p += sort_align256(2 * sort_tiles(capacity) * RADIX * 4);
+  p += sort_align256(2 * sort_status_words(capacity, max_digit_bits) * 4);
   s->hist = (uint32_t*)p;
-  s->ctl = s->hist + kSortMaxPasses * RADIX;
+  s->ctl = s->hist + kSortHistWords;
   s->capacity = capacity;
+  s->max_digit_bits = max_digit_bits >= 11 ? 11 : 8;
 }
 
-int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev) {
-  if (n <= 0) return 0;
-  const int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
+namespace {
+template <int RB>
+int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n, int bits,
+             SortScratch& s, cudaStream_t stream, int* err, const int* n_dev) {
+  using S = SortShape<RB>;
+  const int passes = (bits + RB - 1) / RB;
   if (n_dev && (passes == 0 || ((passes % 2) == 1 && (keys_in == keys_out || (vals_in && vals_in == vals_out)))))
     return -1;  // a device count needs distinct outputs and at least one pass
   const uint32_t* src_k;
@@ -333,32 +382,52 @@ int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
   bool done;
   int launches = sort_prologue(src_k, src_v, keys_in, vals_in, keys_out, vals_out, n, passes, s, stream, &done);
   if (done) return launches;
-  const int tiles = (n + kSortTile - 1) / kSortTile;
+  const int tiles = (n + S::TILE - 1) / S::TILE;
   uint32_t* status0 = s.status;
-  uint32_t* status1 = s.status + (size_t)tiles * RADIX;
+  uint32_t* status1 = s.status + (size_t)tiles * S::RADIX;
   // zero the first look-back array, the histograms, the tile counters and the error word
-  cudaMemsetAsync(status0, 0, (size_t)tiles * RADIX * 4, stream);
-  cudaMemsetAsync(s.hist, 0, (size_t)kSortMaxPasses * RADIX * 4 + 64, stream);
-  int* errw = err ? err : (int*)(s.ctl + kSortMaxPasses);
-  const int hist_blocks = tiles < 2 * 152 ? tiles : 2 * 152;
-  k_onesweep_hist<<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
+  cudaMemsetAsync(status0, 0, (size_t)tiles * S::RADIX * 4, stream);
+  cudaMemsetAsync(s.hist, 0, (size_t)kSortHistWords * 4 + 64, stream);
+  int* errw = err ? err : (int*)(s.ctl + kSortMaxPassesAny);
+  const int hist_blocks = std::min(std::max(1, (n + S::TILE - 1) / S::TILE), 2 * 152);
+  k_onesweep_hist<RB><<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
   ++launches;
   for (int p = 0; p < passes; ++p) {
     const bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
     uint32_t* dst_v = to_out ? vals_out : s.vals_alt;
-    const int shift = p * kSortRadixBits;
-    const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;  // the last pass may be narrower
+    const int shift = p * RB;
+    const int width = bits - shift < RB ? bits - shift : RB;  // the last pass may be narrower
     const uint32_t mask = (1u << width) - 1u;
     uint32_t* cur = (p & 1) ? status1 : status0;
     uint32_t* next = (p + 1 < passes) ? ((p & 1) ? status0 : status1) : nullptr;
-    k_onesweep_pass<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, n_dev, shift, mask, p, s.hist,
-                                                      cur, next, s.ctl, errw);
+    k_onesweep_pass<RB><<<tiles, kSortBlock, sizeof(PassSmem<RB>), stream>>>(
+        src_k, src_v, dst_k, dst_v, n, n_dev, shift, mask, p, s.hist, cur, next, s.ctl, errw);
     ++launches;
     src_k = dst_k;
     src_v = dst_v;
   }
   return launches;
+}
+}  // namespace
+
+void sort_init() {
+  static bool done = false;
+  if (done) return;
+  done = true;
+  cudaFuncSetAttribute(k_onesweep_pass<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem<4>));
+  cudaFuncSetAttribute(k_onesweep_pass<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem<8>));
+  cudaFuncSetAttribute(k_onesweep_pass<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem<11>));
+}
+
+int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
+               int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, int digit_bits) {
+  if (n <= 0) return 0;
+  sort_init();
+  if (digit_bits > s.max_digit_bits) digit_bits = 8;  // scratch sized for narrower digits
+  if (digit_bits == 4) return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
+  if (digit_bits == 11) return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
+  return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
 }
 
 int sort_pairs_reduce_scan(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,

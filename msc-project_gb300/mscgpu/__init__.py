@@ -105,6 +105,7 @@ def load_library():
         "msc_batch_set_profiling": (I, [P, I]),
         "msc_batch_set_max_active": (I, [P, I]),
         "msc_stage_sort_keys64": (I, [C.POINTER(C.c_uint64), I, U32]),
+        "msc_stage_sort_pairs_digits": (I, [U32, U32, I, I, I]),
         "msc_batch_autotune": (I, [P, I]),
         "msc_get_tuning": (I, [P, C.POINTER(_Tuning)]),
         "msc_set_tuning": (I, [P, C.POINTER(_Tuning)]),
@@ -207,8 +208,9 @@ class Pathtracer:
         _check(self._lib.msc_get_tuning(self._h, C.byref(t)), self._h)
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False,
+                   digit_bits=8):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0)
         _check(self._lib.msc_set_tuning(self._h, C.byref(t)), self._h)
 
     def stats(self):
@@ -295,6 +297,15 @@ def sort_pairs(keys, vals, bits=32):
     return k, v
 
 
+def sort_pairs_digits(keys, vals, bits=32, digit_bits=8):
+    """Stable radix sort with 4-, 8- or 11-bit digits; returns sorted (keys, vals)."""
+    lib = load_library()
+    k = np.ascontiguousarray(keys, np.uint32).copy()
+    v = np.ascontiguousarray(vals, np.uint32).copy()
+    _check(lib.msc_stage_sort_pairs_digits(_ptr(k, C.c_uint32), _ptr(v, C.c_uint32), k.shape[0], bits, digit_bits))
+    return k, v
+
+
 def sort_keys64(keys):
     """Stable order of 64-bit keys as the 64-bit hit sort takes it."""
     lib = load_library()
@@ -344,12 +355,13 @@ def scene_load_host(yaml_path):
 
 class _Tuning(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("bins", C.c_int), ("persistent", C.c_int), ("tuning", C.c_int), ("samples", C.c_int)]
+                ("bins", C.c_int), ("persistent", C.c_int), ("digit_bits", C.c_int), ("tuning", C.c_int),
+                ("samples", C.c_int)]
 
 
 class _TuneSample(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("bins", C.c_int), ("persistent", C.c_int), ("mrays_per_s", C.c_double)]
+                ("bins", C.c_int), ("persistent", C.c_int), ("digit_bits", C.c_int), ("mrays_per_s", C.c_double)]
 
 
 def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
@@ -440,8 +452,9 @@ class Batch:
         self._check(self._lib.msc_batch_get_tuning(self._b, C.byref(t)))
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
-    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), 0, 0)
+    def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False,
+                   digit_bits=8):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0)
         self._check(self._lib.msc_batch_set_tuning(self._b, C.byref(t)))
 
     def tune_log(self):

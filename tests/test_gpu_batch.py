@@ -168,7 +168,9 @@ def test_results_do_not_depend_on_the_tuning_choice(built, scenes):
     for cfg in (dict(batch_exponent=10, trace_block=64, ray_sort=False, hit_sort=True),
                 dict(batch_exponent=12, trace_block=256, ray_sort=True, hit_sort=False),
                 dict(batch_exponent=14, trace_block=128, ray_sort=False, hit_sort=False),
-                dict(batch_exponent=13, trace_block=128, ray_sort=True, hit_sort=False, persistent=True, bins=26)):
+                dict(batch_exponent=13, trace_block=128, ray_sort=True, hit_sort=False, persistent=True, bins=26),
+                dict(batch_exponent=12, trace_block=64, ray_sort=True, hit_sort=True, bins=98, digit_bits=11),
+                dict(batch_exponent=14, trace_block=256, ray_sort=True, hit_sort=True, digit_bits=4)):
         b = mscgpu.Batch(batch_exponent=14, film_samples=1 << 22)
         for s in scenes:
             b.add_scene(s)

@@ -189,3 +189,18 @@ def test_bin_partition_n_bins_stable_and_bit_exact(built, nbins, n):
     assert np.array_equal(gc, wc)
     for b in range(nbins):
         assert np.array_equal(got[b * cap: b * cap + gc[b]].view(np.uint32), want[b * cap: b * cap + wc[b]].view(np.uint32))
+
+
+@pytest.mark.parametrize("digit_bits", [4, 8, 11])
+@pytest.mark.parametrize("n,bits", [(1, 32), (2047, 32), (2049, 22), (100000, 32), (300001, 13), (1 << 20, 30)])
+def test_radix_digit_widths_are_the_stable_order(built, digit_bits, n, bits):
+    """4-, 8- and 11-bit digits (the autotuner's widths) give CPU std::stable_sort's order."""
+    mscgpu, oracle = built
+    rng = np.random.default_rng(n + bits + digit_bits)
+    keys = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 3] = keys[: n // 3] & np.uint32(0xF0F)  # many equal digits
+    vals = np.arange(n, dtype=np.uint32)
+    gk, gv = mscgpu.sort_pairs_digits(keys, vals, bits, digit_bits)
+    wk, wv = oracle.stable_sort_pairs(keys, vals, bits)
+    assert np.array_equal(gv, wv)
+    assert np.array_equal(gk, wk)
