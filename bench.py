@@ -209,7 +209,7 @@ def bench_forms(args):
     gen_s = time.time() - t
     film_cap = 1_800_000_000  # the film pool indexes samples with 31 bits
     t = time.time()
-    b = mscgpu.Batch(batch_exponent=22, film_samples=film_cap)
+    b = mscgpu.Batch(batch_exponent=23, film_samples=film_cap)
     bboxes, tris = [], []
     for y in scenes:
         k = b.add_scene(y)
@@ -231,10 +231,10 @@ def bench_forms(args):
 
     out = {}
     # autotune on a sample of the same workload (untimed): the first 16 jobs at
-    # up to 16 spp, repeated until the tuner has booked every candidate
-    b.autotune(windows=2)
+    # up to 16 spp, one run per candidate until the tuner has booked them all
+    b.autotune(windows=1)
     sample = [dict(j, spp=min(j["spp"], 16)) for j in jobs[:16]]
-    for _ in range(8):
+    for _ in range(24):
         ids = [b.submit(**j) for j in sample]
         b.run()
         for i in ids:
@@ -430,7 +430,7 @@ def main():
                       persistent=bool(v[5]), digit_bits=v[6])
     else:
         # the engine tunes itself during its first passes: let it finish before the warm-up
-        while pt.tuning()["tuning"] and tuning_passes < 16:
+        while pt.tuning()["tuning"] and tuning_passes < 24:
             pt.process_device()
             tuning_passes += 1
         log("autotuner settled after %d passes: %s" % (tuning_passes, pt.tuning()))

@@ -203,9 +203,10 @@ typedef struct msc_tune_sample {
   int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent, digit_bits;
   double mrays_per_s; /* device-timed rays per second over the candidate's windows */
 } msc_tune_sample;
-/* Starts the online autotuner: the next batches are spread over candidate
-   choices (batch size, direction bins, traversal block, sort digit width, the two sorts), each timed
-   over `windows` windows (0: 3), and the fastest is kept.  No reference
+/* Starts the online autotuner: each following msc_batch_run (each pass of
+   the plain engine) renders with the next candidate choice (direction bins,
+   traversal block and form, sort digit width, the two sorts) and is timed;
+   every candidate gets `windows` runs (0: 1), and the fastest is kept.  No reference
    counterpart. */
 int msc_batch_autotune(msc_batch* b, int windows);
 int msc_batch_get_tuning(msc_batch* b, msc_tuning* out);

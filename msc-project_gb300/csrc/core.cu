@@ -826,7 +826,6 @@ int Core::run_batches(int k) {
 
 void Core::reset_stats() {
   stats = CoreStats();
-  tune_pending_ = -1;  // a window in flight is not booked across a reset
   if (ctr_) {
     cudaMemsetAsync(&ctr_->closest, 0, 3 * sizeof(unsigned long long), stream_);
     h_ctr_->closest = h_ctr_->shadow = h_ctr_->batches = 0;
@@ -845,7 +844,6 @@ int Core::step(bool* idle) {
   stats.closest = h_ctr_->closest;
   stats.shadow = h_ctr_->shadow;
   stats.batches = h_ctr_->batches;
-  if (tune_pending_ >= 0) tune_window_done();
   if (h_ctr_->err != 0) {
     const int e = h_ctr_->err;
     err = (e & ERR_BIN_OVERFLOW)    ? "a direction bin overflowed"
@@ -882,25 +880,8 @@ int Core::step(bool* idle) {
     return MSC_OK;
   }
   if (merge_bins) need = (total + bs - 1) / bs;
-  int k = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)std::max(1, max_batches_per_step));
-  if (!tune_active_) return run_batches(k);
-  // a tuning window: this candidate's choice for at most two batch bodies
-  const int n = (int)tune_cands_.size();
-  const int c = tune_next_ % n;
-  apply(tune_cands_[c].choice);
-  k = std::min(k, 2);
-  tune_rays0_ = (double)(h_ctr_->closest + h_ctr_->shadow);
-  {
-    const int grc = ensure_graph();  // graph construction stays outside the timed window
-    if (grc != MSC_OK) return grc;
-  }
-  CK(cudaEventRecord(tune_ev_[0], stream_));
-  int rc2 = run_batches(k);
-  if (rc2 != MSC_OK) return rc2;
-  CK(cudaEventRecord(tune_ev_[1], stream_));
-  tune_pending_ = c;
-  tune_next_ += 1;
-  return MSC_OK;
+  const int k = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)std::max(1, max_batches_per_step));
+  return run_batches(k);
 }
 
 TuneChoice Core::choice() const {
@@ -932,7 +913,6 @@ void Core::start_autotune(int windows) {
   tune_windows_ = std::max(1, windows);
   tune_active_ = true;
   tune_dim_ = 0;
-  tune_pending_ = -1;
   tune_log.clear();
   tune_begin_dim();
 }
@@ -949,12 +929,9 @@ void Core::tune_begin_dim() {
       tune_cands_.push_back(t);
     };
     if (tune_dim_ == 0) {
-      for (int e = 18; e <= 23; ++e)
-        if ((1 << e) <= batch_cap_) {
-          TuneChoice c = base;
-          c.batch_exp = e;
-          add(c);
-        }
+      // Batch size is not sampled: on a pass's first batches the bins hold too
+      // few rays to fill large batches, which biases short windows against
+      // them, while every measured workload ran fastest at the full capacity.
     } else if (tune_dim_ == 1) {
       for (int nb : {6, 26, 98}) {
         TuneChoice c = base;
@@ -1000,16 +977,9 @@ void Core::tune_begin_dim() {
   }
 }
 
-// Called at a step's start, after the sync: books the window that just ended.
-void Core::tune_window_done() {
-  if (tune_pending_ < 0) return;
-  float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, tune_ev_[0], tune_ev_[1]) == cudaSuccess) {
-    TuneSample& t = tune_cands_[tune_pending_];
-    t.rays += (double)(h_ctr_->closest + h_ctr_->shadow) - tune_rays0_;
-    t.ms += ms;
-  }
-  tune_pending_ = -1;
+// After a booked run: when every candidate of the dimension has its runs,
+// keep the fastest (rays per device ms) and move to the next dimension.
+void Core::tune_sample_done() {
   if (tune_next_ < (int)tune_cands_.size() * tune_windows_) return;
   int best = -1;
   double best_rate = -1.0;
@@ -1028,6 +998,17 @@ void Core::tune_window_done() {
 }
 
 int Core::run_all(const volatile bool* stop) {
+  // while tuning, the whole run is one sample of the next candidate
+  int cand = -1;
+  double rays0 = 0;
+  if (tune_active_ && !tune_cands_.empty()) {
+    cand = tune_next_ % (int)tune_cands_.size();
+    apply(tune_cands_[cand].choice);
+    const int grc = ensure_graph();  // graph construction stays outside the timed run
+    if (grc != MSC_OK) return grc;
+    rays0 = (double)(h_ctr_->closest + h_ctr_->shadow);
+    CK(cudaEventRecord(tune_ev_[0], stream_));
+  }
   while (true) {
     if (stop && *stop) return MSC_OK;
     bool idle = false;
@@ -1039,6 +1020,18 @@ int Core::run_all(const volatile bool* stop) {
         if (jp->slot >= 0 && !jp->complete) open = true;
       if (!open) break;
     }
+  }
+  if (cand >= 0) {
+    CK(cudaEventRecord(tune_ev_[1], stream_));
+    CK(cudaEventSynchronize(tune_ev_[1]));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, tune_ev_[0], tune_ev_[1]) == cudaSuccess) {
+      TuneSample& t = tune_cands_[cand];
+      t.rays += (double)(h_ctr_->closest + h_ctr_->shadow) - rays0;
+      t.ms += ms;
+    }
+    tune_next_ += 1;
+    tune_sample_done();
   }
   CK(cudaStreamSynchronize(stream_));
   CK(cudaGetLastError());

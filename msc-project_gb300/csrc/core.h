@@ -110,13 +110,13 @@ class Core {
   bool persistent_trace = false;  // persistent traversal kernels (8-wide BVH)
   int sort_digits = 8;            // radix sort digit width (4, 8 or 11)
 
-  // Online autotuner: while on, the next batches are spread over candidate
-  // choices (coordinate descent: batch size, direction bins, traversal
-  // block and form, sort digit width, then the two sorts), each timed on the
-  // device over a few windows;
+  // Online autotuner: while on, each run_all (a render pass or a batched
+  // run) is one timed sample of the next candidate choice (coordinate
+  // descent: direction bins, traversal block and form, sort digit width,
+  // then the two sorts);
   // the fastest in rays per ms is kept.  Results are the same under any choice.
-  void start_autotune(int windows_per_candidate = 3);
-  void stop_autotune() { tune_active_ = false; tune_pending_ = -1; }
+  void start_autotune(int runs_per_candidate = 1);
+  void stop_autotune() { tune_active_ = false; }
   bool tuning() const { return tune_active_; }
   TuneChoice choice() const;
   void apply(const TuneChoice& c);
@@ -177,12 +177,10 @@ class Core {
   bool tune_active_ = false;
   int tune_dim_ = 0, tune_windows_ = 2;
   std::vector<TuneSample> tune_cands_;
-  int tune_next_ = 0;           // candidate of the next window
-  int tune_pending_ = -1;       // candidate timed by the window in flight
-  double tune_rays0_ = 0;
+  int tune_next_ = 0;           // candidate of the next run
   cudaEvent_t tune_ev_[2] = {nullptr, nullptr};
   void tune_begin_dim();
-  void tune_window_done();
+  void tune_sample_done();
   std::vector<std::unique_ptr<SceneGPU>> scenes_;
   std::vector<std::unique_ptr<JobState>> jobs_;
   std::vector<int> free_slots_;

@@ -153,7 +153,9 @@ int plain_setup(msc_handle* h) {
   h->core.hit_sort = d.ext.hit_sort != 0;
   {
     TuneChoice c = h->core.choice();
-    c.batch_exp = std::max(6, e);  // the scene's bin exponent (Settings.h:16-24) is the starting batch size
+    // eight times the scene's bin exponent (Settings.h:16-24): larger
+    // traversal grids amortise the kernels' tails
+    c.batch_exp = std::min(e + 3, 23);
     c.bins = d.ext.bins;
     h->core.apply(c);
   }
@@ -956,7 +958,7 @@ int msc_batch_get_stats(msc_batch* b, msc_stats* out) {
 
 int msc_batch_autotune(msc_batch* b, int windows) {
   if (!b || windows < 0) return MSC_ERR_ARG;
-  b->core.start_autotune(windows == 0 ? 3 : windows);
+  b->core.start_autotune(windows == 0 ? 1 : windows);
   return MSC_OK;
 }
 

@@ -193,7 +193,7 @@ def test_autotuner_books_samples_and_keeps_results(built, scenes):
     for s in scenes:
         b.add_scene(s)
     b.autotune(windows=1)
-    for _ in range(6):  # the tuner spends a window per step; keep feeding work until it is done
+    for _ in range(6):  # the tuner spends one run per candidate; keep feeding work
         ids = [b.submit(**j) for j in JOBS]
         b.run()
         for k, i in enumerate(ids):
