@@ -644,11 +644,17 @@ bool decode_texture(const YNode* n, ShaderRec* sh, SceneDesc* S, const std::stri
 // ---------------------------------------------------------------- images
 // PFM: "PF" (RGB) or "Pf" (grey), width height, scale (< 0: little endian),
 // rows bottom first.  PPM: "P6", width height, maxval (< 256: 8 bit, else 16
-// bit big endian), rows top first, values / maxval.  Both end up top first.
+// bit big endian), rows top first, values / maxval.  OpenEXR: uncompressed
+// scanline files (read_exr_rgb).  All end up top first.
+bool read_exr_rgb(const std::string& path, int* w, int* h, std::vector<float>* rgb, std::string* err);
+
 bool image_load(const std::string& path, TexImage* out, std::string* err) {
   std::ifstream f(path, std::ios::binary);
   if (!f) { *err = "cannot open texture image [" + path + "]"; return false; }
   std::string data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  if (data.size() >= 4 && (unsigned char)data[0] == 0x76 && (unsigned char)data[1] == 0x2f &&
+      (unsigned char)data[2] == 0x31 && (unsigned char)data[3] == 0x01)
+    return read_exr_rgb(path, &out->width, &out->height, &out->rgb, err);
   size_t p = 0;
   auto token = [&]() {
     while (p < data.size()) {
@@ -697,7 +703,7 @@ bool image_load(const std::string& path, TexImage* out, std::string* err) {
     }
     return true;
   }
-  *err = "texture image [" + path + "] is not PFM or binary PPM";
+  *err = "texture image [" + path + "] is not PFM, binary PPM or OpenEXR";
   return false;
 }
 

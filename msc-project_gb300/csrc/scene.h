@@ -66,7 +66,7 @@ struct TexImage {
   int width = 0, height = 0;
   std::vector<float> rgb;  // 3 per texel
 };
-// Reads PFM (PF/Pf), PPM (P6, 8 or 16 bit) images.
+// Reads PFM (PF/Pf), PPM (P6, 8 or 16 bit) and uncompressed scanline OpenEXR images.
 bool image_load(const std::string& path, TexImage* out, std::string* err);
 enum LightType : int { LIGHT_QUAD = 0, LIGHT_SPHERE = 1 };
 enum CameraType : int { CAMERA_PINHOLE = 0, CAMERA_THINLENS = 1 };

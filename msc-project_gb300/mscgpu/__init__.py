@@ -105,6 +105,7 @@ def load_library():
         "msc_batch_set_profiling": (I, [P, I]),
         "msc_batch_set_max_active": (I, [P, I]),
         "msc_stage_sort_keys64": (I, [C.POINTER(C.c_uint64), I, U32]),
+        "msc_write_image_file": (I, [C.c_char_p, I, I, F]),
         "msc_stage_sort_pairs_digits": (I, [U32, U32, I, I, I]),
         "msc_batch_autotune": (I, [P, I]),
         "msc_get_tuning": (I, [P, C.POINTER(_Tuning)]),
@@ -295,6 +296,14 @@ def sort_pairs(keys, vals, bits=32):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     _check(lib.msc_sort_pairs(_ptr(k, C.c_uint32), _ptr(v, C.c_uint32), k.shape[0], bits))
     return k, v
+
+
+def write_image(path, rgb):
+    """Writes an (h, w, 3) float image as OpenEXR (RGBA half) or PFM, by the file's extension."""
+    lib = load_library()
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w = rgb.shape[:2]
+    _check(lib.msc_write_image_file(os.fsencode(path), w, h, _ptr(rgb, C.c_float)))
 
 
 def sort_pairs_digits(keys, vals, bits=32, digit_bits=8):

@@ -509,10 +509,89 @@ namespace orc {
 
 // PFM ("PF"/"Pf", rows bottom first, scale < 0 little endian) and binary PPM
 // ("P6", maxval < 256: bytes, else 16-bit big endian), both stored top first.
+// binary16 -> binary32, exact.
+float h2f(uint16_t h) {
+  const int e = (h >> 10) & 31, m = h & 1023;
+  float v;
+  if (e == 0) v = std::ldexp((float)m, -24);
+  else if (e == 31) v = m ? NAN : INFINITY;
+  else v = std::ldexp((float)(1024 + m), e - 25);
+  return (h & 0x8000) ? -v : v;
+}
+
+// Uncompressed single-part scanline OpenEXR: R, G, B (or Y) of HALF / FLOAT.
+bool read_exr(const std::string& d, OImage* im) {
+  auto u32 = [&](size_t p) { return (uint32_t)(unsigned char)d[p] | ((uint32_t)(unsigned char)d[p + 1] << 8) |
+                                    ((uint32_t)(unsigned char)d[p + 2] << 16) | ((uint32_t)(unsigned char)d[p + 3] << 24); };
+  if (d.size() < 8 || u32(0) != 20000630u || (u32(4) & 0xff) != 2 || (u32(4) & 0x1e00)) return false;
+  size_t p = 8;
+  std::vector<std::pair<std::string, int>> ch;
+  int comp = -1, x0 = 0, y0 = 0, x1 = -1, y1 = -1;
+  while (p < d.size() && d[p]) {
+    std::string name, type;
+    while (p < d.size() && d[p]) name.push_back(d[p++]);
+    ++p;
+    while (p < d.size() && d[p]) type.push_back(d[p++]);
+    ++p;
+    if (p + 4 > d.size()) return false;
+    size_t sz = u32(p);
+    p += 4;
+    size_t end = p + sz;
+    if (end > d.size()) return false;
+    if (name == "channels") {
+      size_t q = p;
+      while (q < end && d[q]) {
+        std::string cn;
+        while (q < end && d[q]) cn.push_back(d[q++]);
+        ++q;
+        ch.push_back({cn, (int)u32(q)});
+        q += 16;
+      }
+    } else if (name == "compression") comp = (unsigned char)d[p];
+    else if (name == "dataWindow") { x0 = (int)u32(p); y0 = (int)u32(p + 4); x1 = (int)u32(p + 8); y1 = (int)u32(p + 12); }
+    p = end;
+  }
+  ++p;
+  const int w = x1 - x0 + 1, h = y1 - y0 + 1;
+  if (comp != 0 || w <= 0 || h <= 0 || ch.empty()) return false;
+  size_t line = 0;
+  std::vector<size_t> off;
+  int idx[3] = {-1, -1, -1}, iy = -1;
+  for (size_t c = 0; c < ch.size(); ++c) {
+    if (ch[c].second != 1 && ch[c].second != 2) return false;
+    off.push_back(line);
+    line += (size_t)w * (ch[c].second == 1 ? 2 : 4);
+    if (ch[c].first == "R") idx[0] = (int)c;
+    if (ch[c].first == "G") idx[1] = (int)c;
+    if (ch[c].first == "B") idx[2] = (int)c;
+    if (ch[c].first == "Y") iy = (int)c;
+  }
+  if (idx[0] < 0 || idx[1] < 0 || idx[2] < 0) { if (iy < 0) return false; idx[0] = idx[1] = idx[2] = iy; }
+  im->w = w; im->h = h;
+  im->rgb.assign((size_t)w * h * 3, 0.f);
+  for (int k = 0; k < h; ++k) {
+    const size_t bo = (size_t)u32(p + 8 * (size_t)k) | ((size_t)u32(p + 8 * (size_t)k + 4) << 32);
+    if (bo + 8 + line > d.size()) return false;
+    const int y = (int)u32(bo) - y0;
+    if (y < 0 || y >= h) return false;
+    for (int x = 0; x < w; ++x)
+      for (int c = 0; c < 3; ++c) {
+        const int t = ch[idx[c]].second;
+        const size_t q = bo + 8 + off[idx[c]] + (size_t)x * (t == 1 ? 2 : 4);
+        float v;
+        if (t == 1) v = h2f((uint16_t)((unsigned char)d[q] | ((unsigned char)d[q + 1] << 8)));
+        else { uint32_t u = u32(q); memcpy(&v, &u, 4); }
+        im->rgb[((size_t)y * w + x) * 3 + c] = v;
+      }
+  }
+  return true;
+}
+
 bool read_image(const std::string& path, OImage* im) {
   std::ifstream f(path, std::ios::binary);
   if (!f) return false;
   std::string d((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  if (d.size() >= 4 && (unsigned char)d[0] == 0x76 && (unsigned char)d[1] == 0x2f) return read_exr(d, im);
   size_t p = 0;
   auto tok = [&]() {
     while (p < d.size() && (isspace((unsigned char)d[p]) || d[p] == '#')) {

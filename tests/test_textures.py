@@ -68,5 +68,22 @@ def test_unreadable_texture_image_is_rejected(built, tmp_path):
     y = make_texture_scene(mscgpu, str(tmp_path))
     with open(os.path.join(str(tmp_path), "tex_a.pfm"), "wb") as f:
         f.write(b"P3\n1 1\n255\n0 0 0\n")  # ASCII PPM: not a format this build reads
-    with pytest.raises(mscgpu.MscError, match="not PFM or binary PPM"):
+    with pytest.raises(mscgpu.MscError, match="not PFM, binary PPM or OpenEXR"):
         mscgpu.scene_load_host(y)
+
+
+def test_exr_texture_reads_back_the_written_halves(built, tmp_path):
+    """An image written by the product's OpenEXR writer (RGBA half) is read back
+    by the texture loader: at texel centres the lookup returns the halves."""
+    mscgpu, oracle = built
+    rng = np.random.default_rng(11)
+    img = rng.uniform(0, 3, size=(4, 7, 3)).astype(np.float32)
+    path = str(tmp_path / "t.exr")
+    mscgpu.write_image(path, img)
+    h, w = img.shape[:2]
+    ys, xs = np.mgrid[0:h, 0:w]
+    s = ((xs + 0.5) / w).astype(np.float32).ravel()
+    t = ((ys + 0.5) / h).astype(np.float32).ravel()
+    got = oracle.image_lookup(path, s, t)
+    want = img.astype(np.float16).astype(np.float32).reshape(-1, 3)
+    assert np.allclose(got, want, rtol=1e-6, atol=1e-7)

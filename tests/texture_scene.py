@@ -31,6 +31,7 @@ def make_texture_scene(mscgpu, out_dir, seed=7):
     write_pfm(os.path.join(out_dir, "tex_a.pfm"), rng.uniform(0.1, 0.9, size=(5, 7, 3)).astype(np.float32))
     write_ppm(os.path.join(out_dir, "tex_b.ppm"), rng.integers(0, 256, size=(4, 6, 3)))
     write_pfm(os.path.join(out_dir, "mask.pfm"), rng.uniform(0, 1, size=(3, 3)).astype(np.float32), little=False)
+    mscgpu.write_image(os.path.join(out_dir, "tex_c.exr"), rng.uniform(0, 1.5, size=(6, 5, 3)).astype(np.float32))
     text = open(y).read()
     head, scene, ext = text.split("---")
     blocks = list(re.finditer(r"  texture:\n    type: Constant\n    colour: \[[^\]]*\]\n", scene))
@@ -40,7 +41,7 @@ def make_texture_scene(mscgpu, out_dir, seed=7):
                "    mask:\n      type: Standard\n      string: mask.pfm\n")
     nested = ("  texture:\n    type: Layered\n    upper:\n      type: Layered\n"
               "      upper:\n        type: Constant\n        colour: [0.9, 0.1, 0.1]\n"
-              "      lower:\n        type: Standard\n        string: tex_a.pfm\n"
+              "      lower:\n        type: Standard\n        string: tex_c.exr\n"
               "      mask:\n        type: Standard\n        string: tex_b.ppm\n"
               "    lower:\n      type: Standard\n      string: tex_b.ppm\n"
               "    mask:\n      type: Constant\n      colour: [0.5, 0.25, 0.75]\n")
