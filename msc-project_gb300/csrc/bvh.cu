@@ -371,6 +371,8 @@ size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // octant o that visits slots o ^ 0, o ^ 1, ..., o ^ 7 meets the children
 // roughly front to back without sorting them.
 constexpr int kWideLeafMax = 2;
+// a node's triangle bits (eight slots of at most kWideLeafMax) fit one word
+static_assert(8 * kWideLeafMax <= 32, "triangle bits of a node must fit one word");
 
 struct WideBuild {
   std::vector<uint32_t> words;  // 20 words per node

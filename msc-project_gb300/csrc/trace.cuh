@@ -26,11 +26,13 @@ struct TriHit {
 
 // Moller-Trumbore with u, v the weights of v1 and v2 (the barycentric
 // convention PolygonObject::texture relies on, src/core/PolygonObject.cpp:45-63).
-// Accepts tmin < t < tmax.
+// Accepts tmin < t < tmax, or tmin < t <= tmax when CLOSED (the closest-hit
+// queries, which settle equal distances by the triangle's scene index).
 // Before the IEEE reciprocal, candidates are rejected in det-scaled terms only
 // where the exact test below would reject them too: the signs of u and v are
 // exact, and the upper bounds keep a margin far above the rounding of the
 // scaled sums, so the accepted set and every result are unchanged.
+template <bool CLOSED>
 __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float3 v0, float3 e1, float3 e2, float tmin,
                                               float tmax, float* t_out, float* u_out, float* v_out) {
   float3 p = v_cross(d, e2);
@@ -51,11 +53,19 @@ __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float3 v0, flo
   float v = vs * inv;
   if (v < 0.0f || u + v > 1.0f) return false;
   float t = v_dot(e2, q) * inv;
-  if (!(t > tmin && t < tmax)) return false;
+  if (!(t > tmin && (CLOSED ? t <= tmax : t < tmax))) return false;
   *t_out = t;
   *u_out = u;
   *v_out = v;
   return true;
+}
+
+// Closest-hit acceptance of a candidate at distance t <= tmax with scene
+// triangle index g: nearer, or as near with a smaller index (best_g < 0 until
+// the first hit, so a first hit must be strictly inside tmax).  The result is
+// then the same whatever order the candidates are met in.
+__device__ __forceinline__ bool closer_hit(float t, int g, float tmax, int best_g) {
+  return t < tmax || g < best_g;
 }
 
 __device__ __forceinline__ float safe_rcp(float x) {
@@ -81,6 +91,7 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
   // a well-formed tree visits far fewer nodes; the cap only guards against a
   // malformed one (reported through *overflow = 2)
   int steps = 0;
+  int best_g = -1;
   while (true) {
     while (node >= 0) {
       if (++steps > kTraceStepCap) {
@@ -127,14 +138,18 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
       const float4 c = __ldg(&tris[3 * k + 2]);
       if (!ANY || __float_as_int(b.w) == 0) {
         float t, u, v;
-        if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
-          found = true;
+        if (tri_intersect<!ANY>(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
           if (ANY) return true;
-          tmax = t;
-          hit->t = t;
-          hit->u = u;
-          hit->v = v;
-          hit->tri = k;
+          const int g = __float_as_int(c.w);
+          if (closer_hit(t, g, tmax, best_g)) {
+            found = true;
+            tmax = t;
+            best_g = g;
+            hit->t = t;
+            hit->u = u;
+            hit->v = v;
+            hit->tri = k;
+          }
         }
       }
     }
@@ -190,12 +205,13 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
   int sp = 0;
   // the root as the only child of a virtual group: base 0, slot 0 internal
   uint32_t g_base = 0, g_imask = 1u, g_hits = 1u << oct;
+  uint32_t t_base = 0, t_mask = 0;
   bool found = false;
   const float widen = 1.0000004f;
   int steps = 0;
+  int best_g = -1;
   while (true) {
-    uint32_t t_base = 0, t_mask = 0;
-    if (g_hits != 0u) {
+    if (g_hits != 0u && t_mask == 0u) {
       const uint32_t j = (uint32_t)(__ffs(g_hits) - 1);
       g_hits &= g_hits - 1u;
       const uint32_t slot = j ^ oct;
@@ -266,14 +282,18 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
       const float4 c = __ldg(&tris[3 * k + 2]);
       if (ANY && __float_as_int(b.w) != 0) continue;
       float t, u, v;
-      if (tri_intersect(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
-        found = true;
+      if (tri_intersect<!ANY>(o, d, f3(a), f3(b), f3(c), tmin, tmax, &t, &u, &v)) {
         if (ANY) return true;
-        tmax = t;
-        hit->t = t;
-        hit->u = u;
-        hit->v = v;
-        hit->tri = k;
+        const int g = __float_as_int(c.w);
+        if (closer_hit(t, g, tmax, best_g)) {
+          found = true;
+          tmax = t;
+          best_g = g;
+          hit->t = t;
+          hit->u = u;
+          hit->v = v;
+          hit->tri = k;
+        }
       }
     }
     if (g_hits == 0u) {
@@ -292,13 +312,14 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
 // keeps one ray per lane and, when a lane's ray ends, hands the lane a new ray
 // (Aila and Laine, "Understanding the Efficiency of Ray Traversal on GPUs",
 // HPG 2009), so warps stay full instead of waiting for their slowest ray.
-// The per-ray order of steps is that of bvh8_trace, so hits are identical.
+// Hits are identical to bvh8_trace's: both return the nearest candidate,
+// equal distances settled by the smaller scene triangle index.
 struct Trav8 {
   float3 o, d, id;
   float tmin, tmax;
   uint32_t oct;
   uint32_t g_base, g_imask, g_hits, t_base, t_mask;
-  int sp, steps;
+  int sp, steps, best_g;
   bool found;
 };
 
@@ -316,6 +337,7 @@ __device__ __forceinline__ void trav8_init(Trav8& s, float3 o, float3 d, float t
   s.t_mask = 0;
   s.sp = 0;
   s.steps = 0;
+  s.best_g = -1;
   s.found = false;
 }
 
@@ -336,14 +358,21 @@ __device__ __forceinline__ bool trav8_step(Trav8& s, uint2* stack, const uint4* 
     const float4 c = __ldg(&tris[3 * k + 2]);
     if (ANY && __float_as_int(b.w) != 0) return false;
     float t, u, v;
-    if (tri_intersect(s.o, s.d, f3(a), f3(b), f3(c), s.tmin, s.tmax, &t, &u, &v)) {
-      s.found = true;
-      if (ANY) return true;
-      s.tmax = t;
-      hit->t = t;
-      hit->u = u;
-      hit->v = v;
-      hit->tri = k;
+    if (tri_intersect<!ANY>(s.o, s.d, f3(a), f3(b), f3(c), s.tmin, s.tmax, &t, &u, &v)) {
+      if (ANY) {
+        s.found = true;
+        return true;
+      }
+      const int g = __float_as_int(c.w);
+      if (closer_hit(t, g, s.tmax, s.best_g)) {
+        s.found = true;
+        s.tmax = t;
+        s.best_g = g;
+        hit->t = t;
+        hit->u = u;
+        hit->v = v;
+        hit->tri = k;
+      }
     }
     return false;
   }

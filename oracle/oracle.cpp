@@ -977,8 +977,11 @@ void build_bvh(oracle_scene* S) {
 }
 
 // Moller-Trumbore in the documented order (fused multiply-adds inside dot and cross).
+// Accepts tmin < t < tmax, or tmin < t <= tmax when closed (closest-hit
+// queries, which settle equal distances by the smaller scene triangle index,
+// so the answer does not depend on the order the tree presents candidates in).
 template <class T>
-bool tri_hit(const oracle_scene* S, int tri, V<T> o, V<T> d, T tmin, T tmax, T* tt, T* uu, T* vv) {
+bool tri_hit(const oracle_scene* S, int tri, V<T> o, V<T> d, T tmin, T tmax, bool closed, T* tt, T* uu, T* vv) {
   const float* p = &S->tv[9 * tri];
   V<T> v0 = mk<T>(p[0], p[1], p[2]);
   V<T> e1 = sub(mk<T>(p[3], p[4], p[5]), v0);
@@ -994,7 +997,7 @@ bool tri_hit(const oracle_scene* S, int tri, V<T> o, V<T> d, T tmin, T tmax, T* 
   T v = dot(d, q) * inv;
   if (v < T(0) || u + v > T(1)) return false;
   T t = dot(e2, q) * inv;
-  if (!(t > tmin && t < tmax)) return false;
+  if (!(t > tmin && (closed ? t <= tmax : t < tmax))) return false;
   *tt = t; *uu = u; *vv = v;
   return true;
 }
@@ -1030,11 +1033,13 @@ int trace(const oracle_scene* S, V<T> o, V<T> d, T tmin, T tmax, bool any, T* th
         int tri = S->order[k];
         if (any && S->tlight[tri]) continue;
         T t, u, v;
-        if (tri_hit<T>(S, tri, o, d, tmin, tmax, &t, &u, &v)) {
+        if (tri_hit<T>(S, tri, o, d, tmin, tmax, !any, &t, &u, &v)) {
           if (any) return tri;
-          tmax = t;
-          *th = t; *uh = u; *vh = v;
-          hit = tri;
+          if (t < tmax || (hit >= 0 && tri < hit)) {
+            tmax = t;
+            *th = t; *uh = u; *vh = v;
+            hit = tri;
+          }
         }
       }
     } else {

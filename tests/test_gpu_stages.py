@@ -141,6 +141,48 @@ def test_closest_hit_matches_oracle(built, box_scene, form, tmp_path):
     assert (t[hit].view(np.uint32) == wt[hit].view(np.uint32)).mean() > 0.999
 
 
+def _duplicated_scene(mscgpu, out_dir):
+    """The tiny scene with every box face listed twice in its OBJ and the
+    icosphere object placed twice: coincident triangles, so many rays meet two
+    candidates at exactly the same distance."""
+    import os
+    import re
+    y = mscgpu.generate_scene(100, 1234, str(out_dir))
+    box = os.path.join(str(out_dir), "box.obj")
+    lines = open(box).read().splitlines()
+    open(box, "w").write("\n".join(lines + [l for l in lines if l.startswith("f ")]) + "\n")
+    text = open(y).read()
+    obj = re.search(r"object:\n  type: Polygon\n  filename: icosphere.obj\n(?:  .*\n)*", text).group(0)
+    head, scene, ext = text.split("---")
+    open(y, "w").write(head + "---" + scene + obj + "---" + ext)
+    return y
+
+
+@pytest.mark.parametrize("form", ["wide", "binary"])
+def test_exact_ties_go_to_the_smaller_triangle_index(built, tmp_path, form):
+    """Equal distances are settled by the scene triangle index (geomID, then
+    primID) on both sides, whatever order the two BVHs present the candidates in."""
+    mscgpu, oracle = built
+    y = _duplicated_scene(mscgpu, tmp_path / "dup")
+    s = oracle.Scene(y)
+    org, d = _scene_rays(s, np.random.default_rng(21), 100000)
+    with mscgpu.Pathtracer(_with_bvh(y, form, tmp_path)) as pt:
+        t, u, v, g, p = pt.trace_closest(org, d)
+    wt, wu, wv, wg, wp = s.trace(org, d)
+    assert np.array_equal(g, wg) and np.array_equal(p, wp)
+    hit = wg >= 0
+    assert (t[hit].view(np.uint32) == wt[hit].view(np.uint32)).mean() > 0.999
+    # triangles of one copy of the box faces (fan triangulation of each face)
+    ntri = sum(len(l.split()) - 3 for l in open(str(tmp_path / "dup" / "box.obj")) if l.startswith("f ")) // 2
+    geoms = open(y).read().split("---")[1].split("object:")[1:]
+    box_g = [i for i, m in enumerate(geoms) if "box.obj" in m]
+    ico_g = [i for i, m in enumerate(geoms) if "icosphere.obj" in m]
+    # the first copy always wins, and both coincident sets are hit
+    on_box = np.isin(g, box_g)
+    assert np.all(p[on_box] < ntri) and on_box.sum() > 100
+    assert len(ico_g) == 2 and not np.any(g == ico_g[1]) and (g == ico_g[0]).sum() > 100
+
+
 @pytest.mark.parametrize("form", ["wide", "binary"])
 def test_occlusion_matches_oracle(built, box_scene, form, tmp_path):
     mscgpu, oracle = built
