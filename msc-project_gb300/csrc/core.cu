@@ -11,6 +11,12 @@ namespace mscg {
 
 namespace {
 
+// Bits of the ray sort key the batch sort orders by (the top ones): a ray's
+// order within a batch only shapes traversal coherence, and the top 16 bits
+// of the interleaved key (three levels of origin and direction under the
+// bin) carry nearly all of it in two sort passes instead of four.
+constexpr int kRayKeyBits = 16;
+
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Arena {  // one cudaMalloc carved into aligned pieces
@@ -178,7 +184,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
                  2 * al256((size_t)kMaxBins * 4) + al256((size_t)kMaxBins * max_chunks * 4) + al256(chunks * 4) +
                  al256(4) +
                  3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
-                 al256(8 * 4) + al256(sizeof(BatchPlan)) +
+                 al256(pool_rays * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B, 11) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
@@ -186,6 +192,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   bins_.rays.o = A.take<float4>(pool_rays);
   bins_.rays.d = A.take<float4>(pool_rays);
   bins_.rays.w = A.take<float4>(pool_rays);
+  bins_.keys = A.take<uint32_t>(pool_rays);
   bins_.num_chunks = (int)chunks;
   bins_.max_chunks = max_chunks;
   bins_.held = A.take<int>(kMaxBins);
@@ -210,7 +217,6 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   hperm1_ = A.take<uint32_t>(B);
   ctr_ = A.take<Counters>(1);
   trace_counter_ = A.take<int>(2);
-  box6_ = A.take<uint32_t>(8);
   plan_ = A.take<BatchPlan>(1);
   sort_scratch_bind(&ss_, A.take<char>(sort_scratch_bytes(B, 11)), B, 11);
   hits_ = A.take<float4>(B);
@@ -233,6 +239,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   persistent_grids_init();
   sort_init();
   launch_pool_reset(bins_, stream_);
+  CK(cudaMemsetAsync(bins_.keys, 0, (size_t)bins_.num_chunks * kChunk * 4, stream_));
   CK(cudaStreamSynchronize(stream_));
   CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
   memset(h_ctr_, 0, sizeof(Counters));
@@ -364,6 +371,17 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
   r.tex_images = sg->d_tex_images;
   r.tex_texels = sg->d_tex_texels;
   r.tri_uv = sg->d_tri_uv;
+  {  // the ray sort key quantises origins in the scene box
+    float b[8];
+    CK(cudaMemcpy(b, sg->bvh.bounds_dev, sizeof(b), cudaMemcpyDeviceToHost));
+    float sc[3];
+    for (int a = 0; a < 3; ++a) {
+      const float e = b[3 + a] - b[a];
+      sc[a] = e > 0.f ? 64.0f / e : 0.f;
+    }
+    r.key_lo = make_float4(b[0], b[1], b[2], 0.f);
+    r.key_scale = make_float4(sc[0], sc[1], sc[2], 0.f);
+  }
   if (!d.sphere_lights.empty()) {
     std::vector<float4> sp;
     for (int li : d.sphere_lights) {
@@ -644,7 +662,7 @@ int Core::generate(bool* did) {
   t.done(launches);
   if (filled > 0) {
     StageClock tb(this, MSC_STAGE_BINS);
-    tb.done(launch_bin_partition(staging_, (int)filled, bins_, stream_));
+    tb.done(launch_bin_partition(staging_, (int)filled, bins_, stream_, nullptr, ray_sort ? d_scenes_ : nullptr));
     stats.generations += 1;
     *did = true;
   }
@@ -686,18 +704,16 @@ int Core::enqueue_batch(int index, bool overlap) {
   while ((1 << scene_bits) < ns) ++scene_bits;
   {
     StageClock t(this, MSC_STAGE_OTHER);
-    t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, box6_, ctr_, st));
+    t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, ctr_, st));
   }
   const uint32_t* perm = nullptr;
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      int l = launch_origin_box(bins_, plan_, B, box6_, st);
-      l += launch_ray_keys(bins_, plan_, B, box6_, keys_, st);
-      t.done(l);
+      t.done(launch_ray_keys(bins_, plan_, B, kRayKeyBits, keys_, st));
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, 32, ss_, st, errw, nb, sort_digits);
+    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, kRayKeyBits, ss_, st, errw, nb, sort_digits);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;
@@ -760,7 +776,7 @@ int Core::enqueue_batch(int index, bool overlap) {
   }
   {
     StageClock t(this, MSC_STAGE_BINS);
-    t.done(launch_bin_partition(staging_, B, bins_, st, nb));
+    t.done(launch_bin_partition(staging_, B, bins_, st, nb, ray_sort ? d_scenes_ : nullptr));
   }
   return MSC_OK;
 }

@@ -202,7 +202,7 @@ class Core {
   BinPool bins_;
   RayBuf staging_, batch_;
   uint32_t *keys_ = nullptr, *keys_sorted_ = nullptr, *perm_ = nullptr, *hkeys_ = nullptr, *hkeys_sorted_ = nullptr,
-           *hperm_ = nullptr, *box6_ = nullptr, *hhi_ = nullptr, *hhi_g_ = nullptr, *hperm1_ = nullptr;
+           *hperm_ = nullptr, *hhi_ = nullptr, *hhi_g_ = nullptr, *hperm1_ = nullptr;
   SortScratch ss_;
   float4* hits_ = nullptr;
   ShadowBuf shadow_[2];          // shadow queues, alternating between batches

@@ -242,25 +242,32 @@ MSC_HD uint32_t quantise(float v, float lo, float scale, int cells) {
   return (uint32_t)clamp_i(i, 0, cells - 1);
 }
 
-// 32-bit ray sort key: origin Morton code (3 x 6 bits, in the batch origin
-// box) above a direction Morton code (2 x 7 bits of the two minor direction
-// components divided by the dominant one, each in [-1,1]).  Sorting on it
-// groups rays by origin first and direction second, the order in which the
-// reference's median split refines a batch (RaySort.cpp:11-117).
+// 32-bit ray sort key: a five-dimensional Morton code of the origin (3 x 6
+// bits, in the batch origin box) and the direction (2 x 7 bits: the two minor
+// direction components divided by the dominant one, each in [-1,1]).  From
+// the top, each of six levels holds one bit of x, y, z, u, v (coarse to
+// fine), and the last two bits are the finest u, v bits; so every prefix of
+// the key refines origin and direction together, and a sort on its top bits
+// alone already groups rays that start close together and point the same
+// way.  Sorting by origin and direction is the order the reference's median
+// split refines a batch in (RaySort.cpp:11-117).
 MSC_HD uint32_t ray_sort_key(float3 o, float3 d, float3 lo, float3 scale) {
-  uint32_t qx = quantise(o.x, lo.x, scale.x, 64);
-  uint32_t qy = quantise(o.y, lo.y, scale.y, 64);
-  uint32_t qz = quantise(o.z, lo.z, scale.z, 64);
-  uint32_t om = (spread_bits_3(qx) << 2) | (spread_bits_3(qy) << 1) | spread_bits_3(qz);
-  int c = cardinal_bin(d) % 3;
-  float da = (c == 0) ? d.x : ((c == 1) ? d.y : d.z);
-  float du = (c == 0) ? d.y : ((c == 1) ? d.z : d.x);
-  float dv = (c == 0) ? d.z : ((c == 1) ? d.x : d.y);
-  float inv = 1.0f / fabsf(da);
-  uint32_t qu = quantise(du * inv, -1.0f, 64.0f, 128);
-  uint32_t qv = quantise(dv * inv, -1.0f, 64.0f, 128);
-  uint32_t dm = (spread_bits_2(qu) << 1) | spread_bits_2(qv);
-  return (om << 14) | (dm & 0x3fffu);
+  const uint32_t qx = quantise(o.x, lo.x, scale.x, 64);
+  const uint32_t qy = quantise(o.y, lo.y, scale.y, 64);
+  const uint32_t qz = quantise(o.z, lo.z, scale.z, 64);
+  const int c = cardinal_bin(d) % 3;
+  const float da = (c == 0) ? d.x : ((c == 1) ? d.y : d.z);
+  const float du = (c == 0) ? d.y : ((c == 1) ? d.z : d.x);
+  const float dv = (c == 0) ? d.z : ((c == 1) ? d.x : d.y);
+  const float inv = 1.0f / fabsf(da);
+  const uint32_t qu = quantise(du * inv, -1.0f, 64.0f, 128);
+  const uint32_t qv = quantise(dv * inv, -1.0f, 64.0f, 128);
+  uint32_t key = 0u;
+  for (int l = 0; l < 6; ++l) {
+    key = (key << 5) | (((qx >> (5 - l)) & 1u) << 4) | (((qy >> (5 - l)) & 1u) << 3) |
+          (((qz >> (5 - l)) & 1u) << 2) | (((qu >> (6 - l)) & 1u) << 1) | ((qv >> (6 - l)) & 1u);
+  }
+  return (key << 2) | ((qu & 1u) << 1) | (qv & 1u);
 }
 
 }  // namespace mscg

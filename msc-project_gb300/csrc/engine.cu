@@ -71,16 +71,6 @@ int upload_f4(const float* src, int n, int stride, int comps, float4** dst, floa
   return MSC_OK;
 }
 
-Segments one_segment(int start, int n) {
-  Segments s;
-  memset(&s, 0, sizeof(s));
-  s.start[0] = start;
-  s.prefix[0] = 0;
-  s.prefix[1] = n;
-  s.count = 1;
-  return s;
-}
-
 void fill_stats(const CoreStats& cs, double ms, msc_stats* out) {
   out->closest_queries = cs.closest;
   out->shadow_queries = cs.shadow;
@@ -587,46 +577,30 @@ int msc_stage_ray_bins(const float* dirs, int n, int nbins, int32_t* bins) {
 int msc_stage_ray_keys(const float* org, const float* dir, int n, uint32_t* keys) {
   if (n < 0 || (n > 0 && (!org || !dir || !keys))) return MSC_ERR_ARG;
   if (n == 0) return MSC_OK;
+  // the origin box of the given rays (RayBoundingbox.cpp:10-35)
+  float lo[3] = {org[0], org[1], org[2]}, hi[3] = {org[0], org[1], org[2]};
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], org[3 * i + a]);
+      hi[a] = std::max(hi[a], org[3 * i + a]);
+    }
+  float sc[3];
+  for (int a = 0; a < 3; ++a) {
+    const float e = hi[a] - lo[a];
+    sc[a] = e > 0.f ? 64.0f / e : 0.f;
+  }
   float4 *o = nullptr, *d = nullptr;
   uint32_t* mem = nullptr;
   int rc = MSC_OK;
   if (upload_f4(org, n, 3, 3, &o, 0.f) || upload_f4(dir, n, 3, 3, &d, 0.f)) rc = MSC_ERR_CUDA;
-  BatchPlan* plan = nullptr;
-  int* table = nullptr;
-  const int nchunks = (n + kChunk - 1) / kChunk;
-  if (rc == MSC_OK && cudaMalloc(&mem, (size_t)(n + 8) * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
-  if (rc == MSC_OK && cudaMalloc(&plan, sizeof(BatchPlan)) != cudaSuccess) rc = MSC_ERR_CUDA;
-  if (rc == MSC_OK && cudaMalloc(&table, (size_t)nchunks * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && cudaMalloc(&mem, (size_t)n * 4) != cudaSuccess) rc = MSC_ERR_CUDA;
   if (rc == MSC_OK) {
-    uint32_t* box = mem + n;
-    cudaMemset(box, 0xff, 12);
-    cudaMemset(box + 3, 0, 12);
-    // the input rays as bin 0 of a pool whose chunk table is the identity
-    std::vector<int> ht((size_t)nchunks);
-    for (int k = 0; k < nchunks; ++k) ht[k] = k;
-    cudaMemcpy(table, ht.data(), ht.size() * 4, cudaMemcpyHostToDevice);
-    BinPool pool;
-    pool.rays.o = o;
-    pool.rays.d = d;
-    pool.table = table;
-    pool.max_chunks = nchunks;
-    pool.nbins = 6;
-    BatchPlan hp;
-    memset(&hp, 0, sizeof(hp));
-    hp.seg = one_segment(0, n);
-    hp.nb = n;
-    hp.prefix_bits = 0;
-    hp.bin_bits = 3;
-    cudaMemcpy(plan, &hp, sizeof(hp), cudaMemcpyHostToDevice);
-    launch_origin_box(pool, plan, n, box, 0);
-    launch_ray_keys(pool, plan, n, box, mem, 0);
+    launch_ray_keys_direct(o, d, n, make_float3(lo[0], lo[1], lo[2]), make_float3(sc[0], sc[1], sc[2]), mem, 0);
     if (cudaMemcpy(keys, mem, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MSC_ERR_CUDA;
   }
   if (o) cudaFree(o);
   if (d) cudaFree(d);
   if (mem) cudaFree(mem);
-  if (plan) cudaFree(plan);
-  if (table) cudaFree(table);
   return rc;
 }
 

@@ -16,14 +16,6 @@ namespace {
 constexpr int TB = 256;
 inline int grid_for(int n, int tb = TB) { return (n + tb - 1) / tb; }
 
-__device__ __forceinline__ uint32_t f2ord(float f) {
-  uint32_t u = __float_as_uint(f);
-  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float ord2f(uint32_t u) {
-  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
-}
-
 // samples[i].rgb += v (one writer per sample within a batch, so no atomics)
 __device__ __forceinline__ void add_rgb(float4* p, float3 v) {
   float4 c = *p;
@@ -225,7 +217,8 @@ __global__ void __launch_bounds__(kBinRadix) k_part_reserve(const uint32_t* __re
 }
 
 __global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, const int* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ scanned, int tiles, BinPool pool) {
+                                                     const uint32_t* __restrict__ scanned, int tiles, BinPool pool,
+                                                     const SceneRec* __restrict__ scenes) {
   const int n = dev_count(n_max, n_dev);
   __shared__ RankSmem<PB, PRADIX> sm;
   __shared__ uint32_t sidx[kPartTile];
@@ -255,9 +248,16 @@ __global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, cons
     const int at = gofs[b] + (p - sm.tile_start[b]);
     if ((at >> kChunkShift) >= pool.held[b]) continue;  // no chunk reserved: reported by k_part_reserve
     const int o = pool_index(pool.table, pool.max_chunks, b, at);
-    pool.rays.o[o] = src.o[s];
-    pool.rays.d[o] = src.d[s];
+    const float4 ro = src.o[s], rd = src.d[s];
+    pool.rays.o[o] = ro;
+    pool.rays.d[o] = rd;
     pool.rays.w[o] = src.w[s];
+    if (scenes) {  // the ray sort key, in the ray's scene box
+      const int sc = info_scene(__float_as_int(rd.w));
+      const float4 lo = scenes[sc].key_lo, sca = scenes[sc].key_scale;
+      const uint32_t k = ray_sort_key(f3(ro), f3(rd), f3(lo), f3(sca));
+      pool.keys[o] = (k & ~0xffu) | (uint32_t)sc;
+    }
   }
 }
 
@@ -303,7 +303,7 @@ __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict_
 // ties to the lower bin), thread 0 then walks the ranks.  Every bin of the
 // pool is a candidate, so rays of a bin function used before a retune drain too.
 __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap, int merge, int scene_bits,
-                                                    BatchPlan* plan, uint32_t* box6, Counters* ctr) {
+                                                    BatchPlan* plan, Counters* ctr) {
   __shared__ int cnt[kMaxBins];
   __shared__ int by_rank[kMaxBins];
   __shared__ int f_bin[kMaxBins], f_keep[kMaxBins], f_held[kMaxBins], f_ofs[kMaxBins + 1];
@@ -354,10 +354,6 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
     plan->bin_bits = bb;
     plan->prefix_bits = (nsg > 1 || scene_bits > 0) ? scene_bits + bb : 0;
     *pool.in_bins -= nb;
-    for (int a = 0; a < 3; ++a) {
-      box6[a] = 0xffffffffu;
-      box6[3 + a] = 0u;
-    }
     ctr->closest += (unsigned long long)nb;
     ctr->batches += nb > 0 ? 1ull : 0ull;
   }
@@ -370,66 +366,40 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
 }
 
 // ------------------------------------------------------------ ray keys
-// RayBoundingbox (src/core/RayBoundingbox.cpp:5-50): origin box of the batch.
-__global__ void __launch_bounds__(TB) k_origin_box(const float4* __restrict__ o, const int* __restrict__ table,
-                                                   int max_chunks, const BatchPlan* __restrict__ plan,
-                                                   uint32_t* box6) {
-  __shared__ Segments seg;
-  __shared__ float red[TB / 32][6];
-  load_segments(plan, seg);
-  const int n = plan->nb;
-  float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float4 p = o[seg_source(seg, table, max_chunks, i)];
-    mn[0] = fminf(mn[0], p.x); mn[1] = fminf(mn[1], p.y); mn[2] = fminf(mn[2], p.z);
-    mx[0] = fmaxf(mx[0], p.x); mx[1] = fmaxf(mx[1], p.y); mx[2] = fmaxf(mx[2], p.z);
-  }
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-    for (int s = 16; s > 0; s >>= 1) {
-      mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], s));
-      mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], s));
-    }
-  const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-    for (int a = 0; a < 3; ++a) {
-      red[warp][a] = mn[a];
-      red[warp][3 + a] = mx[a];
-    }
-  __syncthreads();
-  if (threadIdx.x < 6) {  // one atomic per block and component
-    const int a = threadIdx.x;
-    float v = red[0][a];
-    for (int w = 1; w < TB / 32; ++w) v = a < 3 ? fminf(v, red[w][a]) : fmaxf(v, red[w][a]);
-    if (a < 3) atomicMin(&box6[a], f2ord(v));
-    else atomicMax(&box6[a], f2ord(v));
-  }
-}
-
-__global__ void __launch_bounds__(TB) k_ray_keys(const float4* __restrict__ o, const float4* __restrict__ d,
-                                                 const int* __restrict__ table, int max_chunks, int nbins,
-                                                 const BatchPlan* __restrict__ plan,
-                                                 const uint32_t* __restrict__ box6, uint32_t* __restrict__ keys) {
+// Sort keys of the batch rays: the key each ray got when it was binned (its
+// scene's box in place of the reference's per-batch origin box,
+// RayBoundingbox.cpp:5-50), under (scene, direction bin) when the batch
+// spans several; the bin is the run's, the scene sits in the key's low byte.
+__global__ void __launch_bounds__(TB) k_ray_keys(const uint32_t* __restrict__ pool_keys, const int* __restrict__ table,
+                                                 int max_chunks, const BatchPlan* __restrict__ plan, int key_bits,
+                                                 uint32_t* __restrict__ keys) {
   __shared__ Segments seg;
   const int n = plan->nb;
   if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole block
   load_segments(plan, seg);
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  int lo = 0, hi = seg.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg.prefix[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  const int bin = seg.bin[lo];
+  const uint32_t pk = pool_keys[pool_index(table, max_chunks, bin, seg.start[lo] + (i - seg.prefix[lo]))];
+  uint32_t key = pk & ~0xffu;
   const int prefix_bits = plan->prefix_bits;
-  const int src = seg_source(seg, table, max_chunks, i);
-  float3 lo = f3(ord2f(box6[0]), ord2f(box6[1]), ord2f(box6[2]));
-  float3 hi = f3(ord2f(box6[3]), ord2f(box6[4]), ord2f(box6[5]));
-  float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
-  float3 sc = f3(ex > 0.f ? 64.0f / ex : 0.f, ey > 0.f ? 64.0f / ey : 0.f, ez > 0.f ? 64.0f / ez : 0.f);
-  const float4 dd = d[src];
-  uint32_t key = ray_sort_key(f3(o[src]), f3(dd), lo, sc);
   if (prefix_bits > 0) {
-    const uint32_t prefix = ((uint32_t)info_scene(__float_as_int(dd.w)) << plan->bin_bits) |
-                            (uint32_t)ray_bin(f3(dd), nbins);
+    const uint32_t prefix = ((pk & 0xffu) << plan->bin_bits) | (uint32_t)bin;
     key = (prefix << (32 - prefix_bits)) | (key >> prefix_bits);
   }
-  keys[i] = key;
+  keys[i] = key >> (32 - key_bits);
+}
+
+__global__ void __launch_bounds__(TB) k_ray_keys_direct(const float4* __restrict__ o, const float4* __restrict__ d,
+                                                        int n, float3 lo, float3 scale, uint32_t* __restrict__ keys) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) keys[i] = ray_sort_key(f3(o[i]), f3(d[i]), lo, scale);
 }
 
 // RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
@@ -1121,7 +1091,8 @@ int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBu
   return 1;
 }
 
-int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev) {
+int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev,
+                         const SceneRec* scenes) {
   if (n <= 0) return 0;
   const int tiles = (n + kPartTile - 1) / kPartTile;
   k_part_count<<<tiles, PB, 0, s>>>(src.d, n, n_dev, pool.nbins, pool.tile_counts, tiles);
@@ -1129,7 +1100,7 @@ int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s
   // difference of two scanned row starts
   k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * (pool.nbins + 1), nullptr);
   k_part_reserve<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
-  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, n_dev, pool.tile_counts, tiles, pool);
+  k_part_scatter<<<tiles, PB, 0, s>>>(src, n, n_dev, pool.tile_counts, tiles, pool, pool.keys ? scenes : nullptr);
   k_part_commit<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
   return 5;
 }
@@ -1152,23 +1123,23 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
   return 1;
 }
 
-int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
-                Counters* ctr, cudaStream_t s) {
-  k_plan<<<1, kBinRadix, 0, s>>>(pool, batch_cap, merge, scene_bits, plan, box6, ctr);
+int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, Counters* ctr,
+                cudaStream_t s) {
+  k_plan<<<1, kBinRadix, 0, s>>>(pool, batch_cap, merge, scene_bits, plan, ctr);
   return 1;
 }
 
-int launch_origin_box(const BinPool& pool, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s) {
-  if (n_max <= 0) return 0;
-  k_origin_box<<<std::min(grid_for(n_max), 512), TB, 0, s>>>(pool.rays.o, pool.table, pool.max_chunks, plan, box6);
-  return 1;
-}
-
-int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* box6, uint32_t* keys,
+int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
                     cudaStream_t s) {
   if (n_max <= 0) return 0;
-  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.rays.o, pool.rays.d, pool.table, pool.max_chunks, pool.nbins, plan,
-                                            box6, keys);
+  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.keys, pool.table, pool.max_chunks, plan, key_bits, keys);
+  return 1;
+}
+
+int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, float3 scale, uint32_t* keys,
+                           cudaStream_t s) {
+  if (n <= 0) return 0;
+  k_ray_keys_direct<<<grid_for(n), TB, 0, s>>>(o, d, n, lo, scale, keys);
   return 1;
 }
 

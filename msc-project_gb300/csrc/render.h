@@ -68,6 +68,8 @@ struct SceneRec {        // one resident scene
   const int4* tex_images;
   const float4* tex_texels;
   const float* tri_uv;   // 6 per original triangle: uv of v0, v1, v2
+  float4 key_lo;         // ray sort key: the scene box's low corner
+  float4 key_scale;      // and 64 / its extent per axis (0 for a flat axis)
 };
 
 // Texture coordinate of a hit (PolygonObject::texture, src/core/PolygonObject.cpp:45-63).
@@ -156,6 +158,8 @@ struct BinPool {
   int* free_stack = nullptr; // device [num_chunks]
   int* free_top = nullptr;   // device: entries on the free stack
   int* in_bins = nullptr;    // device: rays held in all bins
+  uint32_t* keys = nullptr;  // device [num_chunks * kChunk]: ray sort key of each held ray
+                             // (top 24 bits of ray_sort_key, the ray's scene in the low byte)
   uint32_t* tile_counts = nullptr;  // partition scratch ((kMaxBins + 1) * tiles)
   int max_tiles = 0;
   int* err = nullptr;
@@ -174,25 +178,28 @@ constexpr int kPartTile = 2048;
 // Stable partition of src[0, n) by direction bin, appended behind each bin's
 // current content; dead rays (info < 0) are dropped.
 // n_dev (optional): the count is read on the device, n is then its upper bound.
-int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev = nullptr);
+// scenes (optional): also store each ray's sort key (pool.keys) for the ray sort.
+int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev = nullptr,
+                         const SceneRec* scenes = nullptr);
 
 // The next batch from the bins: the fullest bin's top, topped up from the
 // next fullest while merge is set (the order of the host's choice before).
-// Also opens the batch: origin box reset, shadow count zeroed, counters.
-int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, uint32_t* box6,
-                Counters* ctr, cudaStream_t s);
+// Also opens the batch: shadow count zeroed, counters.
+int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, Counters* ctr,
+                cudaStream_t s);
 // Direction bin of each direction (6, 26 or 98 bins).
 int launch_ray_bins(const float4* d, int n, int nbins, int* out, cudaStream_t s);
 
 // Per-ray cardinal bin only (stage test).
 int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 
-// Origin box of the batch rays into box6 (ordered-int min xyz, max xyz; caller initialises).
-// n_max bounds the plan's batch size (grid size).
-int launch_origin_box(const BinPool& pool, const BatchPlan* plan, int n_max, uint32_t* box6, cudaStream_t s);
-// 32-bit keys; prefix_bits > 0 puts (scene << 3 | cardinal bin) above the origin/direction code.
-int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* box6, uint32_t* keys,
+// Sort keys of the batch rays from pool.keys: (scene, direction bin) above the
+// key when prefix_bits > 0; only the top key_bits bits are kept (shifted down).
+int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
                     cudaStream_t s);
+// ray_sort_key of n rays (o, d as float4) in the origin box lo + [0, 64 / scale).
+int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, float3 scale, uint32_t* keys,
+                           cudaStream_t s);
 int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
                   cudaStream_t s);
 

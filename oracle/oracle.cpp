@@ -1433,18 +1433,8 @@ int render_full(oracle_scene* S, int iteration, int threads, T* rgb, T* xy, T* p
   return 0;
 }
 
-// 32-bit origin/direction ray key (quantised origin Morton above quantised
-// minor-direction Morton), the device key's restatement.
-uint32_t spread3(uint32_t v) {
-  uint32_t r = 0;
-  for (int b = 0; b < 10; ++b) r |= ((v >> b) & 1u) << (3 * b);
-  return r;
-}
-uint32_t spread2(uint32_t v) {
-  uint32_t r = 0;
-  for (int b = 0; b < 16; ++b) r |= ((v >> b) & 1u) << (2 * b);
-  return r;
-}
+// Quantisation of the 32-bit origin/direction ray key (oracle_ray_keys), the
+// device key's restatement.
 uint32_t quant(float v, float lo, float sc, int cells) {
   int i = (int)std::floor((v - lo) * sc);
   return (uint32_t)std::min(std::max(i, 0), cells - 1);
@@ -1564,14 +1554,21 @@ void oracle_ray_keys(const float* org, const float* dir, int n, uint32_t* keys) 
   for (int i = 0; i < n; ++i) {
     const float* o = org + 3 * i;
     const float* d = dir + 3 * i;
-    uint32_t om = (orc::spread3(orc::quant(o[0], lo[0], sc[0], 64)) << 2) | (orc::spread3(orc::quant(o[1], lo[1], sc[1], 64)) << 1) |
-                  orc::spread3(orc::quant(o[2], lo[2], sc[2], 64));
+    // five-dimensional Morton code, six levels of (x, y, z, u, v) bits from the
+    // top, then the finest u, v bits
+    const uint32_t q[3] = {orc::quant(o[0], lo[0], sc[0], 64), orc::quant(o[1], lo[1], sc[1], 64),
+                           orc::quant(o[2], lo[2], sc[2], 64)};
     int c = orc::cardinal(d[0], d[1], d[2]) % 3;
     float da = d[c], du = d[(c + 1) % 3], dv = d[(c + 2) % 3];
     float inv = 1.0f / std::fabs(da);
     uint32_t qu = orc::quant(du * inv, -1.0f, 64.0f, 128), qv = orc::quant(dv * inv, -1.0f, 64.0f, 128);
-    uint32_t dm = (orc::spread2(qu) << 1) | orc::spread2(qv);
-    keys[i] = (om << 14) | (dm & 0x3fffu);
+    uint32_t key = 0;
+    for (int l = 0; l < 6; ++l) {
+      for (int a = 0; a < 3; ++a) key = (key << 1) | ((q[a] >> (5 - l)) & 1u);
+      key = (key << 1) | ((qu >> (6 - l)) & 1u);
+      key = (key << 1) | ((qv >> (6 - l)) & 1u);
+    }
+    keys[i] = (key << 2) | ((qu & 1u) << 1) | (qv & 1u);
   }
 }
 
