@@ -210,7 +210,22 @@ __global__ void __launch_bounds__(kBinRadix) k_part_reserve(const uint32_t* __re
   if (total > top && b == 0) atomicOr(pool.err, ERR_BIN_OVERFLOW);
   const int base = top - min(total, top);
   const int h0 = b < pool.nbins ? pool.held[b] : 0;
-  for (int i = 0; i < give; ++i) pool.table[b * pool.max_chunks + h0 + i] = pool.free_stack[base + ofs + i];
+  // the chunks handed out form one run [base, base + min(total, top)) of the
+  // stack, bin b's part starting at its offset: the whole block copies them
+  __shared__ int s_ofs[kBinRadix], s_h0[kBinRadix];
+  s_ofs[b] = ofs;
+  s_h0[b] = h0;
+  __syncthreads();
+  const int given = min(total, top);
+  for (int x = b; x < given; x += kBinRadix) {
+    int lo = 0, hi = kBinRadix - 1;  // the last bin whose offset is <= x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_ofs[mid] <= x) lo = mid;
+      else hi = mid - 1;
+    }
+    pool.table[lo * pool.max_chunks + s_h0[lo] + (x - s_ofs[lo])] = pool.free_stack[base + x];
+  }
   if (b < pool.nbins) pool.held[b] = h0 + give;
   __syncthreads();
   if (b == 0) *pool.free_top = base;
