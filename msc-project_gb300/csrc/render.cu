@@ -689,6 +689,9 @@ __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z)
 
 // Integrator::operator() (src/core/Integrator.cpp:12-255), one hit per thread.
 // job_done[j] counts the finished paths of job j.
+constexpr int kShadowGroups = 64;  // two per lane of one warp in the group scan
+static_assert(kShadowGroups == 64 && TB >= kShadowGroups, "the shadow group scan takes one warp");
+
 __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
                                               Film film, RayBuf batch, const float4* __restrict__ hits,
                                               const uint32_t* __restrict__ order, int n_max,
@@ -699,7 +702,7 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
   if (blockIdx.x * blockDim.x >= n) return;  // whole block past the batch
   const bool live = j < n;
   bool emit = false, cont = false;
-  int job = -1;
+  int job = -1, light = 0;
   float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sd = so, scol = so;
   float4 no = so, nd = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), nw = so;
   if (live) {
@@ -819,6 +822,7 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
               const float k0 = (mis * e.cos_theta) / a;
               const float3 c = f3(k0 * (le * e.f.x), k0 * (le * e.f.y), k0 * (le * e.f.z));
               emit = true;
+              light = li;
               so = make_float4(pos.x, pos.y, pos.z, dist);
               sd = make_float4(wi.x, wi.y, wi.z, __int_as_float((int)sample));
               scol = make_float4(c.x * w.x, c.y * w.y, c.z * w.z, __int_as_float(scene));
@@ -869,15 +873,35 @@ __global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scene
     }
   }
   const int lane = threadIdx.x & 31;
-  // warp-aggregated append of shadow rays
-  const unsigned m = __ballot_sync(0xffffffffu, emit);
-  if (m) {
-    const int leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(sh_count, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
+  // the block's shadow rays are appended grouped by light (a block-wide
+  // counting sort on the light index modulo kShadowGroups; the order inside a
+  // group does not matter), so the occlusion kernel's warps trace rays from
+  // one neighbourhood toward one light
+  {
+    __shared__ int grp[kShadowGroups];
+    if (threadIdx.x < kShadowGroups) grp[threadIdx.x] = 0;
+    __syncthreads();
+    const int g = light & (kShadowGroups - 1);
+    const int rank = emit ? atomicAdd(&grp[g], 1) : 0;
+    __syncthreads();
+    if (threadIdx.x < 32) {  // exclusive scan of the group counts, two per lane
+      const int a = grp[2 * lane], b = grp[2 * lane + 1];
+      int incl = a + b;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      int base = 0;
+      if (lane == 0 && total > 0) base = atomicAdd(sh_count, total);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      grp[2 * lane] = base + incl - a - b;
+      grp[2 * lane + 1] = base + incl - b;
+    }
+    __syncthreads();
     if (emit) {
-      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      const int slot = grp[g] + rank;
       sh.o[slot] = so;
       sh.d[slot] = sd;
       sh.c[slot] = scol;
