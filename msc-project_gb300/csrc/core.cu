@@ -1051,6 +1051,7 @@ int Core::run_all(const volatile bool* stop) {
   }
   CK(cudaStreamSynchronize(stream_));
   CK(cudaGetLastError());
+  if (profiling) harvest();  // the stages after the last step (the jobs' filters)
   return MSC_OK;
 }
 

@@ -692,7 +692,7 @@ __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z)
 constexpr int kShadowGroups = 64;  // two per lane of one warp in the group scan
 static_assert(kShadowGroups == 64 && TB >= kShadowGroups, "the shadow group scan takes one warp");
 
-__global__ void __launch_bounds__(TB) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
+__global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
                                               Film film, RayBuf batch, const float4* __restrict__ hits,
                                               const uint32_t* __restrict__ order, int n_max,
                                               const int* __restrict__ n_dev, RayBuf next, ShadowBuf sh,
@@ -1078,8 +1078,8 @@ __global__ void __launch_bounds__(128) k_occluded(BvhRef bvh, const float4* __re
 // at a time with coalesced loads, stored sample-major (padded) so that each
 // thread then reads its pixel's samples without bank conflicts.  Every pixel
 // sums exactly the terms, in exactly the order, of the reference's loop.
-constexpr int kFilterRows = 128;
-constexpr int kFilterChunk = 8;
+constexpr int kFilterRows = 32;
+constexpr int kFilterChunk = 32;
 
 __global__ void __launch_bounds__(kFilterRows) k_filter_tent(JobRec f, Film film) {
   __shared__ float4 s_rgb[kFilterChunk][kFilterRows + 1];
