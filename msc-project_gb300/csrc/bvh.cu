@@ -7,6 +7,9 @@
 // forming its box -> treelet restructuring rounds (SAH) -> pack into the
 // traversal layout of trace.cuh.
 #include <algorithm>
+#include <array>
+#include <functional>
+#include <limits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -371,6 +374,10 @@ size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // octant o that visits slots o ^ 0, o ^ 1, ..., o ^ 7 meets the children
 // roughly front to back without sorting them.
 constexpr int kWideLeafMax = 2;
+// SAH weights of the collapse: a wide-node visit (eight box tests), and one
+// triangle test relative to it (0.6 measured best of 0.15, 0.3 and 0.6).
+constexpr float kCollapseNode = 1.0f;
+constexpr float kCollapseTri = 0.6f;
 // a node's triangle bits (eight slots of at most kWideLeafMax) fit one word
 static_assert(8 * kWideLeafMax <= 32, "triangle bits of a node must fit one word");
 
@@ -428,9 +435,72 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
     const int cl = c.x < 0 ? 1 : count[c.x], cr = c.y < 0 ? 1 : count[c.y];
     count[b] = cl + cr;
   }
-  auto is_leafish = [&](int c) { return c < 0 || count[c] <= kWideLeafMax; };
   auto box_lo = [&](int c) { return c < 0 ? lbox[2 * (~c)] : nbox[2 * c]; };
   auto box_hi = [&](int c) { return c < 0 ? lbox[2 * (~c) + 1] : nbox[2 * c + 1]; };
+  // SAH-optimal collapse (Ylitie, Karras and Laine, HPG 2017), children before
+  // parents: cost[b][i-1] is the least SAH cost of covering b's subtree with at
+  // most i roots, each a leaf slot (at most kWideLeafMax triangles) or a wide
+  // node; split[b][i-1] is the number of roots the left child gets in the best
+  // split into exactly i (0: fewer roots are cheaper); leaf[b] marks a subtree
+  // that is cheapest as one leaf slot.
+  std::vector<std::array<float, 8>> cost((size_t)(n - 1));
+  std::vector<std::array<uint8_t, 8>> split((size_t)(n - 1));
+  std::vector<uint8_t> leaf((size_t)(n - 1), 0);
+  auto child_cost = [&](int c, int i) {  // a triangle is one leaf slot at any i
+    if (c < 0) {
+      const float4 lo = lbox[2 * (~c)], hi = lbox[2 * (~c) + 1];
+      return kCollapseTri * surface(lo, hi);
+    }
+    return cost[c][i - 1];
+  };
+  for (size_t q = bfs.size(); q-- > 0;) {
+    const int b = bfs[q];
+    const int l = ch[b].x, r = ch[b].y;
+    float dist[9];
+    int dsplit[9];
+    for (int j = 2; j <= 8; ++j) {
+      dist[j] = std::numeric_limits<float>::infinity();
+      dsplit[j] = 1;
+      for (int k = 1; k < j; ++k) {
+        const float c = child_cost(l, k) + child_cost(r, j - k);
+        if (c < dist[j]) { dist[j] = c; dsplit[j] = k; }
+      }
+    }
+    const float area = surface(nbox[2 * b], nbox[2 * b + 1]);
+    float best_dist = dist[2];
+    for (int j = 3; j <= 8; ++j) best_dist = std::min(best_dist, dist[j]);
+    const float c_int = kCollapseNode * area + best_dist;
+    const float c_leaf = count[b] <= kWideLeafMax ? kCollapseTri * area * (float)count[b]
+                                                   : std::numeric_limits<float>::infinity();
+    leaf[b] = c_leaf <= c_int ? 1 : 0;
+    cost[b][0] = std::min(c_leaf, c_int);
+    split[b][0] = 0;
+    for (int i = 2; i <= 8; ++i) {
+      if (dist[i] < cost[b][i - 2]) {
+        cost[b][i - 1] = dist[i];
+        split[b][i - 1] = (uint8_t)dsplit[i];
+      } else {
+        cost[b][i - 1] = cost[b][i - 2];
+        split[b][i - 1] = 0;
+      }
+    }
+  }
+  // the roots covering subtree c with at most i of them, per the decisions
+  std::function<void(int, int, int*, int*)> roots = [&](int c, int i, int* C, int* k) {
+    if (c < 0 || i == 1) {
+      C[(*k)++] = c;
+      return;
+    }
+    while (i > 1 && split[c][i - 1] == 0) --i;
+    if (i == 1) {
+      C[(*k)++] = c;
+      return;
+    }
+    const int kl = split[c][i - 1];
+    roots(ch[c].x, kl, C, k);
+    roots(ch[c].y, i - kl, C, k);
+  };
+  auto is_leafish = [&](int c) { return c < 0 || leaf[c] != 0; };
   out->words.clear();
   out->tri_perm.clear();
   out->tri_perm.reserve(n);
@@ -441,22 +511,17 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
     const int b = queue[w];
     int C[8];
     int k = 0;
-    C[k++] = ch[b].x;
-    C[k++] = ch[b].y;
-    while (k < 8) {
-      int best = -1;
-      float best_area = -1.f;
-      for (int i = 0; i < k; ++i) {
-        if (is_leafish(C[i])) continue;
-        float a = surface(nbox[2 * C[i]], nbox[2 * C[i] + 1]);
-        if (a > best_area) { best_area = a; best = i; }
-      }
-      if (best < 0) break;
-      int c = C[best];
-      for (int j = k; j > best + 1; --j) C[j] = C[j - 1];
-      C[best] = ch[c].x;
-      C[best + 1] = ch[c].y;
-      ++k;
+    {  // the best split of b into 2..8 roots
+      const int l = ch[b].x, r = ch[b].y;
+      float best = std::numeric_limits<float>::infinity();
+      int bj = 2, bk = 1;
+      for (int j = 2; j <= 8; ++j)
+        for (int kk = 1; kk < j; ++kk) {
+          const float c = child_cost(l, kk) + child_cost(r, j - kk);
+          if (c < best) { best = c; bj = j; bk = kk; }
+        }
+      roots(l, bk, C, &k);
+      roots(r, bj - bk, C, &k);
     }
     const float4 lo = nbox[2 * b], hi = nbox[2 * b + 1];
     // octant slots: greedy assignment of (child, slot) pairs by increasing
