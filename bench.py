@@ -77,7 +77,14 @@ class ClockSampler:
         for line in self._proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append((time.time(), parts))
+
+    def wait_first(self, timeout=10.0):
+        """Waits (bounded) until nvidia-smi delivers its first sample, so that its
+        start-up does not fall inside a timed region."""
+        end = time.time() + timeout
+        while self._proc and not self.samples and time.time() < end:
+            time.sleep(0.05)
 
     def stop(self):
         if self._proc:
@@ -87,15 +94,19 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self._proc.kill()
 
-    def summary(self):
-        if not self.samples:
+    def summary(self, t0=None, t1=None):
+        """Samples taken in [t0, t1] (the timed region; the next sample after it
+        covers its end), else all of them."""
+        picked = [p for (t, p) in self.samples if t0 is not None and t0 <= t <= t1 + 0.25]
+        samples = picked if picked else [p for (_, p) in self.samples]
+        if not samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        sm = [float(s[0]) for s in samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for s in samples for i in range(4) if s[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(samples)}
 
 
 def measured_peaks():
@@ -434,10 +445,14 @@ def main():
             pt.process_device()
             tuning_passes += 1
         log("autotuner settled after %d passes: %s" % (tuning_passes, pt.tuning()))
-    for _ in range(args.warmup):
-        pt.process_device()
+    # the clock sampler starts before the warm-up, so that nvidia-smi's own
+    # start-up stays out of the timed region
     clocks = ClockSampler()
     clocks.start()
+    for _ in range(args.warmup):
+        pt.process_device()
+    clocks.wait_first()
+    t_timed = time.time()
     dev_ms, wall, rays, launches = [], [], 0, 0
     for _ in range(args.steps):
         t = time.time()
@@ -457,6 +472,7 @@ def main():
         st = pt.stats()
         e2e_rays += st["closest_queries"] + st["shadow_queries"]
         batches += st["batches"]
+    t_timed_end = time.time()
     clocks.stop()
     # one profiled pass for the per-stage split (not part of the timed numbers)
     pt.set_profiling(True)
@@ -490,7 +506,7 @@ def main():
            "e2e": {"value": e2e_rays / sum(e2e_wall) / 1e6, "unit": "Mrays/s",
                    "h2d_bytes_per_step": int(24 * batches / args.steps),
                    "d2h_bytes_per_step": int(img.nbytes + 32 * batches / args.steps)},
-           "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks.summary(),
+           "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks.summary(t_timed, t_timed_end),
            "wall_ms_per_step": 1e3 * sum(wall) / args.steps}
     out["batches_per_step"] = batches / args.steps
     if not args.no_forms:
