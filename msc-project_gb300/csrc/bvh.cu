@@ -182,7 +182,7 @@ __global__ void k_refit(const int2* __restrict__ children, const int* __restrict
 // found by dynamic programming over their 127 subsets and replaces the
 // treelet when it is cheaper, reusing the treelet's 6 internal nodes.  One
 // thread per treelet; a round is one bottom-up pass.
-constexpr int kTreeletRounds = 3;
+constexpr int kTreeletRounds = 6;
 constexpr float kCostNode = 1.2f;  // SAH cost of a node visit relative to a triangle test
 constexpr float kCostTri = 1.0f;
 

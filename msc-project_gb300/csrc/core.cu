@@ -14,8 +14,11 @@ namespace {
 // Bits of the ray sort key the batch sort orders by (the top ones): a ray's
 // order within a batch only shapes traversal coherence, and the top 16 bits
 // of the interleaved key (three levels of origin and direction under the
-// bin) carry nearly all of it in two sort passes instead of four.
+// bin) carry nearly all of it in two sort passes instead of four.  With
+// several resident scenes the (scene, bin) prefix takes more of the key, so
+// the sort keeps 24 bits.
 constexpr int kRayKeyBits = 16;
+constexpr int kRayKeyBitsScenes = 24;
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -710,10 +713,11 @@ int Core::enqueue_batch(int index, bool overlap) {
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      t.done(launch_ray_keys(bins_, plan_, B, kRayKeyBits, keys_, st));
+      t.done(launch_ray_keys(bins_, plan_, B, ns > 1 ? kRayKeyBitsScenes : kRayKeyBits, keys_, st));
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, kRayKeyBits, ss_, st, errw, nb, sort_digits);
+    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, ns > 1 ? kRayKeyBitsScenes : kRayKeyBits, ss_,
+                             st, errw, nb, sort_digits);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;
