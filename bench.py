@@ -423,7 +423,7 @@ def main():
            "triangles": info["triangles"], "lights": info["lights"],
            "batch": 1 << (20 if args.config == 1 else 16), "seed": SEED + args.config,
            "l2": "inputs larger than L2 (129 MB): BVH + triangles ~0.25 GB, sample film 1.6 GB, ray pool up to "
-                 "1.6 GB, batch buffers ~1.7 GB, all read or written every step"}
+                 "1.6 GB, batch buffers ~1.3 GB, all read or written every step"}
     if args.impl == "reference":
         run_reference(args, yaml, cfg)
         return
@@ -503,6 +503,7 @@ def main():
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
            "latency_ms": {"p50": statistics.median(lat), "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+           "step_ms": [round(x, 3) for x in dev_ms],
            "e2e": {"value": e2e_rays / sum(e2e_wall) / 1e6, "unit": "Mrays/s",
                    "h2d_bytes_per_step": int(24 * batches / args.steps),
                    "d2h_bytes_per_step": int(img.nbytes + 32 * batches / args.steps)},

@@ -186,7 +186,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   size_t bytes = 3 * al256(pool_rays * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
                  2 * al256((size_t)kMaxBins * 4) + al256((size_t)kMaxBins * max_chunks * 4) + al256(chunks * 4) +
                  al256(4) +
-                 3 * al256((size_t)B * sizeof(float4)) + 9 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
+                 10 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(pool_rays * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B, 11) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
@@ -206,9 +206,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   staging_.o = A.take<float4>(S);
   staging_.d = A.take<float4>(S);
   staging_.w = A.take<float4>(S);
-  batch_.o = A.take<float4>(B);
-  batch_.d = A.take<float4>(B);
-  batch_.w = A.take<float4>(B);
+  slots_ = A.take<int>(B);
   keys_ = A.take<uint32_t>(B);
   keys_sorted_ = A.take<uint32_t>(B);
   perm_ = A.take<uint32_t>(B);
@@ -727,11 +725,16 @@ int Core::enqueue_batch(int index, bool overlap) {
   }
   {
     StageClock t(this, MSC_STAGE_GATHER);
-    t.done(launch_gather(bins_, plan_, B, perm, batch_, st));
+    // traversal and shading read the batch's rays where the bins hold them
+    // (RayDecompress, RayDecompress.cpp:5-29, needs no copy here), through
+    // the pool index of each ray in sorted order
+    t.done(launch_batch_slots(bins_, plan_, B, perm, slots_, st));
   }
+  const RayBuf& rays = bins_.rays;
+  const int* slots = slots_;
   {
     StageClock t(this, MSC_STAGE_TRACE);
-    t.done(launch_trace_closest(d_scenes_, ns, s0, batch_.o, batch_.d, B, hits_, errw, st, nb, trace_block,
+    t.done(launch_trace_closest(d_scenes_, ns, s0, rays.o, rays.d, slots, B, hits_, errw, st, nb, trace_block,
                                 persistent_trace ? trace_counter_ : nullptr));
   }
   const uint32_t* order = nullptr;
@@ -750,7 +753,7 @@ int Core::enqueue_batch(int index, bool overlap) {
     order = hperm_;
   } else if (hit_sort) {
     StageClock t(this, MSC_STAGE_HITSORT);
-    int l = launch_hit_keys(d_scenes_, batch_.d, hits_, B, hkeys_, st, nb);
+    int l = launch_hit_keys(d_scenes_, rays.d, slots, hits_, B, hkeys_, st, nb);
     const int ls = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, B, hit_bits_, ss_, st, errw, nb, sort_digits);
     if (ls < 0) {
       err = "internal: hit sort without distinct outputs";
@@ -763,7 +766,7 @@ int Core::enqueue_batch(int index, bool overlap) {
   {
     StageClock t(this, MSC_STAGE_SHADE);
     CK(cudaMemsetAsync(shc, 0, sizeof(int), st));
-    t.done(launch_shade(d_scenes_, d_jobs_, film_, batch_, hits_, order, B, staging_, shadow_[q], shc, d_job_done_,
+    t.done(launch_shade(d_scenes_, d_jobs_, film_, rays, slots, hits_, order, B, staging_, shadow_[q], shc, d_job_done_,
                         st, nb));
   }
   {
@@ -1072,7 +1075,7 @@ int Core::trace_closest(const float* org, const float* dir, int n, float4* hits_
   CK(cudaMemset(e, 0, sizeof(int)));
   CK(cudaMemcpy(dev, o.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(dev + n, d.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice));
-  launch_trace_closest(d_scenes_, 1, scenes_[0]->rec, dev, dev + n, n, dev + 2 * n, e, 0);
+  launch_trace_closest(d_scenes_, 1, scenes_[0]->rec, dev, dev + n, nullptr, n, dev + 2 * n, e, 0);
   int he = 0;
   CK(cudaMemcpy(hits_host, dev + 2 * n, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(&he, e, sizeof(int), cudaMemcpyDeviceToHost));

@@ -200,11 +200,12 @@ class Core {
   // wavefront buffers
   char* arena_ = nullptr;
   BinPool bins_;
-  RayBuf staging_, batch_;
+  RayBuf staging_;
   uint32_t *keys_ = nullptr, *keys_sorted_ = nullptr, *perm_ = nullptr, *hkeys_ = nullptr, *hkeys_sorted_ = nullptr,
            *hperm_ = nullptr, *hhi_ = nullptr, *hhi_g_ = nullptr, *hperm1_ = nullptr;
   SortScratch ss_;
   float4* hits_ = nullptr;
+  int* slots_ = nullptr;  // pool index of each batch ray (sorted order)
   ShadowBuf shadow_[2];          // shadow queues, alternating between batches
   cudaStream_t side_ = nullptr;  // occlusion of batch k runs here beside batch k+1's front part
   static constexpr int kGraphBodies = 4;

@@ -417,20 +417,18 @@ __global__ void __launch_bounds__(TB) k_ray_keys_direct(const float4* __restrict
   if (i < n) keys[i] = ray_sort_key(f3(o[i]), f3(d[i]), lo, scale);
 }
 
-// RayDecompress (src/core/RayDecompress.cpp:5-29) folded into the sorted gather.
-__global__ void __launch_bounds__(TB) k_gather(RayBuf src, const int* __restrict__ table, int max_chunks,
-                                               const BatchPlan* __restrict__ plan,
-                                               const uint32_t* __restrict__ perm, RayBuf dst) {
+// Pool index of each batch ray, in sorted order (perm, when given): the
+// traversal and shading read the rays where the bins hold them.
+__global__ void __launch_bounds__(TB) k_batch_slots(const int* __restrict__ table, int max_chunks,
+                                                    const BatchPlan* __restrict__ plan,
+                                                    const uint32_t* __restrict__ perm, int* __restrict__ slots) {
   __shared__ Segments seg;
   const int n = plan->nb;
   if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole block
   load_segments(plan, seg);
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  const int i = seg_source(seg, table, max_chunks, perm ? (int)perm[j] : j);
-  dst.o[j] = src.o[i];
-  dst.d[j] = src.d[i];
-  dst.w[j] = src.w[i];
+  slots[j] = seg_source(seg, table, max_chunks, perm ? (int)perm[j] : j);
 }
 
 // -------------------------------------------------------------- traversal
@@ -512,11 +510,13 @@ __device__ __forceinline__ void trace_spheres(const SceneRec& sr, float3 o, floa
 template <bool WIDE, bool MULTI, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_trace_closest(const SceneRec* __restrict__ scenes, BvhRef scene0,
                                                        const float4* __restrict__ o, const float4* __restrict__ d,
-                                                       int n_max, const int* __restrict__ n_dev,
-                                                       float4* __restrict__ hits, int* err) {
+                                                       const int* __restrict__ slots, int n_max,
+                                                       const int* __restrict__ n_dev, float4* __restrict__ hits,
+                                                       int* err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= dev_count(n_max, n_dev)) return;
-  float4 ro = o[i], rd = d[i];
+  const int src = slots ? slots[i] : i;
+  float4 ro = o[src], rd = d[src];
   const int sc = MULTI ? info_scene(__float_as_int(rd.w)) : 0;
   const BvhRef b = MULTI ? bvh_of(scenes[sc], WIDE) : scene0;
   TriHit h;
@@ -533,8 +533,9 @@ __global__ void __launch_bounds__(BLOCK) k_trace_closest(const SceneRec* __restr
 // follow each other, so tri_base + global triangle index + 1 orders exactly
 // like (scene, geomID, primID), and 0 is a miss.
 __global__ void __launch_bounds__(TB) k_hit_keys(const SceneRec* __restrict__ scenes, const float4* __restrict__ d,
-                                                 const float4* __restrict__ hits, int n_max,
-                                                 const int* __restrict__ n_dev, uint32_t* __restrict__ keys) {
+                                                 const int* __restrict__ slots, const float4* __restrict__ hits,
+                                                 int n_max, const int* __restrict__ n_dev,
+                                                 uint32_t* __restrict__ keys) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= dev_count(n_max, n_dev)) return;
   int k = __float_as_int(hits[i].w);
@@ -542,7 +543,7 @@ __global__ void __launch_bounds__(TB) k_hit_keys(const SceneRec* __restrict__ sc
     keys[i] = 0u;
     return;
   }
-  const SceneRec& sc = scenes[info_scene(__float_as_int(d[i].w))];
+  const SceneRec& sc = scenes[info_scene(__float_as_int(d[slots ? slots[i] : i].w))];
   keys[i] = sc.tri_base + (uint32_t)sc.tri_orig[k] + 1u;
 }
 
@@ -693,7 +694,8 @@ constexpr int kShadowGroups = 64;  // two per lane of one warp in the group scan
 static_assert(kShadowGroups == 64 && TB >= kShadowGroups, "the shadow group scan takes one warp");
 
 __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
-                                              Film film, RayBuf batch, const float4* __restrict__ hits,
+                                              Film film, RayBuf batch, const int* __restrict__ slots,
+                                              const float4* __restrict__ hits,
                                               const uint32_t* __restrict__ order, int n_max,
                                               const int* __restrict__ n_dev, RayBuf next, ShadowBuf sh,
                                               int* sh_count, uint32_t* job_done) {
@@ -707,7 +709,8 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   float4 no = so, nd = make_float4(0.f, 0.f, 0.f, __int_as_float(-1)), nw = so;
   if (live) {
     const int i = order ? (int)order[j] : j;
-    const float4 ro = batch.o[i], rd = batch.d[i], rw = batch.w[i], h = hits[i];
+    const int src = slots ? slots[i] : i;
+    const float4 ro = batch.o[src], rd = batch.d[src], rw = batch.w[src], h = hits[i];
     const int k = __float_as_int(h.w);
     const int info = __float_as_int(rd.w);
     job = info_job(info);
@@ -945,7 +948,8 @@ constexpr int kPersistBlock = 128;
 template <bool MULTI>
 __global__ void __launch_bounds__(kPersistBlock) k_trace_closest_pt(const SceneRec* __restrict__ scenes,
                                                                     BvhRef scene0, const float4* __restrict__ o,
-                                                                    const float4* __restrict__ d, int n_max,
+                                                                    const float4* __restrict__ d,
+                                                                    const int* __restrict__ slots, int n_max,
                                                                     const int* __restrict__ n_dev,
                                                                     float4* __restrict__ hits, int* err,
                                                                     int* counter) {
@@ -969,7 +973,8 @@ __global__ void __launch_bounds__(kPersistBlock) k_trace_closest_pt(const SceneR
         const int my = base + __popc(idle & lt);
         if (my < n) {
           ray = my;
-          const float4 ro = o[my], rd = d[my];
+          const int src = slots ? slots[my] : my;
+          const float4 ro = o[src], rd = d[src];
           sc = MULTI ? info_scene(__float_as_int(rd.w)) : 0;
           b = MULTI ? bvh_of(scenes[sc], true) : scene0;
           trav8_init(st, f3(ro), f3(rd), MSC_TNEAR, MSC_TFAR);
@@ -1212,10 +1217,10 @@ int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, f
   return 1;
 }
 
-int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
-                  cudaStream_t s) {
+int launch_batch_slots(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, int* slots,
+                       cudaStream_t s) {
   if (n_max <= 0) return 0;
-  k_gather<<<grid_for(n_max), TB, 0, s>>>(pool.rays, pool.table, pool.max_chunks, plan, perm, dst);
+  k_batch_slots<<<grid_for(n_max), TB, 0, s>>>(pool.table, pool.max_chunks, plan, perm, slots);
   return 1;
 }
 
@@ -1243,8 +1248,8 @@ int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const u
   } while (0)
 
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
-                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev, int block,
-                         int* counter) {
+                         const float4* d, const int* slots, int n, float4* hits, int* err, cudaStream_t s,
+                         const int* n_dev, int block, int* counter) {
   if (n <= 0) return 0;
   const bool wide = scene0.wnodes != nullptr;
   const BvhRef b0 = bvh_of(scene0, wide);
@@ -1252,13 +1257,14 @@ int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec&
     cudaMemsetAsync(counter, 0, sizeof(int), s);
     if (num_scenes > 1)
       k_trace_closest_pt<true><<<persistent_grid(k_trace_closest_pt<true>), kPersistBlock, 0, s>>>(
-          scenes, b0, o, d, n, n_dev, hits, err, counter);
+          scenes, b0, o, d, slots, n, n_dev, hits, err, counter);
     else
       k_trace_closest_pt<false><<<persistent_grid(k_trace_closest_pt<false>), kPersistBlock, 0, s>>>(
-          scenes, b0, o, d, n, n_dev, hits, err, counter);
+          scenes, b0, o, d, slots, n, n_dev, hits, err, counter);
     return 1;
   }
-  MSC_TRACE_DISPATCH(k_trace_closest, block, wide, num_scenes > 1, n, s, scenes, b0, o, d, n, n_dev, hits, err);
+  MSC_TRACE_DISPATCH(k_trace_closest, block, wide, num_scenes > 1, n, s, scenes, b0, o, d, slots, n, n_dev, hits,
+                     err);
   return 1;
 }
 
@@ -1269,10 +1275,10 @@ void persistent_grids_init() {
   persistent_grid(k_trace_shadow_pt<false>);
 }
 
-int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
-                    cudaStream_t s, const int* n_dev) {
+int launch_hit_keys(const SceneRec* scenes, const float4* d, const int* slots, const float4* hits, int n,
+                    uint32_t* keys, cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
-  k_hit_keys<<<grid_for(n), TB, 0, s>>>(scenes, d, hits, n, n_dev, keys);
+  k_hit_keys<<<grid_for(n), TB, 0, s>>>(scenes, d, slots, hits, n, n_dev, keys);
   return 1;
 }
 
@@ -1297,11 +1303,11 @@ int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t 
   return 1;
 }
 
-int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
-                 const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
-                 cudaStream_t s, const int* n_dev) {
+int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const int* slots,
+                 const float4* hits, const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count,
+                 uint32_t* job_done, cudaStream_t s, const int* n_dev) {
   if (n <= 0) return 0;
-  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, hits, order, n, n_dev, next, sh, sh_count,
+  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, slots, hits, order, n, n_dev, next, sh, sh_count,
                                      job_done);
   return 1;
 }

@@ -200,14 +200,17 @@ int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int k
 // ray_sort_key of n rays (o, d as float4) in the origin box lo + [0, 64 / scale).
 int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, float3 scale, uint32_t* keys,
                            cudaStream_t s);
-int launch_gather(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, RayBuf dst,
-                  cudaStream_t s);
+// Pool index of each batch ray in sorted order (perm optional) into slots.
+int launch_batch_slots(const BinPool& pool, const BatchPlan* plan, int n_max, const uint32_t* perm, int* slots,
+                       cudaStream_t s);
 
+// slots (optional): ray i is (o, d)[slots[i]] (the batch read in place from
+// the bin pool); hits are indexed by i.
 int launch_trace_closest(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const float4* o,
-                         const float4* d, int n, float4* hits, int* err, cudaStream_t s, const int* n_dev = nullptr,
-                         int block = 128, int* counter = nullptr);
-int launch_hit_keys(const SceneRec* scenes, const float4* d, const float4* hits, int n, uint32_t* keys,
-                    cudaStream_t s, const int* n_dev = nullptr);
+                         const float4* d, const int* slots, int n, float4* hits, int* err, cudaStream_t s,
+                         const int* n_dev = nullptr, int block = 128, int* counter = nullptr);
+int launch_hit_keys(const SceneRec* scenes, const float4* d, const int* slots, const float4* hits, int n,
+                    uint32_t* keys, cudaStream_t s, const int* n_dev = nullptr);
 // The 64-bit hit key of one scene (shader id 12 b, face 23 b, quantised u 15 b, v 14 b; misses and
 // sphere-light hits 0) as low and high words.
 int launch_hit_keys64(const SceneRec* scenes, const float4* hits, int n, uint32_t* lo, uint32_t* hi,
@@ -216,9 +219,9 @@ int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t*
                       const int* n_dev = nullptr);
 // Fills the scene's face texels from their seed (FP16 bits of k / 1024).
 int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t seed, cudaStream_t s);
-int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const float4* hits,
-                 const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count, uint32_t* job_done,
-                 cudaStream_t s, const int* n_dev = nullptr);
+int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const int* slots,
+                 const float4* hits, const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count,
+                 uint32_t* job_done, cudaStream_t s, const int* n_dev = nullptr);
 // shadow_total (optional): the batch's shadow count is added to it.
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
                         const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
