@@ -36,6 +36,12 @@ for p in (os.path.join(REPO, "msc-project_gb300"), REPO):
 METRIC = "end-to-end Mrays/s on 1 GB300, batched/served vs plain; p50/p99 job latency"
 SEED = 20261203
 ALG_BYTES_TRACE = 52  # per closest-hit query: read ray 32 B (org, dir), write hit 20 B
+# DRAM bytes per closest-hit query of k_trace_closest, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the half-scale terrain:
+# 71.8 MB and 70.4 MB for two launches of 1,048,576 rays (camera rays, first
+# bounces), i.e. ~68 B per ray: the ray and hit records plus node and triangle
+# misses.
+DRAM_BYTES_PER_CLOSEST = (71.77e6 + 70.39e6) / (2 * 1048576)
 
 
 def log(*a):
@@ -495,7 +501,10 @@ def main():
     achieved = per_launch_bytes / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
     roofline = {"kernel": "k_trace_closest (closest-hit traversal)", "bound": "hbm", "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                "traffic": None,
+                "traffic": DRAM_BYTES_PER_CLOSEST * prof["closest_queries"] / trace_launches,
+                "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of an ncu capture of the half-scale "
+                                "terrain (1,048,576 rays per launch: 71.8 MB and 70.4 MB), scaled by the rays of an "
+                                "average full-size launch",
                 "alg_bytes": "52 B per closest-hit query (ray 32 B read, hit 20 B written; BVH bytes excluded)",
                 "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "top_stage": top}
     lat = sorted(dev_ms)
