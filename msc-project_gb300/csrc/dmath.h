@@ -224,15 +224,6 @@ MSC_HD uint32_t spread_bits_3(uint32_t v) {  // 10 bits -> every third bit
   return v;
 }
 
-MSC_HD uint32_t spread_bits_2(uint32_t v) {  // 16 bits -> every second bit
-  v &= 0xffffu;
-  v = (v | (v << 8)) & 0x00ff00ffu;
-  v = (v | (v << 4)) & 0x0f0f0f0fu;
-  v = (v | (v << 2)) & 0x33333333u;
-  v = (v | (v << 1)) & 0x55555555u;
-  return v;
-}
-
 MSC_HD int clamp_i(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Quantise v in [lo, lo + 1/scale] to [0, cells-1].

@@ -116,7 +116,6 @@ constexpr int kSortMaxPassesAny = 8;
 struct SortScratch {
   uint32_t* keys_alt = nullptr;
   uint32_t* vals_alt = nullptr;
-  uint32_t* counts = nullptr;   // reduce-then-scan: RADIX * tiles (aliases the first half of `status`)
   uint32_t* status = nullptr;   // look-back words: 2 arrays of RADIX * tiles
   uint32_t* hist = nullptr;     // global digit counts of every pass (kSortHistWords)
   uint32_t* ctl = nullptr;      // kSortMaxPassesAny tile counters, then the error word
@@ -161,11 +160,6 @@ void sort_init();
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
                int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr,
                int digit_bits = 8);
-
-// The same order with three kernels per pass (upsweep count, one-block scan,
-// downsweep scatter) and no inter-block waiting.
-int sort_pairs_reduce_scan(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
-                           int n, int bits, SortScratch& s, cudaStream_t stream);
 
 constexpr int kSortErrLookback = 256;
 

@@ -1,17 +1,15 @@
-// Stable LSD radix sort of 32-bit keys with 32-bit values, 8-bit digits.
+// Stable LSD radix sort of 32-bit keys with 32-bit values, 4-, 8- or 11-bit
+// digits.
 //
-// sort_pairs (the one the render loop uses): one histogram kernel counts the
-// digits of every pass in a single read of the keys; then each pass is one
-// kernel.  A block takes the next tile from a counter, ranks its keys stably
-// (tile_rank: warp match + per-warp counters), publishes its per-digit counts,
-// and sums its predecessors' counts by a decoupled look-back (each tile first
-// posts an aggregate, then its inclusive prefix).  The tile is staged in
-// shared memory in digit order, so the global scatter writes contiguous runs.
+// sort_pairs: one histogram kernel counts the digits of every pass in a
+// single read of the keys; then each pass is one kernel.  A block takes the
+// next tile from a counter, ranks its keys stably (tile_rank: warp match +
+// per-warp counters), publishes its per-digit counts, and sums its
+// predecessors' counts by a decoupled look-back (each tile first posts an
+// aggregate, then its inclusive prefix).  The tile is staged in shared memory
+// in digit order, so the global scatter writes contiguous runs.
 //
-// sort_pairs_reduce_scan: the same order with upsweep / one-block scan /
-// downsweep kernels per pass, kept as a wait-free reference path.
-//
-// Both replace the reference's comparison sorts of a batch (tbb::parallel_sort
+// It replaces the reference's comparison sorts of a batch (tbb::parallel_sort
 // in src/core/RaySort.cpp:17,97 and the hit sort of src/core/Pathtracer.cpp:335-339)
 // with a key-based stable order.
 #include "radix.cuh"
@@ -20,7 +18,6 @@ namespace mscg {
 
 namespace {
 
-constexpr int RADIX = 1 << kSortRadixBits;
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;
 constexpr int kLookbackSpinCap = 1 << 20;
@@ -217,69 +214,6 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
   }
 }
 
-// ------------------------------------------------------ reduce-then-scan
-__global__ void __launch_bounds__(kSortBlock) k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift,
-                                                              uint32_t mask, uint32_t* __restrict__ counts,
-                                                              int num_tiles) {
-  __shared__ int hist[RADIX];
-  for (int i = threadIdx.x; i < RADIX; i += kSortBlock) hist[i] = 0;
-  __syncthreads();
-  const int base = blockIdx.x * kSortTile;
-  const int lane = threadIdx.x & 31;
-#pragma unroll 4
-  for (int k = 0; k < kSortItems; ++k) {
-    int idx = base + k * kSortBlock + threadIdx.x;
-    int d = idx < n ? (int)((keys[idx] >> shift) & mask) : -1;
-    unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (d >= 0 && lane == __ffs(peers) - 1) atomicAdd(&hist[d], __popc(peers));
-  }
-  __syncthreads();
-  for (int d = threadIdx.x; d < RADIX; d += kSortBlock) counts[d * num_tiles + blockIdx.x] = (uint32_t)hist[d];
-}
-
-__global__ void __launch_bounds__(kSortBlock) k_radix_downsweep(const uint32_t* __restrict__ keys_in,
-                                                                const uint32_t* __restrict__ vals_in,
-                                                                uint32_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out, int n, int shift,
-                                                                uint32_t mask, const uint32_t* __restrict__ offsets,
-                                                                int num_tiles) {
-  __shared__ RankSmem<kSortBlock, RADIX> sm;
-  __shared__ uint32_t skey[kSortTile];
-  __shared__ uint32_t sval[kSortTile];
-  __shared__ uint32_t gofs[RADIX];
-  const int tile = blockIdx.x;
-  const int base = tile * kSortTile;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int d = threadIdx.x; d < RADIX; d += kSortBlock) gofs[d] = offsets[d * num_tiles + tile];
-  uint32_t key[kSortItems], val[kSortItems];
-  int dig[kSortItems], pos[kSortItems];
-#pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    int idx = base + warp * 32 * kSortItems + k * 32 + lane;
-    bool ok = idx < n;
-    key[k] = ok ? keys_in[idx] : 0u;
-    val[k] = ok ? (vals_in ? vals_in[idx] : (uint32_t)idx) : 0u;
-    dig[k] = ok ? (int)((key[k] >> shift) & mask) : -1;
-  }
-  tile_rank<kSortBlock, kSortItems, RADIX>(dig, pos, sm);
-#pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    if (pos[k] >= 0) {
-      skey[pos[k]] = key[k];
-      sval[pos[k]] = val[k];
-    }
-  }
-  __syncthreads();
-  const int count = min(kSortTile, n - base);
-  for (int p = threadIdx.x; p < count; p += kSortBlock) {
-    uint32_t k = skey[p];
-    int d = (int)((k >> shift) & mask);
-    uint32_t o = gofs[d] + (uint32_t)(p - sm.tile_start[d]);
-    keys_out[o] = k;
-    vals_out[o] = sval[p];
-  }
-}
-
 __global__ void k_copy_u32(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int n, int iota) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) dst[i] = iota ? (uint32_t)i : src[i];
@@ -382,7 +316,6 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_b
   s->vals_alt = (uint32_t*)p;
   p += sort_align256(cap * 4);
   s->status = (uint32_t*)p;
-  s->counts = s->status;
   p += sort_align256(2 * sort_status_words(capacity, max_digit_bits) * 4);
   s->hist = (uint32_t*)p;
   s->ctl = s->hist + kSortHistWords;
@@ -449,34 +382,6 @@ int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_
   if (digit_bits == 4) return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
   if (digit_bits == 11) return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
   return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
-}
-
-int sort_pairs_reduce_scan(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
-                           int n, int bits, SortScratch& s, cudaStream_t stream) {
-  if (n <= 0) return 0;
-  const int passes = (bits + kSortRadixBits - 1) / kSortRadixBits;
-  const uint32_t* src_k;
-  const uint32_t* src_v;
-  bool done;
-  int launches = sort_prologue(src_k, src_v, keys_in, vals_in, keys_out, vals_out, n, passes, s, stream, &done);
-  if (done) return launches;
-  const int tiles = (n + kSortTile - 1) / kSortTile;
-  for (int p = 0; p < passes; ++p) {
-    const bool to_out = ((passes - 1 - p) % 2) == 0;
-    uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
-    uint32_t* dst_v = to_out ? vals_out : s.vals_alt;
-    const int shift = p * kSortRadixBits;
-    const int width = bits - shift < kSortRadixBits ? bits - shift : kSortRadixBits;
-    const uint32_t mask = (1u << width) - 1u;
-    k_radix_upsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, n, shift, mask, s.counts, tiles);
-    k_scan_exclusive<<<1, 1024, 0, stream>>>(s.counts, tiles * RADIX, nullptr);
-    k_radix_downsweep<<<tiles, kSortBlock, 0, stream>>>(src_k, src_v, dst_k, dst_v, n, shift, mask, s.counts,
-                                                         tiles);
-    launches += 3;
-    src_k = dst_k;
-    src_v = dst_v;
-  }
-  return launches;
 }
 
 }  // namespace mscg
