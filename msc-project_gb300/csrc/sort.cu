@@ -50,15 +50,25 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_hist(const uint32_t* __
   __shared__ uint32_t sh[S::MAXP * S::RADIX];
   for (int i = threadIdx.x; i < S::MAXP * S::RADIX; i += kSortBlock) sh[i] = 0;
   __syncthreads();
-  const int stride = gridDim.x * kSortBlock;
-  for (int base = blockIdx.x * kSortBlock; base < n; base += stride) {
-    const int idx = base + threadIdx.x;
-    if (idx < n) {  // shared-memory atomics: cheaper than grouping equal digits first
-      const uint32_t key = keys[idx];
+  // four keys per thread and step, loaded before any is counted (independent
+  // loads in flight); shared-memory atomics are cheaper than grouping equal
+  // digits first
+  constexpr int U = 4;
+  const int stride = gridDim.x * kSortBlock * U;
+  for (int base = blockIdx.x * kSortBlock * U; base < n; base += stride) {
+    uint32_t key[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int idx = base + u * kSortBlock + threadIdx.x;
+      key[u] = idx < n ? keys[idx] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (base + u * kSortBlock + (int)threadIdx.x >= n) break;
       for (int p = 0; p < passes; ++p) {
         const int shift = p * RB;
         const int width = bits - shift < RB ? bits - shift : RB;
-        atomicAdd(&sh[p * S::RADIX + ((key >> shift) & ((1u << width) - 1u))], 1u);
+        atomicAdd(&sh[p * S::RADIX + ((key[u] >> shift) & ((1u << width) - 1u))], 1u);
       }
     }
   }
@@ -343,7 +353,7 @@ int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_ou
   cudaMemsetAsync(status0, 0, (size_t)tiles * S::RADIX * 4, stream);
   cudaMemsetAsync(s.hist, 0, (size_t)kSortHistWords * 4 + 64, stream);
   int* errw = err ? err : (int*)(s.ctl + kSortMaxPassesAny);
-  const int hist_blocks = std::min(std::max(1, (n + S::TILE - 1) / S::TILE), 2 * 152);
+  const int hist_blocks = std::min(std::max(1, (n + S::TILE - 1) / S::TILE), 4 * 152);
   k_onesweep_hist<RB><<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
   ++launches;
   for (int p = 0; p < passes; ++p) {

@@ -200,6 +200,20 @@ def test_hit_key_width_and_sorting_do_not_change_the_image(built, stress_scene, 
         assert np.array_equal(im.view(np.uint32), images[0].view(np.uint32))
 
 
+def test_ray_and_hit_sorts_do_not_change_the_image(built, box_scene):
+    """Sorted or not, a batch is traced and shaded in place in the bin pool;
+    the order of rays within a batch must not change any path's result."""
+    mscgpu, _ = built
+    imgs = []
+    for rs, hs, e in ((False, False, 12), (True, False, 12), (False, True, 10), (True, True, 14)):
+        with mscgpu.Pathtracer(box_scene) as pt:
+            pt.set_tuning(batch_exponent=e, ray_sort=rs, hit_sort=hs)
+            pt.process()
+            imgs.append(pt.image())
+    for im in imgs[1:]:
+        assert np.array_equal(im.view(np.uint32), imgs[0].view(np.uint32))
+
+
 @pytest.mark.parametrize("nbins", [26, 98])
 def test_direction_bin_count_does_not_change_the_image(built, box_scene, nbins):
     mscgpu, _ = built
