@@ -131,6 +131,7 @@ Core::~Core() {
   if (h_jobs_) cudaFreeHost(h_jobs_);
   if (h_job_done_) cudaFreeHost(h_job_done_);
   if (graph_) cudaGraphExecDestroy(graph_);
+  if (drain_graph_) cudaGraphExecDestroy(drain_graph_);
   if (h_ctr_) cudaFreeHost(h_ctr_);
   for (auto e : tune_ev_)
     if (e) cudaEventDestroy(e);
@@ -688,6 +689,9 @@ void Core::drop_graph() {
   if (graph_) cudaGraphExecDestroy(graph_);
   graph_ = nullptr;
   graph_key_ = 0;
+  if (drain_graph_) cudaGraphExecDestroy(drain_graph_);
+  drain_graph_ = nullptr;
+  drain_key_ = 0;
 }
 
 // One batch body.  Every size is read on the device from the plan, so the
@@ -788,12 +792,27 @@ int Core::enqueue_batch(int index, bool overlap) {
   return MSC_OK;
 }
 
-// Captures and instantiates the batch graph for the current choice if needed.
+// Captures and instantiates the batch graph for the current choice if needed,
+// and (for batches above kDrainBatch) the drain graph: the same bodies sized
+// for kDrainBatch rays, replayed once the bins hold no more than that, so the
+// small batches of a pass's end launch grids 8 or more times smaller.
 int Core::ensure_graph() {
   if (profiling || !use_graph) return MSC_OK;
+  int rc = capture_graph(&graph_, &graph_key_, &graph_launches_);
+  if (rc != MSC_OK || batch_size_ <= kDrainBatch) return rc;
+  const int full = batch_size_;
+  batch_size_ = kDrainBatch;
+  rc = capture_graph(&drain_graph_, &drain_key_, &drain_launches_);
+  batch_size_ = full;
+  return rc;
+}
+
+int Core::capture_graph(cudaGraphExec_t* exec, uint64_t* exec_key, int* exec_launches) {
   const uint64_t key = graph_key();
-  if (!graph_ || graph_key_ != key) {
-    drop_graph();
+  if (!*exec || *exec_key != key) {
+    if (*exec) cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+    *exec_key = 0;
     cudaGraph_t g = nullptr;
     const uint64_t launches0 = stats.launches;
     uint64_t stage0[12];
@@ -814,22 +833,22 @@ int Core::ensure_graph() {
       err = std::string("capturing the batch body: ") + cudaGetErrorString(ce);
       return MSC_ERR_CUDA;
     }
-    ce = cudaGraphInstantiate(&graph_, g, 0);
+    ce = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) {
-      graph_ = nullptr;
+      *exec = nullptr;
       err = std::string("instantiating the batch graph: ") + cudaGetErrorString(ce);
       return MSC_ERR_CUDA;
     }
-    graph_launches_ = (int)(stats.launches - launches0);
+    *exec_launches = (int)(stats.launches - launches0);
     stats.launches = launches0;  // counted per replay below
     memcpy(stats.stage_launches, stage0, sizeof(stage0));
-    graph_key_ = key;
+    *exec_key = key;
   }
   return MSC_OK;
 }
 
-int Core::run_batches(int k) {
+int Core::run_batches(int k, bool drain) {
   if (profiling || !use_graph) {
     for (int i = 0; i < k; ++i) {
       int rc = enqueue_batch(i, false);
@@ -840,9 +859,10 @@ int Core::run_batches(int k) {
   }
   const int grc = ensure_graph();
   if (grc != MSC_OK) return grc;
+  const bool small = drain && drain_graph_ != nullptr;
   const int replays = (k + kGraphBodies - 1) / kGraphBodies;  // bodies past the work plan empty batches
-  for (int i = 0; i < replays; ++i) CK(cudaGraphLaunch(graph_, stream_));
-  stats.launches += (uint64_t)graph_launches_ * (uint64_t)replays;
+  for (int i = 0; i < replays; ++i) CK(cudaGraphLaunch(small ? drain_graph_ : graph_, stream_));
+  stats.launches += (uint64_t)(small ? drain_launches_ : graph_launches_) * (uint64_t)replays;
   stats.graph_replays += (uint64_t)replays;
   return MSC_OK;
 }
@@ -904,7 +924,7 @@ int Core::step(bool* idle) {
   }
   if (merge_bins) need = (total + bs - 1) / bs;
   const int k = (int)std::min<uint64_t>(std::max<uint64_t>(need, 1), (uint64_t)std::max(1, max_batches_per_step));
-  return run_batches(k);
+  return run_batches(k, merge_bins && total <= (uint64_t)kDrainBatch);
 }
 
 TuneChoice Core::choice() const {

@@ -160,8 +160,11 @@ class Core {
   // i+1's shading waits for it, so every path still adds to its sample in
   // bounce order.
   int enqueue_batch(int index, bool overlap);
-  int run_batches(int k);         // k batch bodies (graph replays or eager)
+  // k batch bodies (graph replays or eager); drain: the bins hold at most
+  // kDrainBatch rays, so the smaller drain graph serves
+  int run_batches(int k, bool drain = false);
   int ensure_graph();
+  int capture_graph(cudaGraphExec_t* exec, uint64_t* exec_key, int* exec_launches);
   void drop_graph();
   int finish_job(JobState& j);
   int generate(bool* did);
@@ -209,6 +212,7 @@ class Core {
   ShadowBuf shadow_[2];          // shadow queues, alternating between batches
   cudaStream_t side_ = nullptr;  // occlusion of batch k runs here beside batch k+1's front part
   static constexpr int kGraphBodies = 4;
+  static constexpr int kDrainBatch = 1 << 20;  // batch capacity of the drain graph
   cudaEvent_t fork_ev_[kGraphBodies] = {}, join_ev_[kGraphBodies] = {};
   Counters* ctr_ = nullptr;    // device counters
   int* trace_counter_ = nullptr;  // ray counters of the persistent traversal (closest, shadow)
@@ -216,6 +220,9 @@ class Core {
   BatchPlan* plan_ = nullptr;
   cudaGraphExec_t graph_ = nullptr;
   uint64_t graph_key_ = 0;
+  cudaGraphExec_t drain_graph_ = nullptr;  // the bodies sized for kDrainBatch rays
+  uint64_t drain_key_ = 0;
+  int drain_launches_ = 0;
   int graph_launches_ = 0;     // kernels in one replay
   uint64_t graph_key() const;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> stage_events_;
