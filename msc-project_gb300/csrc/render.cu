@@ -263,10 +263,10 @@ __global__ void __launch_bounds__(PB) k_part_scatter(RayBuf src, int n_max, cons
     const int at = gofs[b] + (p - sm.tile_start[b]);
     if ((at >> kChunkShift) >= pool.held[b]) continue;  // no chunk reserved: reported by k_part_reserve
     const int o = pool_index(pool.table, pool.max_chunks, b, at);
-    const float4 ro = src.o[s], rd = src.d[s];
+    const float4 ro = __ldg(&src.o[s]), rd = __ldg(&src.d[s]);
     pool.rays.o[o] = ro;
     pool.rays.d[o] = rd;
-    pool.rays.w[o] = src.w[s];
+    pool.rays.w[o] = __ldg(&src.w[s]);
     if (scenes) {  // the ray sort key, in the ray's scene box
       const int sc = info_scene(__float_as_int(rd.w));
       const float4 lo = scenes[sc].key_lo, sca = scenes[sc].key_scale;
@@ -710,7 +710,9 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   if (live) {
     const int i = order ? (int)order[j] : j;
     const int src = slots ? slots[i] : i;
-    const float4 ro = batch.o[src], rd = batch.d[src], rw = batch.w[src], h = hits[i];
+    // the batch's rays are only read here (the pool is rewritten by the next
+    // partition, after this kernel): the read-only path serves them
+    const float4 ro = __ldg(&batch.o[src]), rd = __ldg(&batch.d[src]), rw = __ldg(&batch.w[src]), h = hits[i];
     const int k = __float_as_int(h.w);
     const int info = __float_as_int(rd.w);
     job = info_job(info);
