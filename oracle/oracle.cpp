@@ -1356,8 +1356,11 @@ void render_path(const oracle_scene* S, uint32_t sid, uint32_t seed, T* rgb, T* 
   rgb[2] = L.z;
 }
 
+// Paths [first, first + n); path sid writes rgb[3 * (sid - out_base)] and
+// xy[2 * (sid - out_base)] when those are given.
 template <class T>
-void parallel_paths(oracle_scene* S, int iteration, int threads, uint64_t first, uint64_t n, T* rgb, T* xy, Counts* total) {
+void parallel_paths(oracle_scene* S, int iteration, int threads, uint64_t first, uint64_t n, T* rgb, T* xy, Counts* total,
+                    uint64_t out_base = 0) {
   const uint32_t seed = iter_seed(S->seed, (uint32_t)iteration);
   if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
   std::atomic<uint64_t> next(0);
@@ -1371,7 +1374,8 @@ void parallel_paths(oracle_scene* S, int iteration, int threads, uint64_t first,
       uint64_t e = std::min(n, b + chunk);
       for (uint64_t k = b; k < e; ++k) {
         uint64_t sid = first + k;
-        render_path<T>(S, (uint32_t)sid, seed, rgb ? rgb + 3 * sid : dummy_rgb, xy ? xy + 2 * sid : dummy_xy, &cs[tid]);
+        const uint64_t o = sid - out_base;
+        render_path<T>(S, (uint32_t)sid, seed, rgb ? rgb + 3 * o : dummy_rgb, xy ? xy + 2 * o : dummy_xy, &cs[tid]);
       }
     }
   };
@@ -1509,6 +1513,14 @@ int oracle_render_f64(oracle_scene* s, int iteration, int threads, double* rgb, 
 int oracle_render_range_f32(oracle_scene* s, int iteration, int threads, uint64_t first, uint64_t n, uint64_t* counts) {
   orc::Counts c;
   orc::parallel_paths<float>(s, iteration, threads, first, n, nullptr, nullptr, &c);
+  if (counts) { counts[0] = c.closest; counts[1] = c.shadow; }
+  return 0;
+}
+
+int oracle_render_range_rgb_f32(oracle_scene* s, int iteration, int threads, uint64_t first, uint64_t n, float* rgb,
+                                float* xy, uint64_t* counts) {
+  orc::Counts c;
+  orc::parallel_paths<float>(s, iteration, threads, first, n, rgb, xy, &c, first);
   if (counts) { counts[0] = c.closest; counts[1] = c.shadow; }
   return 0;
 }

@@ -51,6 +51,10 @@ int oracle_render_f64(oracle_scene* s, int iteration, int threads, double* sampl
                       double* pixels, uint64_t* counts);
 /* Paths [first, first+n) only, no film output: the timed CPU baseline. */
 int oracle_render_range_f32(oracle_scene* s, int iteration, int threads, uint64_t first, uint64_t n, uint64_t* counts);
+/* Paths [first, first+n) with their radiance (3*n floats) and film positions
+ * (2*n floats, may be NULL), indexed from `first`: spot checks of full-size scenes. */
+int oracle_render_range_rgb_f32(oracle_scene* s, int iteration, int threads, uint64_t first, uint64_t n, float* rgb,
+                                float* xy, uint64_t* counts);
 
 /* Closest hit (geom/prim = reference geomID/primID, -1 for a miss) and occlusion. */
 int oracle_trace_f32(const oracle_scene* s, const float* org, const float* dir, int n, float* t, float* u, float* v,

@@ -32,6 +32,7 @@ def lib():
         L.oracle_render_f32.argtypes = [P, I, I, F, F, F, U64]
         L.oracle_render_f64.argtypes = [P, I, I, D, D, D, U64]
         L.oracle_render_range_f32.argtypes = [P, I, I, C.c_uint64, C.c_uint64, U64]
+        L.oracle_render_range_rgb_f32.argtypes = [P, I, I, C.c_uint64, C.c_uint64, F, F, U64]
         L.oracle_trace_f32.argtypes = [P, F, F, I, F, F, F, I32, I32]
         L.oracle_occluded_f32.argtypes = [P, F, F, F, I, I32]
         L.oracle_cardinal.argtypes = [F, I, I32]
@@ -103,6 +104,15 @@ class Scene:
         counts = np.zeros(2, np.uint64)
         lib().oracle_render_range_f32(self._s, iteration, threads, first, n, _p(counts, C.c_uint64))
         return counts
+
+    def render_range_rgb(self, first, n, iteration=0, threads=0):
+        """Radiance (n,3), film positions (n,2) and query counts of paths [first, first+n)."""
+        rgb = np.zeros((n, 3), np.float32)
+        xy = np.zeros((n, 2), np.float32)
+        counts = np.zeros(2, np.uint64)
+        lib().oracle_render_range_rgb_f32(self._s, iteration, threads, first, n, _p(rgb, C.c_float), _p(xy, C.c_float),
+                                          _p(counts, C.c_uint64))
+        return rgb, xy, counts
 
     def trace(self, org, dirs):
         org = np.ascontiguousarray(org, np.float32)
