@@ -48,15 +48,41 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def make_scene(config, scale):
-    import mscgpu
-    d = os.path.join(tempfile.gettempdir(), "msc_bench_scenes", "c%d_s%d_%g" % (config, SEED + config, scale))
+def scene_generator():
+    """The host-only scene generator executable (msc-scenegen): it writes the
+    seeded YAML + OBJ files without loading the CUDA library, so that the CPU
+    reference arm never loads the renderer's shared library."""
+    from mscgpu import build as B  # the build script only; the package loads no library on import
+    if not os.path.exists(B.SCENEGEN):
+        B.build_scenegen()
+    return B.SCENEGEN
+
+
+def make_scene(config, scale, seed=None):
+    seed = SEED + config if seed is None else seed
+    d = os.path.join(tempfile.gettempdir(), "msc_bench_scenes", "c%d_s%d_%g" % (config, seed, scale))
     y = os.path.join(d, "scene.yaml")
     if not os.path.exists(y):
         t = time.time()
-        y = mscgpu.generate_scene(config, SEED + config, d, scale=scale)
+        os.makedirs(d, exist_ok=True)
+        out = subprocess.run([scene_generator(), str(config), str(seed), repr(float(scale)), d], check=True,
+                             stdout=subprocess.PIPE, text=True).stdout.strip()
+        y = out or y
         log("generated scene %s in %.1f s" % (y, time.time() - t))
     return y
+
+
+NAMES = {1: "terrain 1024^2 quads + 300 icospheres, 8 quad lights, 4 Lambert + 4 Phong",
+         0: "Cornell-style box, 1316 tris, 1 quad light"}
+
+
+def workload_config(args, width, height, spp, triangles, lights):
+    """The workload's identity, printed alike by both arms."""
+    return {"workload": NAMES.get(args.config, "config %d" % args.config), "scene_config": args.config,
+            "scale": args.scale, "width": width, "height": height, "spp": spp, "triangles": triangles,
+            "lights": lights, "batch": 1 << (20 if args.config == 1 else 16), "seed": SEED + args.config,
+            "l2": "inputs larger than L2 (129 MB): BVH + triangles ~0.25 GB, sample film 1.6 GB, ray pool up to "
+                  "1.6 GB, batch buffers ~1.3 GB, all read or written every step"}
 
 
 class ClockSampler:
@@ -167,12 +193,7 @@ def scene_set(n, lo_tris, hi_tris, seed):
 
 
 def make_scene_scaled(config, seed, scale):
-    import mscgpu
-    d = os.path.join(tempfile.gettempdir(), "msc_bench_scenes", "c%d_s%d_%g" % (config, seed, scale))
-    y = os.path.join(d, "scene.yaml")
-    if not os.path.exists(y):
-        y = mscgpu.generate_scene(config, seed, d, scale=scale)
-    return y
+    return make_scene(config, scale, seed)
 
 
 def sphere_camera(rng, bbox, fov_lo=30.0, fov_hi=70.0):
@@ -359,19 +380,29 @@ def bench_stress(args):
     return out
 
 
-def run_reference(args, yaml, cfg):
+def run_reference(args):
+    """The CPU arm: the reference algorithm (its CPU restatement in oracle/) on
+    the host cores, on the same scene files.  It loads neither the CUDA
+    renderer's library nor anything built from its sources but the host-only
+    scene generator, which runs as a separate executable."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from oracle import build as oracle_build
+    oracle_build.build()
     from oracle import oracle as O
+    yaml = make_scene(args.config, args.scale)
+    t = time.time()
     s = O.Scene(yaml)
+    log("oracle scene load + SAH build %.1f s" % (time.time() - t))
+    cfg = workload_config(args, s.width, s.height, s.spp, s.triangles, s.lights)
     cores = os.cpu_count() or 1
     first = (s.width // 2) * s.height * s.spp
-    n = 1 << 16
+    n = min(1 << 16, s.paths - first)
     t = time.time()
     s.render_range(first, n, 0, cores)
     dt = time.time() - t
-    n = max(1 << 14, min(int(n * 8.0 / max(dt, 1e-3)), s.paths - first))  # ~8 s per step
+    n = max(min(1 << 14, s.paths - first), min(int(n * 8.0 / max(dt, 1e-3)), s.paths - first))  # ~8 s per step
     for w in range(args.warmup):
         s.render_range(first, n, 1000 + w, cores)
     times, rays = [], 0
@@ -394,51 +425,110 @@ def run_reference(args, yaml, cfg):
     print(json.dumps(out), flush=True)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", type=int, default=1, help="scene config (1: large terrain scene, 0: box)")
-    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
-    ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
-    ap.add_argument("--tuning", default="auto",
-                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort"
-                         "[,persistent[,digit_bits]]")
-    ap.add_argument("--stress-scale", type=float, default=1.0)
-    ap.add_argument("--serve-rates", default="100:6,600:3",
-                    help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
-    ap.add_argument("--forms-scenes", type=int, default=64)
-    ap.add_argument("--serve-seconds", type=float, default=6.0)
-    args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
+def timed_passes(pt, passes, warmup=2):
+    """Device-timed passes of the plain engine: (Mrays/s, ms per pass, rays per pass)."""
+    for _ in range(warmup):
+        pt.process_device()
+    ms, rays = 0.0, 0
+    for _ in range(passes):
+        pt.process_device()
+        st = pt.stats()
+        ms += st["process_ms"]
+        rays += st["closest_queries"] + st["shadow_queries"]
+    return rays / ms / 1e3, ms / passes, rays // passes
 
+
+def profiled_pass(pt):
+    pt.set_profiling(True)
+    pt.process_device()
+    prof = pt.stats()
+    pt.set_profiling(False)
+    return prof
+
+
+TUNE_KEYS = ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits",
+             "ray_key_bits")
+
+
+def hbm_stages(prof, peak, spp):
+    """Achieved HBM bandwidth of the bandwidth-bound stages from one profiled
+    pass: algorithmic bytes per ray (or per sample) / the stage's event time."""
+    sm = prof["stage_ms"]
+    closest = prof["closest_queries"]
+    paths = prof["width"] * prof["height"] * spp
+    out = {}
+    # bin partition: every ray that leaves shading (and every camera ray) is read
+    # from staging (48 B) and written into its bin (48 B) with its key (4 B),
+    # plus the count, scan and commit passes (~12 B)
+    for name, ms, nbytes, what in (
+            ("bins", sm["bins"], 112.0 * closest, "112 B per ray entering the bins"),
+            ("ray_sort", sm["ray_sort"], 36.0 * closest, "36 B per key: histogram read + two 16 B passes"),
+            ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)")):
+        if ms > 0:
+            gbs = nbytes / (ms / 1e3) / 1e9
+            out[name] = {"ms": round(ms, 3), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4), "alg_bytes": what}
+    return out
+
+
+def bench_plain_extra(args, tuned):
+    """C1 at its stated settings (batches of 2^20 rays, 32-bit ray keys, hit
+    sort on, 6 direction bins) beside the tuned point, and the box scene."""
+    import mscgpu
+    out = {}
+    yaml = make_scene(1, args.scale)
+    pt = mscgpu.Pathtracer(yaml)
+    pinned = dict(batch_exponent=20, trace_block=tuned["trace_block"], ray_sort=True, hit_sort=True, bins=6,
+                  persistent=False, digit_bits=8, ray_key_bits=32)
+    pt.set_tuning(**pinned)
+    rate, ms, rays = timed_passes(pt, 3)
+    prof = profiled_pass(pt)
+    out["pinned"] = {"settings": "batches of 2^20 rays, 32-bit ray sort keys (4 x 8-bit digit passes), hit sort "
+                                 "on, 6 direction bins, %d-thread traversal" % tuned["trace_block"],
+                     "mrays_per_s": rate, "ms_per_pass": ms, "rays_per_pass": rays,
+                     "stage_ms": {k: round(v, 3) for k, v in prof["stage_ms"].items()}}
+    pt.close()
+    y0 = make_scene(0, 1.0)
+    pt = mscgpu.Pathtracer(y0)
+    passes = 0
+    while pt.tuning()["tuning"] and passes < 32:
+        pt.process_device()
+        passes += 1
+    t0 = pt.tuning()
+    rate, ms, rays = timed_passes(pt, 20)
+    pt.set_tuning(batch_exponent=16, trace_block=t0["trace_block"], ray_sort=True, hit_sort=True, bins=6,
+                  persistent=False, digit_bits=8, ray_key_bits=32)
+    prate, pms, _ = timed_passes(pt, 20)
+    st = pt.stats()
+    pt.close()
+    out["c0"] = {"workload": "Cornell-style box, 256^2 x 16 spp, depth 4, %d tris" % st["triangles"],
+                 "tuned_mrays_per_s": rate, "tuned_ms_per_pass": ms, "rays_per_pass": rays,
+                 "tuned": {k: t0[k] for k in TUNE_KEYS},
+                 "pinned_mrays_per_s": prate, "pinned_ms_per_pass": pms,
+                 "pinned": "batches of 2^16 rays, 32-bit ray keys, hit sort on, 6 bins"}
+    return out
+
+
+def run_gpu(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return  # one GPU per run: only rank 0 renders
     import __graft_entry__ as g
     g.build()
     import mscgpu
 
     yaml = make_scene(args.config, args.scale)
+    t = time.time()
     info, _, _ = mscgpu.scene_load_host(yaml)
-    names = {1: "terrain 1024^2 quads + 300 icospheres, 8 quad lights, 4 Lambert + 4 Phong",
-             0: "Cornell-style box, 1316 tris, 1 quad light"}
-    cfg = {"workload": names.get(args.config, "config %d" % args.config), "scene_config": args.config,
-           "scale": args.scale, "width": info["width"], "height": info["height"], "spp": info["spp"],
-           "triangles": info["triangles"], "lights": info["lights"],
-           "batch": 1 << (20 if args.config == 1 else 16), "seed": SEED + args.config,
-           "l2": "inputs larger than L2 (129 MB): BVH + triangles ~0.25 GB, sample film 1.6 GB, ray pool up to "
-                 "1.6 GB, batch buffers ~1.3 GB, all read or written every step"}
-    if args.impl == "reference":
-        run_reference(args, yaml, cfg)
-        return
-    if int(os.environ.get("RANK", "0")) != 0:
-        return  # one GPU per run: only rank 0 renders
+    host_parse_s = time.time() - t
+    cfg = workload_config(args, info["width"], info["height"], info["spp"], info["triangles"], info["lights"])
 
     t = time.time()
     pt = mscgpu.Pathtracer(yaml)
-    log("scene load + device BVH build %.1f s" % (time.time() - t))
+    create_s = time.time() - t
+    st0 = pt.stats()
+    scene_input = {"msc_create_s": round(create_s, 3), "load_s": round(st0["load_ms"] / 1e3, 3),
+                   "bvh_build_s": round(st0["bvh_ms"] / 1e3, 3), "host_parse_only_s": round(host_parse_s, 3),
+                   "triangles": info["triangles"]}
+    log("scene input: %s" % json.dumps(scene_input))
     tuning_passes = 0
     if args.tuning != "auto":
         v = [int(x) for x in args.tuning.split(",")]
@@ -447,7 +537,7 @@ def main():
                       persistent=bool(v[5]), digit_bits=v[6])
     else:
         # the engine tunes itself during its first passes: let it finish before the warm-up
-        while pt.tuning()["tuning"] and tuning_passes < 24:
+        while pt.tuning()["tuning"] and tuning_passes < 32:
             pt.process_device()
             tuning_passes += 1
         log("autotuner settled after %d passes: %s" % (tuning_passes, pt.tuning()))
@@ -481,13 +571,9 @@ def main():
     t_timed_end = time.time()
     clocks.stop()
     # one profiled pass for the per-stage split (not part of the timed numbers)
-    pt.set_profiling(True)
-    pt.process_device()
-    prof = pt.stats()
-    pt.set_profiling(False)
+    prof = profiled_pass(pt)
     tuned = pt.tuning()
-    cfg["tuned"] = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")}
-    cfg["tuning_passes"] = tuning_passes
+    tuned_d = {k: tuned[k] for k in TUNE_KEYS}
     pt.close()
 
     total_ms = sum(dev_ms)
@@ -506,7 +592,8 @@ def main():
                                 "terrain (1,048,576 rays per launch: 71.8 MB and 70.4 MB), scaled by the rays of an "
                                 "average full-size launch",
                 "alg_bytes": "52 B per closest-hit query (ray 32 B read, hit 20 B written; BVH bytes excluded)",
-                "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "top_stage": top}
+                "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "top_stage": top,
+                "hbm_stages": hbm_stages(prof, peak, info["spp"])}
     lat = sorted(dev_ms)
     out = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -519,13 +606,50 @@ def main():
            "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks.summary(t_timed, t_timed_end),
            "wall_ms_per_step": 1e3 * sum(wall) / args.steps}
     out["batches_per_step"] = batches / args.steps
+    out["scene_input"] = scene_input
+    extra = {}
+    if not args.no_extra and args.config == 1:
+        extra = bench_plain_extra(args, tuned_d)
+        out["c0"] = extra["c0"]
     if not args.no_forms:
         out["forms"] = bench_forms(args)
     if not args.no_stress:
         out["hit_sort_stress"] = bench_stress(args)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(yaml)
+    # last, so that a reader of the line's end sees them
+    out["tuned"] = dict(tuned_d, tuning_passes=tuning_passes, mrays_per_s=round(value, 1))
+    if "pinned" in extra:
+        out["pinned"] = extra["pinned"]
     print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1, help="scene config (1: large terrain scene, 0: box)")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
+    ap.add_argument("--no-extra", action="store_true", help="skip the stated-settings and box-scene measurements")
+    ap.add_argument("--tuning", default="auto",
+                    help="'auto' (the engine tunes itself) or batch_exp,bins,trace_block,ray_sort,hit_sort"
+                         "[,persistent[,digit_bits]]")
+    ap.add_argument("--stress-scale", type=float, default=1.0)
+    ap.add_argument("--serve-rates", default="100:6,600:3",
+                    help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
+    ap.add_argument("--forms-scenes", type=int, default=64)
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
 
 
 if __name__ == "__main__":

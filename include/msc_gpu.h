@@ -85,6 +85,8 @@ typedef struct msc_stats {
   double stage_ms[12];        /* per-stage device time when profiling is on (see MSC_STAGE_*) */
   uint64_t stage_launches[12];
   int width, height, spp, triangles, lights, iteration;
+  double load_ms;             /* msc_create: host wall time of the YAML + OBJ parse */
+  double bvh_ms;              /* msc_create: host wall time of the device BVH build and scene upload */
 } msc_stats;
 
 enum {
@@ -198,6 +200,8 @@ typedef struct msc_tuning {
   int digit_bits;     /* radix sort digit width: 4, 8 or 11 */
   int tuning;         /* read only: 1 while the autotuner is still sampling */
   int samples;        /* read only: candidate samples booked by the autotuner */
+  int ray_key_bits;   /* top bits of the 32-bit ray key that the ray sort orders: 16, 24 or 32;
+                         0 = 16 for one scene, 24 (scene and bin above the key) for several */
 } msc_tuning;
 typedef struct msc_tune_sample {
   int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent, digit_bits;

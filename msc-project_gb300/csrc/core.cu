@@ -680,9 +680,10 @@ uint64_t Core::graph_key() const {
   const uint64_t bins = bins_.nbins == 6 ? 0 : (bins_.nbins == 26 ? 1 : 2);
   const uint64_t pers = persistent_trace ? 1 : 0;
   const uint64_t dig = sort_digits == 4 ? 0 : (sort_digits == 8 ? 1 : 2);
+  const uint64_t kb = (uint64_t)ray_key_bits_used() / 8;  // 2, 3 or 4
   return ns | (k64 << 9) | ((uint64_t)hit_bits_ << 10) | ((uint64_t)ray_sort << 16) | ((uint64_t)hit_sort << 17) |
          ((uint64_t)merge_bins << 18) | ((uint64_t)wide_ << 19) | (bexp << 20) | (block << 25) | (bins << 27) |
-         (pers << 29) | (dig << 30) | (1ull << 63);
+         (pers << 29) | (dig << 30) | (kb << 32) | (1ull << 63);
 }
 
 void Core::drop_graph() {
@@ -715,11 +716,11 @@ int Core::enqueue_batch(int index, bool overlap) {
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      t.done(launch_ray_keys(bins_, plan_, B, ns > 1 ? kRayKeyBitsScenes : kRayKeyBits, keys_, st));
+      t.done(launch_ray_keys(bins_, plan_, B, ray_key_bits_used(), keys_, st));
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, ns > 1 ? kRayKeyBitsScenes : kRayKeyBits, ss_,
-                             st, errw, nb, sort_digits);
+    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, ray_key_bits_used(), ss_, st, errw, nb,
+                             sort_digits);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;
@@ -938,7 +939,13 @@ TuneChoice Core::choice() const {
   c.bins = bins_.nbins;
   c.persistent = persistent_trace;
   c.digit_bits = sort_digits;
+  c.ray_key_bits = ray_key_bits;
   return c;
+}
+
+int Core::ray_key_bits_used() const {
+  if (ray_key_bits == 16 || ray_key_bits == 24 || ray_key_bits == 32) return ray_key_bits;
+  return scenes_.size() > 1 ? kRayKeyBitsScenes : kRayKeyBits;
 }
 
 void Core::apply(const TuneChoice& c) {
@@ -950,6 +957,7 @@ void Core::apply(const TuneChoice& c) {
   bins_.nbins = (c.bins == 26 || c.bins == 98) ? c.bins : 6;
   persistent_trace = c.persistent;
   sort_digits = (c.digit_bits == 4 || c.digit_bits == 11) ? c.digit_bits : 8;
+  ray_key_bits = (c.ray_key_bits == 16 || c.ray_key_bits == 24 || c.ray_key_bits == 32) ? c.ray_key_bits : 0;
 }
 
 void Core::start_autotune(int windows) {
@@ -972,9 +980,16 @@ void Core::tune_begin_dim() {
       tune_cands_.push_back(t);
     };
     if (tune_dim_ == 0) {
-      // Batch size is not sampled: on a pass's first batches the bins hold too
-      // few rays to fill large batches, which biases short windows against
-      // them, while every measured workload ran fastest at the full capacity.
+      // Batch size: the capacity and two smaller powers of two.  Each sample
+      // is a whole run (a pass of the plain engine), whose first batches are
+      // short for every candidate alike.
+      int cap_exp = 0;
+      while ((2 << cap_exp) <= batch_cap_) ++cap_exp;
+      for (int e = std::max(10, cap_exp - 2); e <= cap_exp; ++e) {
+        TuneChoice c = base;
+        c.batch_exp = e;
+        add(c);
+      }
     } else if (tune_dim_ == 1) {
       for (int nb : {6, 26, 98}) {
         TuneChoice c = base;

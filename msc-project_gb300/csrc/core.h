@@ -83,6 +83,7 @@ struct TuneChoice {
   int bins = 6;         // direction bins: 6, 26 or 98
   bool persistent = false;  // persistent traversal with per-lane ray refill
   int digit_bits = 8;       // radix sort digit width: 4, 8 or 11
+  int ray_key_bits = 0;     // top bits of the ray key sorted: 16, 24 or 32 (0: 16, or 24 with several scenes)
 };
 
 struct TuneSample {
@@ -109,6 +110,7 @@ class Core {
   int trace_block = 128;          // traversal block size
   bool persistent_trace = false;  // persistent traversal kernels (8-wide BVH)
   int sort_digits = 8;            // radix sort digit width (4, 8 or 11)
+  int ray_key_bits = 0;           // ray key bits sorted (0: the default for the scene count)
 
   // Online autotuner: while on, each run_all (a render pass or a batched
   // run) is one timed sample of the next candidate choice (coordinate
@@ -147,6 +149,7 @@ class Core {
   size_t sample_capacity() const { return sample_cap_; }
   Film film() const { return film_; }
   int batch_cap() const { return batch_cap_; }
+  int ray_key_bits_used() const;
   int batch_size() const { return batch_size_; }
   double now() const;
   // Closest hit / occlusion of explicit rays against scene 0 (stage entry points).

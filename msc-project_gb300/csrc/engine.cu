@@ -119,6 +119,7 @@ struct msc_handle {
   std::vector<float> h_pixels;  // page-locked once sized (pixels_pinned), for fast image copies
   bool pixels_pinned = false;
   msc_stats stats;
+  double load_ms = 0, bvh_ms = 0;  // msc_create's scene parse and device BVH build, wall clock
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
   ~msc_handle() {
     if (pixels_pinned) cudaHostUnregister(h_pixels.data());
@@ -155,11 +156,17 @@ int plain_setup(msc_handle* h) {
   }
   if (d.ext.autotune) h->core.start_autotune();
   int sid = 0;
+  const auto t0 = std::chrono::steady_clock::now();
   rc = h->core.add_scene(d, &sid);
   if (rc != MSC_OK) {
     h->err = h->core.err;
     return rc;
   }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    h->err = "device BVH build failed";
+    return MSC_ERR_CUDA;
+  }
+  h->bvh_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   JobSpec spec;
   spec.scene = sid;
   rc = h->core.add_job(spec, &h->job);
@@ -289,6 +296,7 @@ int msc_create(const char* yaml_path, msc_handle** out) {
   }
   std::string err;
   bool ok = false;
+  const auto t0 = std::chrono::steady_clock::now();
   try {
     ok = load_scene(yaml_path, &h->desc, &err);
   } catch (const std::exception& e) {
@@ -299,6 +307,7 @@ int msc_create(const char* yaml_path, msc_handle** out) {
     delete h;
     return MSC_ERR_SCENE;
   }
+  h->load_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   int rc = guarded(&h->err, [&] { return plain_setup(h); });
   if (rc != MSC_OK) {
     g_create_error = h->err;
@@ -427,6 +436,8 @@ int msc_get_stats(msc_handle* h, msc_stats* out) {
   out->triangles = (int)h->desc.tri_geom.size();
   out->lights = (int)h->desc.lights.size();
   out->iteration = h->iteration;
+  out->load_ms = h->load_ms;
+  out->bvh_ms = h->bvh_ms;
   return MSC_OK;
 }
 
@@ -956,6 +967,7 @@ static void tuning_of(Core& c, msc_tuning* out) {
   out->digit_bits = t.digit_bits;
   out->tuning = c.tuning() ? 1 : 0;
   out->samples = (int)c.tune_log.size();
+  out->ray_key_bits = t.ray_key_bits;
 }
 
 int msc_batch_get_tuning(msc_batch* b, msc_tuning* out) {
@@ -975,9 +987,10 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   if (in->batch_exponent < 6 || (1 << std::min(in->batch_exponent, 30)) > core.batch_cap() ||
       (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256) ||
       (in->bins != 6 && in->bins != 26 && in->bins != 98) ||
-      (in->digit_bits != 4 && in->digit_bits != 8 && in->digit_bits != 11)) {
-    *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, bins not 6, 26 or 98, or "
-           "digit width not 4, 8 or 11";
+      (in->digit_bits != 4 && in->digit_bits != 8 && in->digit_bits != 11) ||
+      (in->ray_key_bits != 0 && in->ray_key_bits != 16 && in->ray_key_bits != 24 && in->ray_key_bits != 32)) {
+    *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, bins not 6, 26 or 98, "
+           "digit width not 4, 8 or 11, or ray key bits not 0, 16, 24 or 32";
     return MSC_ERR_ARG;
   }
   TuneChoice c;
@@ -988,6 +1001,7 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
   c.bins = in->bins;
   c.persistent = in->persistent != 0;
   c.digit_bits = in->digit_bits;
+  c.ray_key_bits = in->ray_key_bits;
   core.stop_autotune();
   core.apply(c);
   return MSC_OK;

@@ -32,7 +32,8 @@ class _Stats(C.Structure):
     _fields_ = [("closest_queries", C.c_uint64), ("shadow_queries", C.c_uint64), ("batches", C.c_uint64),
                 ("kernel_launches", C.c_uint64), ("process_ms", C.c_double), ("stage_ms", C.c_double * 12),
                 ("stage_launches", C.c_uint64 * 12), ("width", C.c_int), ("height", C.c_int), ("spp", C.c_int),
-                ("triangles", C.c_int), ("lights", C.c_int), ("iteration", C.c_int)]
+                ("triangles", C.c_int), ("lights", C.c_int), ("iteration", C.c_int), ("load_ms", C.c_double),
+                ("bvh_ms", C.c_double)]
 
 
 class _JobDesc(C.Structure):
@@ -210,8 +211,9 @@ class Pathtracer:
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
     def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False,
-                   digit_bits=8):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0)
+                   digit_bits=8, ray_key_bits=0):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0,
+                    ray_key_bits)
         _check(self._lib.msc_set_tuning(self._h, C.byref(t)), self._h)
 
     def stats(self):
@@ -365,7 +367,7 @@ def scene_load_host(yaml_path):
 class _Tuning(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
                 ("bins", C.c_int), ("persistent", C.c_int), ("digit_bits", C.c_int), ("tuning", C.c_int),
-                ("samples", C.c_int)]
+                ("samples", C.c_int), ("ray_key_bits", C.c_int)]
 
 
 class _TuneSample(C.Structure):
@@ -462,8 +464,9 @@ class Batch:
         return {k: getattr(t, k) for k, _ in _Tuning._fields_}
 
     def set_tuning(self, batch_exponent=20, trace_block=128, ray_sort=True, hit_sort=True, bins=6, persistent=False,
-                   digit_bits=8):
-        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0)
+                   digit_bits=8, ray_key_bits=0):
+        t = _Tuning(batch_exponent, trace_block, int(ray_sort), int(hit_sort), bins, int(persistent), digit_bits, 0, 0,
+                    ray_key_bits)
         self._check(self._lib.msc_batch_set_tuning(self._b, C.byref(t)))
 
     def tune_log(self):

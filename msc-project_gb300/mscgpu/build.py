@@ -25,6 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["sort.cu", "bvh.cu", "render.cu", "core.cu", "engine.cu", "noalloc.cu"]
 CPP_SOURCES = ["scene.cpp", "scenegen.cpp", "imageio.cpp"]
 CLI = os.path.join(HERE, "msc-gpu")
+SCENEGEN = os.path.join(HERE, "msc-scenegen")
 
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-ftz=false", "-prec-div=true", "-prec-sqrt=true",
@@ -49,6 +50,17 @@ def _stale(obj, srcs):
         return True
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_scenegen(force=False):
+    """The scene generator as a host-only executable (no CUDA library loaded):
+    the benchmark's CPU arm writes its scene files with it."""
+    os.makedirs(OUT_DIR, exist_ok=True)
+    srcs = [os.path.join(CSRC, "scenegen.cpp"), os.path.join(CSRC, "scenegen_main.cpp"), os.path.join(CSRC, "scene.h"),
+            os.path.join(CSRC, "dmath.h")]
+    if force or _stale(SCENEGEN, srcs):
+        _run(["g++"] + CXX_FLAGS + srcs[:2] + ["-o", SCENEGEN], os.path.join(OUT_DIR, "scenegen.log"))
+    return SCENEGEN
 
 
 def build(verbose=False, force=False):
@@ -79,6 +91,7 @@ def build(verbose=False, force=False):
     if force or _stale(CLI, [cli_src, LIB]):
         _run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"), cli_src, "-o", CLI, "-L" + HERE,
               "-lmscgpu", "-Wl,-rpath,$ORIGIN"], os.path.join(OUT_DIR, "cli.log"))
+    build_scenegen(force)
     return LIB
 
 

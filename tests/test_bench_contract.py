@@ -27,3 +27,17 @@ def test_reference_arm_prints_one_contract_line(built):
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["config"]["workload"].startswith("terrain")
+
+
+def test_reference_arm_loads_no_library_of_the_renderer(built):
+    """The CPU arm may load the oracle only: neither libmscgpu.so nor the CUDA
+    runtime appear among the process's mapped files after a run."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3', "
+            "'--scale', '0.25']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPPED', 'libmscgpu' in maps, 'liboracle' in maps, 'libcuda.so' in maps, file=sys.stderr)")
+    p = subprocess.run([sys.executable, "-c", code], cwd=REPO, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                       text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    line = [l for l in p.stderr.splitlines() if l.startswith("MAPPED")][-1]
+    assert line == "MAPPED False True False", line
