@@ -3,7 +3,9 @@
 // See scene.h for the reference files each part follows.
 #include "scene.h"
 
+#include <algorithm>
 #include <cctype>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -12,6 +14,7 @@
 #include <map>
 #include <unordered_map>
 #include <sstream>
+#include <thread>
 
 namespace mscg {
 
@@ -347,37 +350,49 @@ float next_float(const char*& tok) {
   return f;
 }
 
-VIdx parse_triple(const char*& tok, int nv, int nvn, int nvt) {
-  VIdx vi{-1, -1, -1};
-  vi.v = fix_index(atoi(tok), nv);
+// One face corner as written: the atoi value of each index, kAbsent where the
+// corner has no such index.  Negative (relative) indices are resolved once the
+// element counts before the face line are known.
+constexpr int kAbsent = INT_MIN;
+struct RawCorner { int v, vt, vn; };
+
+// parseTriple's token rules (tiny_obj_loader.cpp:309-345): "v", "v/vt", "v//vn", "v/vt/vn".
+RawCorner parse_triple_raw(const char*& tok) {
+  RawCorner r{atoi(tok), kAbsent, kAbsent};
   tok += strcspn(tok, "/ \t\r");
-  if (tok[0] != '/') return vi;
+  if (tok[0] != '/') return r;
   ++tok;
   if (tok[0] == '/') {
     ++tok;
-    vi.vn = fix_index(atoi(tok), nvn);
+    r.vn = atoi(tok);
     tok += strcspn(tok, "/ \t\r");
-    return vi;
+    return r;
   }
-  vi.vt = fix_index(atoi(tok), nvt);
+  r.vt = atoi(tok);
   tok += strcspn(tok, "/ \t\r");
-  if (tok[0] != '/') return vi;
+  if (tok[0] != '/') return r;
   ++tok;
-  vi.vn = fix_index(atoi(tok), nvn);
+  r.vn = atoi(tok);
   tok += strcspn(tok, "/ \t\r");
-  return vi;
+  return r;
 }
 
-}  // namespace
-
-bool obj_load_text(const char* text, size_t len, ObjMesh* out) {
+// What one contiguous run of whole lines holds, in file order.
+struct ObjChunk {
   std::vector<float> v, vn, vt;
-  std::vector<std::vector<VIdx>> faces;
+  std::vector<RawCorner> corners;
+  std::vector<uint32_t> face_first;           // first corner of each face
+  std::vector<int> face_nv, face_nvn, face_nvt;  // this chunk's element counts before each face line
+};
+
+// The line loop of LoadObj (tiny_obj_loader.cpp:643-891) for the v, vn, vt and
+// f records over text[begin, end), which starts at a line start.
+void parse_obj_lines(const char* text, size_t begin, size_t end, ObjChunk* c) {
   std::string line;
-  size_t pos = 0;
-  while (pos < len) {
+  size_t pos = begin;
+  while (pos < end) {
     size_t e = pos;
-    while (e < len && text[e] != '\n') ++e;
+    while (e < end && text[e] != '\n') ++e;
     line.assign(text + pos, e - pos);
     pos = e + 1;
     if (!line.empty() && line.back() == '\r') line.pop_back();
@@ -389,71 +404,183 @@ bool obj_load_text(const char* text, size_t len, ObjMesh* out) {
     if (tok[0] == 'v' && is_sp(tok[1])) {
       tok += 2;
       float x = next_float(tok), y = next_float(tok), z = next_float(tok);
-      v.push_back(x); v.push_back(y); v.push_back(z);
+      c->v.push_back(x); c->v.push_back(y); c->v.push_back(z);
       continue;
     }
     if (tok[0] == 'v' && tok[1] == 'n' && is_sp(tok[2])) {
       tok += 3;
       float x = next_float(tok), y = next_float(tok), z = next_float(tok);
-      vn.push_back(x); vn.push_back(y); vn.push_back(z);
+      c->vn.push_back(x); c->vn.push_back(y); c->vn.push_back(z);
       continue;
     }
     if (tok[0] == 'v' && tok[1] == 't' && is_sp(tok[2])) {
       tok += 3;
       float x = next_float(tok), y = next_float(tok);
-      vt.push_back(x); vt.push_back(y);
+      c->vt.push_back(x); c->vt.push_back(y);
       continue;
     }
     if (tok[0] == 'f' && is_sp(tok[1])) {
       tok += 2;
       tok += strspn(tok, " \t");
-      std::vector<VIdx> face;
+      c->face_first.push_back((uint32_t)c->corners.size());
+      c->face_nv.push_back((int)(c->v.size() / 3));
+      c->face_nvn.push_back((int)(c->vn.size() / 3));
+      c->face_nvt.push_back((int)(c->vt.size() / 2));
       while (!is_nl(tok[0])) {
-        face.push_back(parse_triple(tok, (int)(v.size() / 3), (int)(vn.size() / 3), (int)(vt.size() / 2)));
+        c->corners.push_back(parse_triple_raw(tok));
         tok += strspn(tok, " \t\r");
       }
-      faces.push_back(std::move(face));
       continue;
     }
   }
-  // exportFaceGroupToShape (tiny_obj_loader.cpp:366-412): fan triangulation,
-  // one vertex per distinct (v, vt, vn) triple in first-use order.
-  out->positions.clear(); out->normals.clear(); out->texcoords.clear(); out->indices.clear();
-  std::unordered_map<VIdx, uint32_t, VIdxHash, VIdxEq> cache;
-  cache.reserve(v.size() / 3 + 16);
-  auto vertex = [&](const VIdx& i) -> uint32_t {
-    auto it = cache.find(i);
-    if (it != cache.end()) return it->second;
-    if (i.v < 0 || (size_t)(3 * i.v + 2) >= v.size()) return UINT32_MAX;
-    out->positions.push_back(v[3 * i.v + 0]);
-    out->positions.push_back(v[3 * i.v + 1]);
-    out->positions.push_back(v[3 * i.v + 2]);
-    if (i.vn >= 0 && (size_t)(3 * i.vn + 2) < vn.size()) {
-      out->normals.push_back(vn[3 * i.vn + 0]);
-      out->normals.push_back(vn[3 * i.vn + 1]);
-      out->normals.push_back(vn[3 * i.vn + 2]);
+}
+
+template <class F>
+void parallel_for(int workers, F&& fn) {
+  std::vector<std::thread> pool;
+  for (int w = 1; w < workers; ++w) pool.emplace_back(fn, w);
+  fn(0);
+  for (auto& t : pool) t.join();
+}
+
+}  // namespace
+
+// LoadObj with tinyobjloader's results (positions, texcoords, normals, fan
+// triangles with one vertex per distinct (v, vt, vn) triple in first-use
+// order), read in parallel:
+//   1. the text is cut at line starts into one run per worker, and each run's
+//      v / vn / vt / f records are parsed on their own;
+//   2. per-run element counts give every face line the global counts that
+//      resolve its relative (negative) indices;
+//   3. distinct corners are found by hash shards: worker w keeps the corners
+//      whose triple hashes to w, in file order, so the first use of a triple
+//      is known; a prefix sum over first uses numbers the vertices in
+//      first-use order (the fan visits a face's corners in their written
+//      order, so first use in corner order is first use in fan order);
+//   4. vertices, normals, texcoords and fan indices are written at offsets
+//      from prefix sums.
+bool obj_load_text(const char* text, size_t len, ObjMesh* out) {
+  unsigned hw = std::thread::hardware_concurrency();
+  const int workers = len < (1u << 20) ? 1 : (int)std::max(1u, std::min(hw ? hw : 1u, 32u));
+  // 1. runs of whole lines
+  std::vector<size_t> cut((size_t)workers + 1, len);
+  cut[0] = 0;
+  for (int w = 1; w < workers; ++w) {
+    size_t p = std::max(cut[w - 1], len * (size_t)w / (size_t)workers);
+    while (p < len && p > 0 && text[p - 1] != '\n') ++p;
+    cut[w] = p;
+  }
+  std::vector<ObjChunk> ch((size_t)workers);
+  parallel_for(workers, [&](int w) { parse_obj_lines(text, cut[w], cut[w + 1], &ch[w]); });
+  // 2. global element counts and concatenated arrays
+  std::vector<size_t> ov(workers + 1, 0), ovn(workers + 1, 0), ovt(workers + 1, 0), oc(workers + 1, 0),
+      of(workers + 1, 0);
+  for (int w = 0; w < workers; ++w) {
+    ov[w + 1] = ov[w] + ch[w].v.size();
+    ovn[w + 1] = ovn[w] + ch[w].vn.size();
+    ovt[w + 1] = ovt[w] + ch[w].vt.size();
+    oc[w + 1] = oc[w] + ch[w].corners.size();
+    of[w + 1] = of[w] + ch[w].face_first.size();
+  }
+  const size_t C = oc[workers], F = of[workers];
+  std::vector<float> v(ov[workers]), vn(ovn[workers]), vt(ovt[workers]);
+  std::vector<VIdx> corner(C);
+  std::vector<uint32_t> face_first(F + 1);
+  face_first[F] = (uint32_t)C;
+  parallel_for(workers, [&](int w) {
+    const ObjChunk& c = ch[w];
+    std::copy(c.v.begin(), c.v.end(), v.begin() + ov[w]);
+    std::copy(c.vn.begin(), c.vn.end(), vn.begin() + ovn[w]);
+    std::copy(c.vt.begin(), c.vt.end(), vt.begin() + ovt[w]);
+    const size_t nf = c.face_first.size();
+    for (size_t f = 0; f < nf; ++f) {
+      const uint32_t b = c.face_first[f], e = f + 1 < nf ? c.face_first[f + 1] : (uint32_t)c.corners.size();
+      face_first[of[w] + f] = (uint32_t)(oc[w] + b);
+      const int nv = (int)(ov[w] / 3) + c.face_nv[f], nvn = (int)(ovn[w] / 3) + c.face_nvn[f],
+                nvt = (int)(ovt[w] / 2) + c.face_nvt[f];
+      for (uint32_t k = b; k < e; ++k) {
+        const RawCorner& r = c.corners[k];
+        VIdx& x = corner[oc[w] + k];
+        x.v = fix_index(r.v, nv);
+        x.vt = r.vt == kAbsent ? -1 : fix_index(r.vt, nvt);
+        x.vn = r.vn == kAbsent ? -1 : fix_index(r.vn, nvn);
+      }
     }
-    if (i.vt >= 0 && (size_t)(2 * i.vt + 1) < vt.size()) {
-      out->texcoords.push_back(vt[2 * i.vt + 0]);
-      out->texcoords.push_back(vt[2 * i.vt + 1]);
+  });
+  ch.clear();
+  ch.shrink_to_fit();
+  // faces of fewer than three corners are dropped before any vertex is made
+  std::vector<uint8_t> live(C, 0);
+  parallel_for(workers, [&](int w) {
+    for (size_t f = F * (size_t)w / workers; f < F * (size_t)(w + 1) / workers; ++f)
+      if (face_first[f + 1] - face_first[f] >= 3)
+        for (uint32_t k = face_first[f]; k < face_first[f + 1]; ++k) live[k] = 1;
+  });
+  // 3. first use of each distinct triple, by hash shard
+  std::vector<uint32_t> first(C, UINT32_MAX);  // corner -> the corner of its triple's first use
+  VIdxHash hasher;
+  parallel_for(workers, [&](int w) {
+    std::unordered_map<VIdx, uint32_t, VIdxHash, VIdxEq> seen;
+    seen.reserve(v.size() / 3 / workers + 16);
+    for (size_t k = 0; k < C; ++k) {
+      if (!live[k]) continue;
+      const VIdx& x = corner[k];
+      if ((int)(hasher(x) % (size_t)workers) != w) continue;
+      auto it = seen.emplace(x, (uint32_t)k).first;
+      first[k] = it->second;
     }
-    uint32_t idx = (uint32_t)(out->positions.size() / 3 - 1);
-    cache[i] = idx;
-    return idx;
-  };
-  for (const auto& f : faces) {
-    if (f.size() < 3) continue;
-    VIdx i0 = f[0], i2 = f[1], i1;
-    for (size_t k = 2; k < f.size(); ++k) {
-      i1 = i2;
-      i2 = f[k];
-      uint32_t a = vertex(i0), b = vertex(i1), c = vertex(i2);
-      if (a == UINT32_MAX || b == UINT32_MAX || c == UINT32_MAX) return false;
-      out->indices.push_back(a);
-      out->indices.push_back(b);
-      out->indices.push_back(c);
+  });
+  std::vector<uint32_t> vid(C, UINT32_MAX);  // vertex number of a first-use corner
+  uint32_t nverts = 0;
+  for (size_t k = 0; k < C; ++k)
+    if (live[k] && first[k] == (uint32_t)k) {
+      const VIdx& x = corner[k];
+      if (x.v < 0 || (size_t)(3 * x.v + 2) >= v.size()) return false;  // a face names a missing vertex
+      vid[k] = nverts++;
+    }
+  // 4. vertex attributes (normals / texcoords only where the triple names a valid one)
+  out->positions.assign((size_t)3 * nverts, 0.f);
+  out->normals.clear();
+  out->texcoords.clear();
+  out->indices.clear();
+  std::vector<uint32_t> rep(nverts);
+  for (size_t k = 0; k < C; ++k)
+    if (vid[k] != UINT32_MAX) rep[vid[k]] = (uint32_t)k;
+  for (uint32_t i = 0; i < nverts; ++i) {
+    const VIdx& x = corner[rep[i]];
+    out->positions[3 * i + 0] = v[3 * x.v + 0];
+    out->positions[3 * i + 1] = v[3 * x.v + 1];
+    out->positions[3 * i + 2] = v[3 * x.v + 2];
+    if (x.vn >= 0 && (size_t)(3 * x.vn + 2) < vn.size()) {
+      out->normals.push_back(vn[3 * x.vn + 0]);
+      out->normals.push_back(vn[3 * x.vn + 1]);
+      out->normals.push_back(vn[3 * x.vn + 2]);
+    }
+    if (x.vt >= 0 && (size_t)(2 * x.vt + 1) < vt.size()) {
+      out->texcoords.push_back(vt[2 * x.vt + 0]);
+      out->texcoords.push_back(vt[2 * x.vt + 1]);
     }
   }
+  // fan triangles (exportFaceGroupToShape, tiny_obj_loader.cpp:366-412)
+  std::vector<size_t> tri_at(F + 1, 0);
+  for (size_t f = 0; f < F; ++f) {
+    const uint32_t k = face_first[f + 1] - face_first[f];
+    tri_at[f + 1] = tri_at[f] + (k >= 3 ? k - 2 : 0);
+  }
+  out->indices.resize(3 * tri_at[F]);
+  parallel_for(workers, [&](int w) {
+    for (size_t f = F * (size_t)w / workers; f < F * (size_t)(w + 1) / workers; ++f) {
+      const uint32_t b = face_first[f], e = face_first[f + 1];
+      if (e - b < 3) continue;
+      uint32_t* o = out->indices.data() + 3 * tri_at[f];
+      const uint32_t i0 = vid[first[b]];
+      for (uint32_t k = b + 2; k < e; ++k) {
+        *o++ = i0;
+        *o++ = vid[first[k - 1]];
+        *o++ = vid[first[k]];
+      }
+    }
+  });
   return true;
 }
 
