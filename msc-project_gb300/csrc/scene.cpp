@@ -585,9 +585,18 @@ bool obj_load_text(const char* text, size_t len, ObjMesh* out) {
 }
 
 bool obj_load_file(const std::string& path, ObjMesh* out, std::string* err) {
-  std::ifstream f(path, std::ios::binary);
+  FILE* f = fopen(path.c_str(), "rb");
   if (!f) { *err = "cannot open OBJ file [" + path + "]"; return false; }
-  std::string s((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  std::string s;
+  if (fseek(f, 0, SEEK_END) == 0) {
+    const long size = ftell(f);
+    if (size > 0) {
+      s.resize((size_t)size);
+      rewind(f);
+      s.resize(fread(&s[0], 1, (size_t)size, f));
+    }
+  }
+  fclose(f);
   if (!obj_load_text(s.data(), s.size(), out)) { *err = "OBJ face references a missing vertex in [" + path + "]"; return false; }
   return true;
 }
@@ -949,20 +958,29 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
     }
   }
 
+  const int workers = (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 32u));
   auto add_tris = [&](const std::vector<float>& pos3, const std::vector<uint32_t>& idx, const std::vector<float>& uv,
                       int geom, bool light) {
-    size_t nt = idx.size() / 3;
-    for (size_t t = 0; t < nt; ++t) {
-      for (int k = 0; k < 3; ++k) {
-        uint32_t vi = idx[3 * t + k];
-        for (int a = 0; a < 3; ++a) S.tri_v.push_back(pos3[3 * vi + a]);
-        bool has_uv = (size_t)(2 * vi + 1) < uv.size();
-        S.tri_uv.push_back(has_uv ? uv[2 * vi + 0] : 0.f);
-        S.tri_uv.push_back(has_uv ? uv[2 * vi + 1] : 0.f);
+    const size_t nt = idx.size() / 3, b = S.tri_geom.size();
+    S.tri_v.resize(9 * (b + nt));
+    S.tri_uv.resize(6 * (b + nt));
+    S.tri_geom.resize(b + nt, geom);
+    S.tri_is_light.resize(b + nt, light ? 1 : 0);
+    auto fill = [&](size_t t0, size_t t1) {
+      for (size_t t = t0; t < t1; ++t) {
+        float* tv = &S.tri_v[9 * (b + t)];
+        float* tu = &S.tri_uv[6 * (b + t)];
+        for (int k = 0; k < 3; ++k) {
+          const uint32_t vi = idx[3 * t + k];
+          for (int a = 0; a < 3; ++a) tv[3 * k + a] = pos3[3 * vi + a];
+          const bool has_uv = (size_t)(2 * vi + 1) < uv.size();
+          tu[2 * k + 0] = has_uv ? uv[2 * vi + 0] : 0.f;
+          tu[2 * k + 1] = has_uv ? uv[2 * vi + 1] : 0.f;
+        }
       }
-      S.tri_geom.push_back(geom);
-      S.tri_is_light.push_back(light ? 1 : 0);
-    }
+    };
+    if (nt < (1u << 16)) fill(0, nt);
+    else parallel_for(workers, [&](int w) { fill(nt * w / workers, nt * (w + 1) / workers); });
   };
 
   if (scene.kind != YNode::Map && scene.kind != YNode::Null) return c.fail("scene document must be a mapping");
@@ -992,7 +1010,12 @@ bool load_scene(const std::string& yaml_path, SceneDesc* out, std::string* err) 
       const ObjMesh& mesh = *found;
       Affine3 xf = make_trs_xyz(t, r, s);  // PolygonObject.cpp:17-22
       std::vector<float> pos(mesh.positions.size());
-      for (size_t i = 0; i + 2 < mesh.positions.size(); i += 3) xf_host_point(xf, &mesh.positions[i], &pos[i]);
+      const size_t nvert = mesh.positions.size() / 3;
+      auto xf_range = [&](size_t v0, size_t v1) {
+        for (size_t i = v0; i < v1; ++i) xf_host_point(xf, &mesh.positions[3 * i], &pos[3 * i]);
+      };
+      if (nvert < (1u << 16)) xf_range(0, nvert);
+      else parallel_for(workers, [&](int w) { xf_range(nvert * w / workers, nvert * (w + 1) / workers); });
       GeomRec g;
       g.shader = shader;
       g.first_prim = (int)S.tri_geom.size();

@@ -74,7 +74,7 @@ def test_fan_and_dedup_semantics(built, obj_dir):
     assert pos.shape[0] == tex.shape[0]
 
 
-@pytest.mark.parametrize("cfg,scale", [(100, 1.0), (0, 0.25), (1, 0.02), (2, 0.02)])
+@pytest.mark.parametrize("cfg,scale", [(100, 1.0), (0, 0.25), (1, 0.02), (2, 0.02), (1, 0.3)])
 def test_product_scene_matches_oracle_loader(built, scene_dir, cfg, scale):
     mscgpu, oracle = built
     y = mscgpu.generate_scene(cfg, 99, str(scene_dir / ("load%d" % cfg)), scale=scale)
@@ -166,3 +166,62 @@ def test_missing_scene_file_fails_before_any_gpu_call(built, tmp_path):
     with pytest.raises(mscgpu.MscError) as e:
         mscgpu.Pathtracer(str(tmp_path / "absent.yaml"))
     assert e.value.code == -2 and "cannot open" in str(e.value)
+
+
+def _random_obj(path, records, seed):
+    """A large OBJ (several MB, so the reader splits it between workers) of
+    random v / vt / vn records and faces of 2-5 corners in every index form,
+    with relative (negative) indices and repeated triples."""
+    rng = np.random.default_rng(seed)
+    lines, nv, nvt, nvn = [], 0, 0, 0
+
+    def idx(n):
+        if rng.random() < 0.3:
+            return -int(rng.integers(1, min(n, 50) + 1))
+        if rng.random() < 0.05:
+            return int(rng.integers(1, min(n, 8) + 1))
+        return int(rng.integers(1, n + 1))
+    for _ in range(records):
+        r = rng.random()
+        if r < 0.35 or nv < 4:
+            lines.append("v %.6f %.6f %.6f" % tuple(rng.uniform(-5, 5, 3)))
+            nv += 1
+        elif r < 0.45:
+            lines.append("vt %.6f %.6f" % tuple(rng.uniform(0, 1, 2)))
+            nvt += 1
+        elif r < 0.52:
+            lines.append("vn %.6f %.6f %.6f" % tuple(rng.uniform(-1, 1, 3)))
+            nvn += 1
+        elif r < 0.53:
+            lines.append("# f 1 2 3")
+        else:
+            corners = []
+            for _ in range(int(rng.choice([2, 3, 3, 4, 5]))):
+                t, v = rng.random(), idx(nv)
+                if t < 0.25 or (nvt == 0 and nvn == 0):
+                    corners.append("%d" % v)
+                elif t < 0.5 and nvt:
+                    corners.append("%d/%d" % (v, idx(nvt)))
+                elif t < 0.75 and nvn:
+                    corners.append("%d//%d" % (v, idx(nvn)))
+                elif nvt and nvn:
+                    corners.append("%d/%d/%d" % (v, idx(nvt), idx(nvn)))
+                else:
+                    corners.append("%d" % v)
+            lines.append("f " + " ".join(corners))
+    with open(path, "w", newline="") as f:
+        f.write("\r\n".join(lines) + "\r\n")
+
+
+def test_parallel_obj_reader_matches_reference_on_a_large_file(built, tmp_path):
+    """The reader splits files of 1 MB and more between worker threads; the
+    result must stay tinyobjloader's (vertex order, fans, relative indices)."""
+    mscgpu, oracle = built
+    path = str(tmp_path / "large.obj")
+    _random_obj(path, 120000, 11)
+    assert os.path.getsize(path) > (1 << 20)
+    mine = mscgpu.obj_load(path)
+    _same(mine, oracle.obj_load(path))
+    ref = oracle.ref_tinyobj()
+    if ref is not None:
+        _same(mine, oracle.obj_load(path, library=ref))
