@@ -224,12 +224,96 @@ def log_uniform_int(rng, lo, hi):
 def random_job(rng, scene, bbox, res_choices, spp_lo, spp_hi, depth_lo=4, depth_hi=10):
     res = int(rng.choice(res_choices))
     return dict(scene=scene, width=res, height=res, spp=log_uniform_int(rng, spp_lo, spp_hi), min_depth=3,
-                max_depth=int(rng.integers(depth_lo, depth_hi + 1)), camera=sphere_camera(rng, bbox),
+                max_depth=int(rng.integers(depth_lo, depth_hi + 1)),
+                camera=sphere_camera(rng, bbox) if bbox is not None else None,
                 seed=int(rng.integers(1, 1 << 30)))
 
 
 def job_paths(j):
     return j["width"] * j["height"] * j["spp"]
+
+
+def job_yaml(scene_yaml, job, out_path):
+    """One job as the reference's engine takes it: a copy of the scene file with
+    the job's image size, sample count, depth limits, pinhole camera and seed
+    (msc::Pathtracer reads them from the file and has no setter for them).  The
+    plain engine's autotuner is switched off: a one-pass job renders with the
+    engine's default choice (batches of 8x the scene's `bin exponent`)."""
+    import re
+    text = open(scene_yaml).read()
+    setup, rest = text.split("---", 1)
+    t, r, f = job["camera"]
+    subs = [(r"width: \d+", "width: %d" % job["width"]), (r"height: \d+", "height: %d" % job["height"]),
+            (r"sample base: \d+", "sample base: 1"), (r"min depth: \d+", "min depth: %d" % job["min_depth"]),
+            (r"max depth: \d+", "max depth: %d" % job["max_depth"]),
+            (r"type: ThinLens", "type: PinHole"),
+            (r"translation: \[[^\]]*\]", "translation: [%r, %r, %r]" % tuple(float(x) for x in t)),
+            (r"rotation: \[[^\]]*\]", "rotation: [%r, %r, %r]" % tuple(float(x) for x in r)),
+            (r"focal length: [^\n]*", "focal length: %r" % float(f))]
+    for pat, rep in subs:
+        setup = re.sub(pat, rep, setup, count=1)
+    setup = re.sub(r"\n  focal distance: [^\n]*|\n  aperture: [^\n]*", "", setup)
+    scene_doc, ext = rest.rsplit("---", 1)
+    ext = re.sub(r"\n  seed: \d+", "", ext).rstrip("\n")
+    ext += "\n  seed: %d\n  samples per pixel: %d\n  autotune: 0\n" % (job["seed"], job["spp"])
+    with open(out_path, "w") as fo:
+        fo.write(setup + "---" + scene_doc + "---" + ext)
+    # the scene's OBJ files sit next to its YAML: link them beside the copy
+    src_dir, dst_dir = os.path.dirname(scene_yaml), os.path.dirname(out_path)
+    if os.path.abspath(src_dir) != os.path.abspath(dst_dir):
+        for fn in os.listdir(src_dir):
+            if fn.endswith(".obj") and not os.path.exists(os.path.join(dst_dir, fn)):
+                os.symlink(os.path.join(src_dir, fn), os.path.join(dst_dir, fn))
+    return out_path
+
+
+def plain_api_jobs(scenes, jobs, max_jobs, limit_s):
+    """The jobs rendered one by one through the reference's engine interface:
+    msc_create from the job's scene file (scene parse + BVH build), one
+    msc_process, msc_image, msc_destroy - as the reference's batch mode drives
+    msc::Pathtracer (src/main.cpp:137-215).  Wall-clock per job."""
+    import mscgpu
+    rows, t_all = [], time.time()
+    for i, j in enumerate(jobs[:max_jobs]):
+        d = os.path.join(tempfile.gettempdir(), "msc_bench_jobs", "job%d" % i)
+        os.makedirs(d, exist_ok=True)
+        y = job_yaml(scenes[j["scene"]], j, os.path.join(d, "scene.yaml"))
+        t = time.time()
+        pt = mscgpu.Pathtracer(y)
+        t_create = time.time() - t
+        pt.process()
+        pt.image()
+        st = pt.stats()
+        pt.close()
+        rows.append({"create_s": t_create, "wall_s": time.time() - t,
+                     "rays": st["closest_queries"] + st["shadow_queries"], "busy_ms": st["gpu_busy_ms"]})
+        if time.time() - t_all > limit_s:
+            break
+    wall = sum(r["wall_s"] for r in rows)
+    rays = sum(r["rays"] for r in rows)
+    render = sum(r["wall_s"] - r["create_s"] for r in rows)
+    return {"jobs": len(rows), "mrays_per_s": rays / wall / 1e6 if wall else None,
+            "render_only_mrays_per_s": rays / render / 1e6 if render else None,
+            "create_s_total": sum(r["create_s"] for r in rows), "wall_s": wall}
+
+
+def rel_mse_against_fp64(b, scenes, jobs, ids, picks):
+    """Relative MSE of batched job images against the FP64 oracle rendering the
+    same jobs (same cameras, sample counts and per-path random sequences)."""
+    import numpy as np
+    from oracle import oracle as O
+    out = []
+    for k in picks:
+        j = jobs[k]
+        s = O.Scene(scenes[j["scene"]])
+        t, r, f = j["camera"]
+        s.set_job(width=j["width"], height=j["height"], spp=j["spp"], min_depth=j["min_depth"],
+                  max_depth=j["max_depth"], cam_t=t, cam_r=r, focal=f, seed=j["seed"])
+        ref, _, _, _ = s.render(0, double=True)
+        img = b.image(ids[k]).astype(np.float64)
+        out.append({"job": k, "paths": job_paths(j), "triangles": s.triangles,
+                     "rel_mse": float(np.mean((img - ref) ** 2) / max(np.mean(ref ** 2), 1e-30))})
+    return out
 
 
 def bench_forms(args):
@@ -287,7 +371,15 @@ def bench_forms(args):
     t = time.time()
     b.run()
     wall = time.time() - t
-    rays = rays_of(b.stats()) - rays_of(s0)
+    st1 = b.stats()
+    rays = rays_of(st1) - rays_of(s0)
+    busy = st1["gpu_busy_ms"] / 1e3
+    # matched error: the smallest jobs' images against the FP64 oracle
+    picks = sorted(range(len(jobs)), key=lambda k: (tris[jobs[k]["scene"]], job_paths(jobs[k])))[:3]
+    try:
+        mse = rel_mse_against_fp64(b, scenes, jobs, ids, picks)
+    except Exception as e:  # the checker is optional on a box without the oracle
+        mse = "unavailable: %s" % e
     for i in ids:
         b.release(i)
     # the per-job loop on the same jobs: one job in flight at a time, with the
@@ -298,6 +390,7 @@ def bench_forms(args):
     _, pst = b.serve([(0.0, j) for j in jobs])
     plain_rate = rays_of(pst) / pst["wall_s"] / 1e6
     rate = rays / wall / 1e6
+    api = plain_api_jobs(scenes, jobs, len(jobs), args.plain_api_seconds)
     out["batched"] = {
         "workload": "%d jobs, one per terrain scene (%d-%d tris, log-uniform; %d total), resolutions "
                     "128^2-1024^2, 4-256 spp log-uniform, depth 4-10, RR from 3, cameras on the bounding sphere "
@@ -305,6 +398,15 @@ def bench_forms(args):
         "paths": sum(job_paths(j) for j in jobs), "mrays_per_s": rate, "wall_s": wall,
         "per_job_loop_mrays_per_s": plain_rate, "per_job_loop_wall_s": pst["wall_s"],
         "speedup_vs_per_job_loop": rate / plain_rate if plain_rate else None,
+        "gpu_busy_fraction": busy / wall if wall else None,
+        "per_job_loop_gpu_busy_fraction": pst["gpu_busy_s"] / pst["wall_s"] if pst["wall_s"] else None,
+        "scene_load_s": load_s,
+        "plain_api": dict(api, comparator="msc_create + msc_process + msc_image + msc_destroy per job, scene parse "
+                                          "and BVH build included, as src/main.cpp drives msc::Pathtracer"),
+        "e2e_incl_scene_load_mrays_per_s": rays / (wall + load_s) / 1e6,
+        "speedup_e2e_vs_plain_api": ((rays / (wall + load_s) / 1e6) / api["mrays_per_s"]
+                                     if api["mrays_per_s"] else None),
+        "rel_mse_vs_fp64_oracle": mse,
         "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")},
         "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["persistent"], t["digit_bits"],
                           t["ray_sort"], t["hit_sort"], round(t["mrays_per_s"], 1)] for t in tune_log]}
@@ -331,12 +433,96 @@ def bench_forms(args):
             row[label] = {"completed": sst["completed"], "mrays_per_s": sst["mrays_per_s"],
                           "p50_ms": 1e3 * sst["p50_s"], "p99_ms": 1e3 * sst["p99_s"],
                           "p999_ms": 1e3 * sst["p999_s"], "wall_s": sst["wall_s"],
-                          "peak_film_samples": sst["peak_film_samples"]}
+                          "peak_film_samples": sst["peak_film_samples"],
+                          "gpu_busy_fraction": sst["gpu_busy_s"] / sst["wall_s"] if sst["wall_s"] else None}
         row["speedup_vs_per_job_loop"] = (row["served"]["mrays_per_s"] / row["per_job_loop"]["mrays_per_s"]
                                           if row["per_job_loop"]["mrays_per_s"] else None)
         out["served"]["rates"].append(row)
         log("served at %g req/s: %s" % (rrate, json.dumps(row)))
     b.close()
+    return out
+
+
+def bench_c4(args):
+    """The served form at its stated configuration: 16 resident scenes (terrain
+    rules, triangle counts log-uniform in 10K-3M), Poisson requests at each rate
+    for a window of 60 s, each a seeded camera on its scene's bounding sphere
+    (fov 30-70) at 256^2-2048^2 pixels and 4-256 spp (log-uniform), depth
+    4-10.  Admission follows the film-memory budget; at these rates the offered
+    work exceeds what any single GPU renders, so admission closes at the end of
+    the window and the requests still waiting are counted, not served.  Each
+    rate runs the served form, then the one-job-at-a-time loop on the same
+    requests; a sample of requests also goes through the plain engine interface
+    (msc_create per request, since a request's camera and image size live in
+    its scene file)."""
+    import mscgpu
+    import numpy as np
+    scenes = scene_set(16, 1e4, 3e6, SEED + 400)
+    film_cap = 2_000_000_000  # 48 GB of film samples (31-bit sample index)
+    b = mscgpu.Batch(batch_exponent=23, film_samples=film_cap)
+    b.set_memory_budget(120_000_000_000)  # the stated 120 GB: fixed buffers, scenes and job images
+    bboxes, tris = [], []
+    t = time.time()
+    for y in scenes:
+        k = b.add_scene(y)
+        lo, hi, n = b.scene_info(k)
+        bboxes.append((lo, hi))
+        tris.append(n)
+    load_s = time.time() - t
+    rng = np.random.default_rng(SEED + 401)
+    # tune on a sample of the request mix (untimed)
+    b.autotune(windows=1)
+    sample = [random_job(rng, k % 16, bboxes[k % 16], [256, 512], 4, 16) for k in range(16)]
+    for _ in range(32):
+        ids = [b.submit(**j) for j in sample]
+        b.run()
+        for i in ids:
+            b.release(i)
+        if not b.tuning()["tuning"]:
+            break
+    tuned = b.tuning()
+    tuned_kw = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent",
+                                       "digit_bits")}
+    out = {"workload": "16 resident terrain scenes (%d-%d tris, %d total; loaded in %.1f s), Poisson requests, "
+                       "256^2-2048^2 (uniform over the four sizes), 4-256 spp log-uniform, depth 4-10, cameras on "
+                       "the bounding sphere (fov 30-70); film budget %d samples (%.0f GB); admission closes after "
+                       "the window" % (min(tris), max(tris), sum(tris), load_s, film_cap, film_cap * 24 / 1e9),
+           "tuned": tuned_kw, "rates": []}
+    used, fixed, _ = b.memory()
+    out["device_memory"] = {"budget_gb": 120.0, "fixed_and_scenes_gb": round(fixed / 1e9, 2)}
+    for spec in args.c4_rates.split(","):
+        rrate, dur = (float(x) for x in spec.split(":"))
+        arrivals = np.cumsum(rng.exponential(1.0 / rrate, size=int(rrate * dur * 2) + 16))
+        arrivals = arrivals[arrivals < dur]
+        reqs = []
+        for a in arrivals:
+            k = int(rng.integers(0, 16))
+            reqs.append((float(a), random_job(rng, k, bboxes[k], [256, 512, 1024, 2048], 4, 256)))
+        offered = sum(job_paths(j) for _, j in reqs)
+        row = {"rate_per_s": rrate, "window_s": dur, "requests": len(reqs), "offered_paths": offered}
+        for label, max_active in (("served", 0), ("per_job_loop", 1)):
+            b.set_max_active(max_active)
+            b.set_tuning(**tuned_kw)
+            _, sst = b.serve(reqs, window_s=dur)
+            row[label] = {"completed": sst["completed"], "not_admitted": sst["not_admitted"],
+                          "mrays_per_s": sst["mrays_per_s"], "p50_s": sst["p50_s"], "p99_s": sst["p99_s"],
+                          "p999_s": sst["p999_s"], "wall_s": sst["wall_s"],
+                          "peak_film_samples": sst["peak_film_samples"],
+                          "gpu_busy_fraction": sst["gpu_busy_s"] / sst["wall_s"] if sst["wall_s"] else None}
+            log("c4 %g req/s %s: %s" % (rrate, label, json.dumps(row[label])))
+        row["speedup_vs_per_job_loop"] = (row["served"]["mrays_per_s"] / row["per_job_loop"]["mrays_per_s"]
+                                          if row["per_job_loop"]["mrays_per_s"] else None)
+        out["rates"].append(row)
+    b.close()
+    # the plain engine interface on a sample of the same request mix
+    sample = [random_job(rng, int(rng.integers(0, 16)), None, [256, 512, 1024, 2048], 4, 256) for _ in range(64)]
+    for j in sample:
+        j["camera"] = sphere_camera(rng, bboxes[j["scene"]])
+    api = plain_api_jobs(scenes, sample, len(sample), args.plain_api_seconds)
+    out["plain_api"] = dict(api, comparator="msc_create + msc_process + msc_image + msc_destroy per request")
+    for row in out["rates"]:
+        row["speedup_vs_plain_api"] = (row["served"]["mrays_per_s"] / api["mrays_per_s"]
+                                       if api["mrays_per_s"] else None)
     return out
 
 
@@ -380,6 +566,20 @@ def bench_stress(args):
     return out
 
 
+def scene_for(args):
+    """The workload's scene file; --sample-base writes a copy with another sample base."""
+    y = make_scene(args.config, args.scale)
+    if args.sample_base > 0:
+        import re
+        text = open(y).read()
+        text = re.sub(r"sample base: \d+", "sample base: %d" % args.sample_base, text, count=1)
+        y2 = os.path.join(os.path.dirname(y), "scene_base%d.yaml" % args.sample_base)
+        with open(y2, "w") as f:
+            f.write(text)
+        y = y2
+    return y
+
+
 def run_reference(args):
     """The CPU arm: the reference algorithm (its CPU restatement in oracle/) on
     the host cores, on the same scene files.  It loads neither the CUDA
@@ -391,7 +591,7 @@ def run_reference(args):
     from oracle import build as oracle_build
     oracle_build.build()
     from oracle import oracle as O
-    yaml = make_scene(args.config, args.scale)
+    yaml = scene_for(args)
     t = time.time()
     s = O.Scene(yaml)
     log("oracle scene load + SAH build %.1f s" % (time.time() - t))
@@ -515,7 +715,7 @@ def run_gpu(args):
     g.build()
     import mscgpu
 
-    yaml = make_scene(args.config, args.scale)
+    yaml = scene_for(args)
     t = time.time()
     info, _, _ = mscgpu.scene_load_host(yaml)
     host_parse_s = time.time() - t
@@ -549,13 +749,14 @@ def run_gpu(args):
         pt.process_device()
     clocks.wait_first()
     t_timed = time.time()
-    dev_ms, wall, rays, launches = [], [], 0, 0
+    dev_ms, wall, rays, launches, busy_ms = [], [], 0, 0, 0.0
     for _ in range(args.steps):
         t = time.time()
         pt.process_device()
         wall.append(time.time() - t)
         st = pt.stats()
         dev_ms.append(st["process_ms"])
+        busy_ms += st["gpu_busy_ms"]
         rays += st["closest_queries"] + st["shadow_queries"]
         launches += st["kernel_launches"]
     # end to end through the C ABI with the image copied to host memory every step
@@ -606,6 +807,9 @@ def run_gpu(args):
            "gpu_launches": int(launches), "roofline": roofline, "clocks": clocks.summary(t_timed, t_timed_end),
            "wall_ms_per_step": 1e3 * sum(wall) / args.steps}
     out["batches_per_step"] = batches / args.steps
+    # device time of the work queued between the engine's host waits, over the
+    # timed passes' device time: the rest is the GPU waiting for the host
+    out["gpu_busy_fraction"] = busy_ms / total_ms if total_ms > 0 else None
     out["scene_input"] = scene_input
     extra = {}
     if not args.no_extra and args.config == 1:
@@ -631,7 +835,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1, help="scene config (1: large terrain scene, 0: box)")
-    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests only)")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (tests and profiling cases)")
+    ap.add_argument("--sample-base", type=int, default=0,
+                    help="override the scene's sample base (spp = base^2): small profiling cases at full spp")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and served measurements")
     ap.add_argument("--no-stress", action="store_true", help="skip the hit-sort stress scene")
@@ -644,10 +850,20 @@ def main():
                     help="Poisson request rates as rate:seconds (req/s, window), comma-separated")
     ap.add_argument("--forms-scenes", type=int, default=64)
     ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--c4", action="store_true",
+                    help="only the served form at its stated configuration (Poisson 50/200/400 req/s, 60 s "
+                         "windows); prints one JSON line of its own")
+    ap.add_argument("--c4-rates", default="50:60,200:60,400:60")
+    ap.add_argument("--plain-api-seconds", type=float, default=20.0,
+                    help="time limit of the plain-API comparator (jobs rendered one by one through msc_create)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
+    elif args.c4:
+        import __graft_entry__ as g
+        g.build()
+        print(json.dumps({"served_c4": bench_c4(args)}), flush=True)
     else:
         run_gpu(args)
 

@@ -87,6 +87,8 @@ typedef struct msc_stats {
   int width, height, spp, triangles, lights, iteration;
   double load_ms;             /* msc_create: host wall time of the YAML + OBJ parse */
   double bvh_ms;              /* msc_create: host wall time of the device BVH build and scene upload */
+  double gpu_busy_ms;         /* device time of the enqueued work between host waits (the rest of the
+                                 wall time the GPU sat idle waiting for the host) */
 } msc_stats;
 
 enum {
@@ -138,11 +140,23 @@ int msc_stage_sort_pairs_digits(uint32_t* keys, uint32_t* vals, int n, int bits,
  * hits by (geomID, primID) with tbb::parallel_sort (Pathtracer.cpp:335-339). */
 int msc_stage_sort_keys64(const uint64_t* keys, int n, uint32_t* perm);
 
+/* Test hook of the sort's bounded waits (no reference counterpart): sorts host
+ * arrays on the device with the look-back spin cap set to spin_cap; with
+ * withhold_first_tile != 0 the first tile never posts its digit counts, so every
+ * later tile's look-back gives up after spin_cap rounds.  Returns MSC_ERR_DEVICE
+ * (message in msc_last_error(NULL)) when a wait ran out; the output pairs are then
+ * not sorted.  Every wait is bounded, so the call always returns. */
+int msc_stage_sort_lookback_check(uint32_t* keys, uint32_t* vals, int n, int bits, int spin_cap,
+                                  int withhold_first_tile);
+
 /* Device-pointer form of msc_sort_pairs on the given CUDA stream (0 = default).
- * Scratch is allocated per call. */
+ * Scratch is allocated per call.  A look-back wait that runs out of its spin cap
+ * (which only a scheduling failure of the GPU could cause) is not reported by
+ * this form; msc_stage_sort_lookback_check shows the cap at work. */
 int msc_sort_pairs_device(uint32_t* keys, uint32_t* vals, int n, int bits, void* stream);
 
-/* Same sort as msc_sort_pairs_device, for callers that cannot allocate device memory
+/* Same sort as msc_sort_pairs_device (a look-back time-out is likewise not reported),
+ * for callers that cannot allocate device memory
  * while they run (a host that reserves its whole device budget up front, or a
  * latency-critical loop that cannot take cudaFree's device synchronisation).
  * No counterpart in the reference.  Allocates nothing: its scratch is a static
@@ -187,8 +201,21 @@ int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id);
 /* The resident scene's triangle box (lo.xyz, hi.xyz) and triangle count, for
    placing job cameras.  No reference counterpart. */
 int msc_batch_scene_info(msc_batch* b, int scene, float lo[3], float hi[3], int64_t* triangles);
-/* MSC_ERR_BUSY when the job's film does not fit in the free film capacity. */
+/* MSC_ERR_BUSY when the job's film does not fit in the free film capacity, or
+ * its image does not fit in the device-memory budget. */
 int msc_batch_submit(msc_batch* b, const msc_job_desc* desc, int* job_id);
+/* A device-memory budget in bytes for the batch object (0, the default: none).
+ * What counts: the fixed buffers taken at msc_batch_create (film pool, ray
+ * pools, batch buffers), every resident scene (BVH, triangles, tables, texels,
+ * as measured when it was built) and the images of admitted jobs.
+ * msc_batch_add_scene returns MSC_ERR_BUSY when a scene (estimated before it is
+ * built) would not fit; msc_batch_submit and the served form's admission treat
+ * a job whose image would not fit like a full film pool.  No reference
+ * counterpart. */
+int msc_batch_set_memory_budget(msc_batch* b, int64_t bytes);
+/* Bytes counted against the budget: all of them, the fixed buffers and
+ * scenes, and the admitted jobs' images (any pointer may be NULL). */
+int msc_batch_memory(msc_batch* b, int64_t* in_use, int64_t* fixed_bytes, int64_t* job_bytes);
 /* The batch loop's tuning point.  No choice changes a result. */
 typedef struct msc_tuning {
   int batch_exponent; /* rays per batch = 2^batch_exponent (at most the capacity given at create) */
@@ -251,6 +278,8 @@ typedef struct msc_serve_stats {
   double wall_s, p50_s, p99_s, p999_s, mrays_per_s;
   uint64_t closest_queries, shadow_queries;
   int64_t peak_film_samples;
+  double gpu_busy_s;          /* device time of the enqueued work between host waits */
+  int not_admitted;           /* requests still waiting when admission closed (msc_serve_window) */
 } msc_serve_stats;
 
 /* Runs the request stream in real time on the batch object's resident scenes:
@@ -258,6 +287,13 @@ typedef struct msc_serve_stats {
  * admitted jobs share the wavefront; a finished job's image is copied to the
  * host and its film released.  Images stay readable with msc_batch_job_image. */
 int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* results, msc_serve_stats* stats);
+
+/* msc_serve with admission open only for window_s seconds: requests that have
+ * not been admitted by then are not served (status MSC_ERR_BUSY, counted in
+ * stats->not_admitted); the admitted ones run to completion.  Measures an
+ * overloaded request stream over a fixed window. */
+int msc_serve_window(msc_batch* b, const msc_request* reqs, int n, double window_s, msc_request_result* results,
+                     msc_serve_stats* stats);
 
 /* ---- host-only scene input (no GPU needed) ---- */
 

@@ -70,6 +70,7 @@ SceneGPU::~SceneGPU() {
   if (d_tex_images) cudaFree(d_tex_images);
   if (d_tex_texels) cudaFree(d_tex_texels);
   if (d_tri_uv) cudaFree(d_tri_uv);
+  if (d_shade_rank) cudaFree(d_shade_rank);
 }
 
 namespace {
@@ -133,6 +134,8 @@ Core::~Core() {
   if (graph_) cudaGraphExecDestroy(graph_);
   if (drain_graph_) cudaGraphExecDestroy(drain_graph_);
   if (h_ctr_) cudaFreeHost(h_ctr_);
+  for (auto e : busy_ev_)
+    if (e) cudaEventDestroy(e);
   for (auto e : tune_ev_)
     if (e) cudaEventDestroy(e);
   for (int i = 0; i < kGraphBodies; ++i) {
@@ -169,6 +172,8 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   }
   CK(cudaEventCreate(&tune_ev_[0]));
   CK(cudaEventCreate(&tune_ev_[1]));
+  CK(cudaEventCreate(&busy_ev_[0]));
+  CK(cudaEventCreate(&busy_ev_[1]));
   CK(cudaMalloc(&d_scenes_, kMaxScenes * sizeof(SceneRec)));
   CK(cudaMallocHost(&h_scenes_, kMaxScenes * sizeof(SceneRec)));
   CK(cudaMalloc(&d_jobs_, (size_t)kMaxJobs * sizeof(JobRec)));
@@ -407,6 +412,29 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
     r.texel_res = d.texels.res;
     r.texels = sg->d_texels;
   }
+  if (d.ext.hit_key_bits == 64 && T < (1 << 23)) {
+    // The 64-bit hit key is shader id (12 bits) | face id (23 bits) | quantised uv.
+    // Its top 35 bits order a batch's hits by (shader, face); the rank of each
+    // triangle in that order gives the same grouping from a sort of
+    // ceil(log2(T + 1)) bits (three 8-bit digit passes for 8 M triangles)
+    // instead of two 32-bit sorts.  Hits on the same face keep their batch
+    // order (the uv bits only split such ties).  Counting sort by shader
+    // over the faces in original order:
+    std::vector<uint32_t> shader_of(T), start(4097, 0), rank(T);
+    for (int o = 0; o < T; ++o) {
+      const int g = tg[o];
+      shader_of[o] = (g >= 0 && g < (int)geoms.size()) ? (uint32_t)(geoms[g].shader & 0xfff) : 0u;
+      ++start[shader_of[o] + 1];
+    }
+    for (int s = 0; s < 4096; ++s) start[s + 1] += start[s];
+    for (int o = 0; o < T; ++o) rank[o] = start[shader_of[o]]++;
+    std::vector<uint32_t> leaf(T);
+    for (int k = 0; k < T; ++k) leaf[k] = rank[sg->h_tri_orig[k]] + 1u;
+    CK(cudaMalloc(&sg->d_shade_rank, (size_t)T * sizeof(uint32_t)));
+    CK(cudaMemcpy(sg->d_shade_rank, leaf.data(), (size_t)T * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    r.shade_rank = sg->d_shade_rank;
+    r.shade_rank_bits = 32 - __builtin_clz((uint32_t)T);  // keys lie in [0, T]
+  }
   if ((uint64_t)total_tris_ + (uint64_t)T + 1 >= (1ull << 32)) {
     err = "too many triangles across resident scenes";
     return MSC_ERR_ARG;
@@ -479,6 +507,11 @@ int Core::add_job(const JobSpec& spec, int* id) {
       return MSC_ERR_BUSY;
     }
   }
+  const int64_t image_bytes = (int64_t)3 * rec.width * rec.height * (int64_t)sizeof(float);
+  if (mem_budget > 0 && mem_fixed + mem_jobs + image_bytes > mem_budget) {
+    err = "the device-memory budget has no room for this job's image yet";
+    return MSC_ERR_BUSY;
+  }
   int slot = -1;
   if (!free_slots_.empty()) {
     slot = free_slots_.back();
@@ -505,6 +538,7 @@ int Core::add_job(const JobSpec& spec, int* id) {
   }
   CK(cudaMemsetAsync(js->d_pixels, 0, px * sizeof(float), stream_));
   max_slot_ = std::max(max_slot_, slot);
+  mem_jobs += image_bytes;
   rec.sample_base = (uint32_t)off;
   rec.pixels = js->d_pixels;
   js->rec = rec;
@@ -558,7 +592,10 @@ int Core::remove_job(int id) {
     err = "a job with rays in flight cannot be removed";
     return MSC_ERR_BUSY;
   }
-  if (j->d_pixels) cudaFreeAsync(j->d_pixels, stream_);
+  if (j->d_pixels) {
+    cudaFreeAsync(j->d_pixels, stream_);
+    mem_jobs -= (int64_t)3 * j->rec.width * j->rec.height * (int64_t)sizeof(float);
+  }
   j->d_pixels = nullptr;
   if (j->sample_len) free_samples(j->sample_off, j->sample_len);
   j->sample_len = 0;
@@ -606,7 +643,31 @@ void Core::harvest() {
   event_used_ = 0;
 }
 
+void Core::mark_busy() {
+  if (busy_open_ || !busy_ev_[0]) return;
+  if (cudaEventRecord(busy_ev_[0], stream_) == cudaSuccess) busy_open_ = true;
+}
+
+void Core::close_busy() {
+  if (busy_open_ && cudaEventRecord(busy_ev_[1], stream_) != cudaSuccess) busy_open_ = false;
+}
+
+cudaError_t Core::sync_stream() {
+  close_busy();
+  const cudaError_t e = cudaStreamSynchronize(stream_);
+  settle_busy();
+  return e;
+}
+
+void Core::settle_busy() {
+  if (!busy_open_) return;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, busy_ev_[0], busy_ev_[1]) == cudaSuccess) stats.busy_ms += ms;
+  busy_open_ = false;
+}
+
 int Core::finish_job(JobState& j) {
+  mark_busy();
   {
     StageClock t(this, MSC_STAGE_FILTER);
     t.done(launch_filter(j.rec, film_, stream_));
@@ -620,9 +681,12 @@ int Core::copy_image(int id) {
   JobState* j = job(id);
   if (!j || !j->d_pixels) return MSC_ERR_ARG;
   j->h_pixels.resize((size_t)3 * j->rec.width * j->rec.height);
+  mark_busy();
   CK(cudaMemcpyAsync(j->h_pixels.data(), j->d_pixels, j->h_pixels.size() * sizeof(float), cudaMemcpyDeviceToHost,
                      stream_));
+  close_busy();
   CK(cudaStreamSynchronize(stream_));
+  settle_busy();
   j->image_on_host = true;
   return MSC_OK;
 }
@@ -648,6 +712,7 @@ int Core::generate(bool* did) {
   const uint64_t want = std::min<uint64_t>((uint64_t)staging_cap_, room);
   if (want < std::min<uint64_t>((uint64_t)batch_size_, left_total)) return MSC_OK;
   uint64_t filled = 0;
+  mark_busy();
   StageClock t(this, MSC_STAGE_RAYGEN);
   int launches = 0;
   for (auto& jp : jobs_) {
@@ -743,7 +808,19 @@ int Core::enqueue_batch(int index, bool overlap) {
                                 persistent_trace ? trace_counter_ : nullptr));
   }
   const uint32_t* order = nullptr;
-  if (hit_sort && ns == 1 && s0.hit_key_bits == 64) {
+  if (hit_sort && ns == 1 && s0.hit_key_bits == 64 && s0.shade_rank) {
+    // 64-bit key scenes: the (shader, face) order from the rank table
+    StageClock t(this, MSC_STAGE_HITSORT);
+    int l = launch_hit_keys_rank(d_scenes_, hits_, B, hkeys_, st, nb);
+    const int ls = sort_pairs(hkeys_, nullptr, hkeys_sorted_, hperm_, B, s0.shade_rank_bits, ss_, st, errw, nb,
+                              sort_digits);
+    if (ls < 0) {
+      err = "internal: hit sort without distinct outputs";
+      return MSC_ERR_CUDA;
+    }
+    t.done(l + ls);
+    order = hperm_;
+  } else if (hit_sort && ns == 1 && s0.hit_key_bits == 64) {
     // 64-bit key: stable by the low word, then stable by the high word
     StageClock t(this, MSC_STAGE_HITSORT);
     int l = launch_hit_keys64(d_scenes_, hits_, B, hkeys_, hhi_, st, nb);
@@ -850,6 +927,7 @@ int Core::capture_graph(cudaGraphExec_t* exec, uint64_t* exec_key, int* exec_lau
 }
 
 int Core::run_batches(int k, bool drain) {
+  mark_busy();
   if (profiling || !use_graph) {
     for (int i = 0; i < k; ++i) {
       int rc = enqueue_batch(i, false);
@@ -883,7 +961,9 @@ int Core::step(bool* idle) {
   if (max_slot_ >= 0)
     CK(cudaMemcpyAsync(h_job_done_, d_job_done_, (size_t)(max_slot_ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                        st));
+  close_busy();
   CK(cudaStreamSynchronize(st));
+  settle_busy();
   if (profiling) harvest();
   stats.closest = h_ctr_->closest;
   stats.shadow = h_ctr_->shadow;

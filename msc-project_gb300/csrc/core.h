@@ -43,6 +43,7 @@ struct SceneGPU {
   int4* d_tex_images = nullptr;
   float4* d_tex_texels = nullptr;
   float* d_tri_uv = nullptr;
+  uint32_t* d_shade_rank = nullptr;  // 64-bit hit key scenes: (shader, face) rank + 1 per leaf-order triangle
   std::vector<int> h_tri_orig;  // leaf order -> global triangle index
   SceneRec rec;
   ~SceneGPU();
@@ -93,6 +94,7 @@ struct TuneSample {
 
 struct CoreStats {
   uint64_t closest = 0, shadow = 0, batches = 0, launches = 0, generations = 0, graph_replays = 0;
+  double busy_ms = 0;  // device time from the first enqueue after a host wait to the next host wait
   double stage_ms[12] = {0};
   uint64_t stage_launches[12] = {0};
 };
@@ -105,6 +107,9 @@ class Core {
   bool ray_sort = true, hit_sort = true;
   bool merge_bins = true;  // let a batch take rays of several bins when the fullest is short
   int max_active = 0;      // jobs admitted at once (0 = no limit); 1 gives the one-job-at-a-time loop
+  // Device-memory budget (0: none): the fixed buffers and the resident scenes
+  // (mem_fixed) plus the admitted jobs' images (mem_jobs) must stay within it.
+  int64_t mem_budget = 0, mem_fixed = 0, mem_jobs = 0;
   bool use_graph = true;   // replay the batch body from a captured CUDA graph (eager launches when profiling)
   int max_batches_per_step = 16;  // batch bodies enqueued between two host looks at the counters
   int trace_block = 128;          // traversal block size
@@ -152,6 +157,8 @@ class Core {
   int ray_key_bits_used() const;
   int batch_size() const { return batch_size_; }
   double now() const;
+  // Host wait for the core's stream that keeps the busy accounting right.
+  cudaError_t sync_stream();
   // Closest hit / occlusion of explicit rays against scene 0 (stage entry points).
   int trace_closest(const float* org, const float* dir, int n, float4* hits_host);
   int trace_occluded(const float* org, const float* dir, const float* tmax, int n, int* occluded);
@@ -185,6 +192,13 @@ class Core {
   std::vector<TuneSample> tune_cands_;
   int tune_next_ = 0;           // candidate of the next run
   cudaEvent_t tune_ev_[2] = {nullptr, nullptr};
+  // GPU busy accounting: an event at the first enqueue after each host wait
+  // and one before the next wait; the stretches between are the GPU's busy time
+  cudaEvent_t busy_ev_[2] = {nullptr, nullptr};
+  bool busy_open_ = false;
+  void mark_busy();
+  void close_busy();   // before a host wait on stream_
+  void settle_busy();  // after it
   void tune_begin_dim();
   void tune_sample_done();
   std::vector<std::unique_ptr<SceneGPU>> scenes_;

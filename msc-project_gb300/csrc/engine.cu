@@ -77,6 +77,7 @@ void fill_stats(const CoreStats& cs, double ms, msc_stats* out) {
   out->batches = cs.batches;
   out->kernel_launches = cs.launches;
   out->process_ms = ms;
+  out->gpu_busy_ms = cs.busy_ms;
   for (int s = 0; s < 12; ++s) {
     out->stage_ms[s] = cs.stage_ms[s];
     out->stage_launches[s] = cs.stage_launches[s];
@@ -238,7 +239,7 @@ int process_impl(msc_handle* h, int* iteration, bool copy_image) {
     return rc;
   }
   if (h->terminate.load() || !j->complete) {
-    cudaStreamSynchronize(c.stream());
+    c.sync_stream();
     return MSC_OK;  // Pathtracer.cpp:486-487: a terminated pass returns 0 and leaves the image alone
   }
   cudaEventRecord(h->ev_end, c.stream());
@@ -249,7 +250,7 @@ int process_impl(msc_handle* h, int* iteration, bool copy_image) {
       return MSC_ERR_CUDA;
     }
   }
-  if (cudaStreamSynchronize(c.stream()) != cudaSuccess) {
+  if (c.sync_stream() != cudaSuccess) {
     h->err = "msc_process: device error";
     return MSC_ERR_CUDA;
   }
@@ -681,6 +682,43 @@ int msc_stage_sort_pairs_digits(uint32_t* keys, uint32_t* vals, int n, int bits,
   return rc;
 }
 
+int msc_stage_sort_lookback_check(uint32_t* keys, uint32_t* vals, int n, int bits, int spin_cap,
+                                  int withhold_first_tile) {
+  if (n <= 0 || bits < 1 || bits > 32 || !keys || !vals || spin_cap < 1) return MSC_ERR_ARG;
+  uint32_t* d = nullptr;
+  char* scratch = nullptr;
+  int* d_err = nullptr;
+  const size_t sb = sort_scratch_bytes(n);
+  int rc = MSC_OK;
+  if (cudaMalloc(&d, (size_t)n * 16) != cudaSuccess || cudaMalloc(&scratch, sb) != cudaSuccess ||
+      cudaMalloc(&d_err, sizeof(int)) != cudaSuccess || cudaMemset(d_err, 0, sizeof(int)) != cudaSuccess)
+    rc = MSC_ERR_CUDA;
+  if (rc == MSC_OK && (cudaMemcpy(d, keys, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMemcpy(d + n, vals, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = MSC_ERR_CUDA;
+  int h_err = 0;
+  if (rc == MSC_OK) {
+    SortScratch ss;
+    sort_scratch_bind(&ss, scratch, n);
+    SortTestHook hook;
+    hook.spin_cap = spin_cap;
+    hook.withhold_first_tile = withhold_first_tile != 0;
+    sort_pairs(d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, n, bits, ss, 0, d_err, nullptr, 8, &hook);
+    if (cudaMemcpy(keys, d + 2 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(vals, d + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = MSC_ERR_CUDA;
+  }
+  if (d) cudaFree(d);
+  if (scratch) cudaFree(scratch);
+  if (d_err) cudaFree(d_err);
+  if (rc == MSC_OK && (h_err & kSortErrLookback)) {
+    set_global_error("sort: a look-back wait ran out of its spin cap (a predecessor tile never posted its counts)");
+    return MSC_ERR_DEVICE;
+  }
+  return rc;
+}
+
 int msc_stage_sort_keys64(const uint64_t* keys, int n, uint32_t* perm) {
   if (n < 0 || (n > 0 && (!keys || !perm))) return MSC_ERR_ARG;
   if (n == 0) return MSC_OK;
@@ -841,7 +879,11 @@ int msc_batch_create(int batch_exponent, int64_t film_samples, msc_batch** out) 
   b->batch_exponent = e;
   b->film_samples = film_samples;
   const int gen = (int)std::min<int64_t>(std::max<int64_t>(16ll << e, 1ll << 22), 1ll << 25);
+  size_t free0 = 0, free1 = 0, total = 0;
+  cudaMemGetInfo(&free0, &total);
   int rc = guarded(&b->err, [&] { return b->core.init(e, gen, (size_t)film_samples, true); });
+  if (rc == MSC_OK && cudaMemGetInfo(&free1, &total) == cudaSuccess && free0 > free1)
+    b->core.mem_fixed = (int64_t)(free0 - free1);  // film pool, ray pools, batch buffers
   if (rc != MSC_OK) {
     g_create_error = b->core.err.empty() ? b->err : b->core.err;
     delete b;
@@ -873,10 +915,38 @@ int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id) {
     b->err = err;
     return MSC_ERR_SCENE;
   }
+  if (b->core.mem_budget > 0) {
+    // a scene's device bytes, estimated before it is built: triangles, BVH
+    // nodes, index tables and texcoords (~160 B per triangle), face texels
+    const int64_t T = (int64_t)d.tri_geom.size();
+    const int64_t est = 160 * T + (int64_t)6 * d.texels.res * d.texels.res * T;
+    if (b->core.mem_fixed + b->core.mem_jobs + est > b->core.mem_budget) {
+      b->err = "the device-memory budget has no room for this scene";
+      return MSC_ERR_BUSY;
+    }
+  }
+  size_t free0 = 0, free1 = 0, total = 0;
+  cudaMemGetInfo(&free0, &total);
   int rc = guarded(&b->err, [&] { return b->core.add_scene(d, scene_id); });
   if (rc != MSC_OK && b->err.empty()) b->err = b->core.err;
   if (rc != MSC_OK) b->err = b->core.err;
+  if (rc == MSC_OK && cudaMemGetInfo(&free1, &total) == cudaSuccess && free0 > free1)
+    b->core.mem_fixed += (int64_t)(free0 - free1);  // the scene as built
   return rc;
+}
+
+int msc_batch_set_memory_budget(msc_batch* b, int64_t bytes) {
+  if (!b || bytes < 0) return MSC_ERR_ARG;
+  b->core.mem_budget = bytes;
+  return MSC_OK;
+}
+
+int msc_batch_memory(msc_batch* b, int64_t* in_use, int64_t* fixed_bytes, int64_t* job_bytes) {
+  if (!b) return MSC_ERR_ARG;
+  if (in_use) *in_use = b->core.mem_fixed + b->core.mem_jobs;
+  if (fixed_bytes) *fixed_bytes = b->core.mem_fixed;
+  if (job_bytes) *job_bytes = b->core.mem_jobs;
+  return MSC_OK;
 }
 
 int msc_batch_scene_info(msc_batch* b, int scene, float lo[3], float hi[3], int64_t* triangles) {
@@ -1050,6 +1120,11 @@ int msc_batch_set_max_active(msc_batch* b, int n) {
 // ------------------------------------------------------------------ served
 
 int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* results, msc_serve_stats* stats) {
+  return msc_serve_window(b, reqs, n, -1.0, results, stats);
+}
+
+int msc_serve_window(msc_batch* b, const msc_request* reqs, int n, double window_s, msc_request_result* results,
+                     msc_serve_stats* stats) {
   if (!b || n < 0 || (n > 0 && (!reqs || !results)) || !stats) return MSC_ERR_ARG;
   return guarded(&b->err, [&]() -> int {
     Core& c = b->core;
@@ -1068,8 +1143,20 @@ int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* 
       results[i].status = 1;  // pending
     }
     std::vector<int> live;  // request indices admitted and not finished
+    int not_admitted = 0;
     while (finished < n) {
       const double t = c.now() - t0;
+      if (window_s >= 0.0 && t >= window_s && next < order.size()) {
+        // admission has closed: what has not been admitted is not served
+        for (; next < order.size(); ++next) {
+          const int r = order[next];
+          results[r].status = MSC_ERR_BUSY;
+          results[r].done_s = t;
+          ++finished;
+          ++not_admitted;
+        }
+        if (finished >= n) break;
+      }
       // admit arrived requests in arrival order while their film fits
       while (next < order.size() && reqs[order[next]].arrival_s <= t) {
         const int r = order[next];
@@ -1123,7 +1210,7 @@ int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* 
         if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 0.002)));
       }
     }
-    cudaStreamSynchronize(c.stream());
+    c.sync_stream();
     const double makespan = c.now() - t0;
     std::vector<double> lat;
     for (int i = 0; i < n; ++i)
@@ -1144,6 +1231,8 @@ int msc_serve(msc_batch* b, const msc_request* reqs, int n, msc_request_result* 
     stats->shadow_queries = c.stats.shadow;
     stats->mrays_per_s = makespan > 0 ? (double)(c.stats.closest + c.stats.shadow) / makespan / 1e6 : 0.0;
     stats->peak_film_samples = (int64_t)peak_samples;
+    stats->gpu_busy_s = c.stats.busy_ms / 1e3;
+    stats->not_admitted = not_admitted;
     return MSC_OK;
   });
 }

@@ -15,7 +15,10 @@
 // it keeps the previous call's contents; every byte a sort reads is written by
 // the same sort first, so nothing needs clearing.  Calls whose work overlaps
 // on the GPU (two streams, or two host threads) race on the array and must be
-// serialised by the caller.
+// serialised by the caller.  A look-back wait of the sort that runs out of its
+// spin cap (possible only if the GPU failed to schedule a running tile's
+// predecessor) sets a word inside the static array that no call reads: such a
+// sort returns MSC_OK with unsorted output.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -78,6 +81,14 @@ extern "C" int msc_sort_pairs_device_noalloc(uint32_t* keys, uint32_t* vals, int
     return MSC_ERR_ARG;
   }
   if (n == 0) return MSC_OK;
+  // an error left by the caller's own earlier work is reported as it is and
+  // not cleared, so that the launch check below sees only this call's errors
+  cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    mscg::set_global_error(std::string("msc_sort_pairs_device_noalloc: an earlier CUDA error is pending: ") +
+                           cudaGetErrorString(pending));
+    return MSC_ERR_CUDA;
+  }
   void* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc != MSC_OK) return rc;

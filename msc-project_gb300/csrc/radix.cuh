@@ -146,6 +146,13 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_b
 // before any stream capture).
 void sort_init();
 
+// Test hook of the look-back's bounded wait: a smaller spin cap, and a first
+// tile that never posts its counts, so that every later tile's wait runs out.
+struct SortTestHook {
+  int spin_cap = 1 << 20;
+  int withhold_first_tile = 0;
+};
+
 // Stable LSD sort of (keys_in, vals_in) on bits [0, bits) into (keys_out, vals_out).
 // vals_in == nullptr means vals_in[i] = i.  Input buffers are left unchanged
 // unless they alias the outputs.  One histogram kernel for all passes, then
@@ -156,10 +163,10 @@ void sort_init();
 // (sizes the grids); this form needs outputs distinct from the inputs when
 // the pass count is odd, and returns -1 otherwise.
 // digit_bits: 4, 8 or 11 (an 11-bit sort needs scratch bound for 11 bits,
-// else it falls back to 8).
+// else it falls back to 8).  hook (tests only): see SortTestHook.
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
                int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr,
-               int digit_bits = 8);
+               int digit_bits = 8, const SortTestHook* hook = nullptr);
 
 constexpr int kSortErrLookback = 256;
 

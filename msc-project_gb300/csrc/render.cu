@@ -571,6 +571,16 @@ __global__ void __launch_bounds__(TB) k_hit_keys64(const SceneRec* __restrict__ 
   hi[i] = (uint32_t)(key >> 32);
 }
 
+// Rank keys of a 64-bit-key scene: a hit's place in (shader, face) order.
+__global__ void __launch_bounds__(TB) k_hit_keys_rank(const SceneRec* __restrict__ scenes,
+                                                      const float4* __restrict__ hits, int n_max,
+                                                      const int* __restrict__ n_dev, uint32_t* __restrict__ keys) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= dev_count(n_max, n_dev)) return;
+  const int k = __float_as_int(hits[i].w);
+  keys[i] = k >= 0 ? __ldg(&scenes[0].shade_rank[k]) : 0u;
+}
+
 __global__ void __launch_bounds__(TB) k_gather_u32(const uint32_t* __restrict__ src, const uint32_t* __restrict__ idx,
                                                    int n_max, const int* __restrict__ n_dev,
                                                    uint32_t* __restrict__ dst) {
@@ -1077,62 +1087,165 @@ __global__ void __launch_bounds__(128) k_occluded(BvhRef bvh, const float4* __re
 }
 
 // ------------------------------------------------------------------ filters
-// TentFilter::convolve (src/core/TentFilter.cpp:5-63): gather over the 3x3
-// neighbour pixels; samples are x-major, pixels row-major.
-// Tiled: a block takes kFilterRows pixels of one image column and walks the
-// 3x3 neighbourhood in the reference's order (mx, then my, then the samples);
-// for each (mx, my) the rows' samples are staged in shared memory kFilterChunk
-// at a time with coalesced loads, stored sample-major (padded) so that each
-// thread then reads its pixel's samples without bank conflicts.  Every pixel
-// sums exactly the terms, in exactly the order, of the reference's loop.
-constexpr int kFilterRows = 32;
-constexpr int kFilterChunk = 32;
+// TentFilter::convolve (src/core/TentFilter.cpp:5-63): each pixel's value is
+// the tent-weighted mean of the samples of its 3x3 neighbour pixels; samples
+// are x-major (x*H*spp + y*spp + i), pixels row-major.
+//
+// Source-centric tiles, so that every sample leaves HBM once: a block owns an
+// output tile of kFtX columns x kFtY rows and the (kFtX+2) x (kFtY+2) source
+// pixels around it, one thread per source pixel.  The sources' samples are
+// staged kFtChunk at a time by asynchronous copies (cp.async) into two shared
+// buffers, so the next chunk streams in while the current one is folded: each
+// thread folds every sample of its source pixel, in sample order, into nine
+// partial sums - one per target pixel of the 3x3 around it - with exactly the
+// reference's per-term weights m = max(0, 1-|x-cx|) * max(0, 1-|y-cy|) (the
+// colour terms c*m fused into the running sums).  The partials go through
+// shared memory and each output pixel adds its nine partials in the
+// reference's neighbour order (mx, then my).  The weights are the reference's;
+// the association differs (each neighbour's samples are summed from zero
+// before they join the pixel's running sum) and the colour products are not
+// rounded apart, a difference of a few float ulps per pixel.
+constexpr int kFtX = 8, kFtY = 30;                   // output tile
+constexpr int kFsX = kFtX + 2, kFsY = kFtY + 2;      // source pixels with their halo
+constexpr int kFsN = kFsX * kFsY;                    // 320 source pixels = block threads
+constexpr int kFtChunk = 4;                          // samples per source in one staging buffer
+constexpr int kFrgbPitch = kFsN + 1;                 // float4 rows: conflict-free stores and loads
+constexpr int kFposPitch = kFsN + 9;                 // float2 rows
+struct FilterStage {
+  float4 rgb[kFtChunk][kFrgbPitch];
+  float2 pos[kFtChunk][kFposPitch];
+};
+struct FilterSmemPart {
+  float4 part[9][kFrgbPitch];  // (r, g, b, weight) of source q for target slot (1+dx)*3 + (1+dy)
+};
+union FilterSmem {
+  FilterStage st[2];
+  FilterSmemPart pa;
+};
 
-__global__ void __launch_bounds__(kFilterRows) k_filter_tent(JobRec f, Film film) {
-  __shared__ float4 s_rgb[kFilterChunk][kFilterRows + 1];
-  __shared__ float2 s_pos[kFilterChunk][kFilterRows + 2];
-  const int x = blockIdx.y;
-  const int y0 = blockIdx.x * kFilterRows;
-  const int t = threadIdx.x;
-  const int y = y0 + t;
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// This thread's share of the staging: element j of a chunk is sample k of
+// source pixel src; gbase is that source's first sample (-1: outside the image).
+struct FilterCopies {  // the film pool indexes samples with 31 bits
+  int gbase[kFtChunk];
+  int dst[kFtChunk];  // src | k << 16
+};
+
+__device__ __forceinline__ FilterCopies filter_copies(const JobRec& f, int x0, int y0) {
+  FilterCopies fc;
+  const int W = f.width, H = f.height;
+#pragma unroll
+  for (int j = 0; j < kFtChunk; ++j) {
+    const int e = threadIdx.x + j * kFsN;
+    const int src = e / kFtChunk, k = e - src * kFtChunk;
+    const int sx = x0 - 1 + src / kFsY, sy = y0 - 1 + src % kFsY;
+    const bool ok = sx >= 0 && sx < W && sy >= 0 && sy < H;
+    fc.gbase[j] = ok ? (int)((int64_t)f.sample_base + ((int64_t)sx * H + sy) * f.spp + k) : -1;
+    fc.dst[j] = src | (k << 16);
+  }
+  return fc;
+}
+
+// Issues the copies of samples [s0, s0 + cs) of every source pixel of the tile.
+__device__ __forceinline__ void filter_stage(FilterStage& st, const FilterCopies& fc, const Film& film, int s0,
+                                             int cs) {
+#pragma unroll
+  for (int j = 0; j < kFtChunk; ++j) {
+    const int src = fc.dst[j] & 0xffff, k = fc.dst[j] >> 16;
+    if (k < cs && fc.gbase[j] >= 0) {
+      const size_t g = (size_t)fc.gbase[j] + (size_t)s0;
+      cp_async16(&st.rgb[k][src], &film.rgb[g]);
+      cp_async8(&st.pos[k][src], &film.pos[g]);
+    }
+  }
+  cp_async_commit();
+}
+
+__global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
+  extern __shared__ __align__(16) unsigned char filter_smem[];
+  FilterSmem& sm = *reinterpret_cast<FilterSmem*>(filter_smem);
   const int W = f.width, H = f.height, spp = f.spp;
-  const float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
-  float sr = 0.f, sg = 0.f, sb = 0.f, den = 0.f;
-  for (int mx = -1; mx < 2; ++mx) {
-    const int px = x + mx;
-    if (px < 0 || px >= W) continue;  // uniform over the block
-    for (int my = -1; my < 2; ++my) {
-      const bool use = y < H && y + my >= 0 && y + my < H;
-      for (int s0 = 0; s0 < spp; s0 += kFilterChunk) {
-        const int cs = min(kFilterChunk, spp - s0);
-        __syncthreads();  // the previous chunk has been read
-        for (int e = t; e < kFilterRows * kFilterChunk; e += kFilterRows) {
-          const int r = e / kFilterChunk, k = e - r * kFilterChunk;
-          const int py = y0 + r + my;
-          if (k < cs && py >= 0 && py < H) {
-            const size_t g = (size_t)f.sample_base + ((size_t)px * H + py) * spp + s0 + k;
-            s_rgb[k][r] = film.rgb[g];
-            s_pos[k][r] = film.pos[g];
-          }
+  const int x0 = blockIdx.y * kFtX, y0 = blockIdx.x * kFtY;
+  const int q = threadIdx.x;
+  const int qx = x0 - 1 + q / kFsY, qy = y0 - 1 + q % kFsY;  // this thread's source pixel
+  const bool qvalid = qx >= 0 && qx < W && qy >= 0 && qy < H;
+  const FilterCopies fc = filter_copies(f, x0, y0);
+  float4 acc[9];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) acc[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  // target pixel centres around the source (the reference's cx, cy of each target)
+  float cxs[3], cys[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    cxs[a] = (float)(qx + a - 1) + 0.5f;
+    cys[a] = (float)(qy + a - 1) + 0.5f;
+  }
+  const int chunks = (spp + kFtChunk - 1) / kFtChunk;
+  filter_stage(sm.st[0], fc, film, 0, min(kFtChunk, spp));
+  for (int c = 0; c < chunks; ++c) {
+    const int s0 = c * kFtChunk, cs = min(kFtChunk, spp - s0);
+    cp_async_wait<0>();  // this thread's copies of chunk c have landed
+    // chunk c is visible to all, and every thread is done with chunk c - 1,
+    // whose buffer the copies of chunk c + 1 now refill
+    __syncthreads();
+    if (c + 1 < chunks) filter_stage(sm.st[(c + 1) & 1], fc, film, s0 + kFtChunk, min(kFtChunk, spp - s0 - kFtChunk));
+    const FilterStage& st = sm.st[c & 1];
+    if (qvalid) {
+      for (int k = 0; k < cs; ++k) {
+        const float2 p = st.pos[k][q];
+        const float4 cc = st.rgb[k][q];
+        float wx[3], wy[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          wx[a] = fmaxf(0.f, 1.f - fabsf(p.x - cxs[a]));
+          wy[a] = fmaxf(0.f, 1.f - fabsf(p.y - cys[a]));
         }
-        __syncthreads();
-        if (use) {
-          for (int k = 0; k < cs; ++k) {
-            const float2 p = s_pos[k][t];
-            const float4 c = s_rgb[k][t];
-            const float dx = fmaxf(0.f, 1.f - fabsf(p.x - cx));
-            const float dy = fmaxf(0.f, 1.f - fabsf(p.y - cy));
-            const float m = dx * dy;
-            den = den + m;
-            sr += c.x * m;
-            sg += c.y * m;
-            sb += c.z * m;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            const float m = wx[a] * wy[b];
+            float4& r = acc[a * 3 + b];
+            r.w = r.w + m;
+            r.x = fmaf(cc.x, m, r.x);
+            r.y = fmaf(cc.y, m, r.y);
+            r.z = fmaf(cc.z, m, r.z);
           }
-        }
       }
     }
   }
-  if (y >= H) return;
+  __syncthreads();  // every thread is done with the staging buffers
+#pragma unroll
+  for (int t = 0; t < 9; ++t) sm.pa.part[t][q] = acc[t];
+  __syncthreads();
+  if (threadIdx.x >= kFtX * kFtY) return;
+  const int tx = threadIdx.x / kFtY, ty = threadIdx.x - tx * kFtY;
+  const int x = x0 + tx, y = y0 + ty;
+  if (x >= W || y >= H) return;
+  float sr = 0.f, sg = 0.f, sb = 0.f, den = 0.f;
+  for (int mx = -1; mx < 2; ++mx) {
+    if (x + mx < 0 || x + mx >= W) continue;
+    for (int my = -1; my < 2; ++my) {
+      if (y + my < 0 || y + my >= H) continue;
+      const int src = (tx + 1 + mx) * kFsY + (ty + 1 + my);
+      const float4 r = sm.pa.part[(1 - mx) * 3 + (1 - my)][src];
+      den = den + r.w;
+      sr = sr + r.x;
+      sg = sg + r.y;
+      sb = sb + r.z;
+    }
+  }
   float* out = f.pixels + 3 * ((size_t)y * W + x);
   out[0] += sr / den;
   out[1] += sg / den;
@@ -1291,6 +1404,13 @@ int launch_hit_keys64(const SceneRec* scenes, const float4* hits, int n, uint32_
   return 1;
 }
 
+int launch_hit_keys_rank(const SceneRec* scenes, const float4* hits, int n, uint32_t* keys, cudaStream_t s,
+                         const int* n_dev) {
+  if (n <= 0) return 0;
+  k_hit_keys_rank<<<grid_for(n), TB, 0, s>>>(scenes, hits, n, n_dev, keys);
+  return 1;
+}
+
 int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t* dst, cudaStream_t s,
                       const int* n_dev) {
   if (n <= 0) return 0;
@@ -1347,7 +1467,15 @@ int launch_occluded(const SceneRec& scene, const float4* o, const float4* d, int
 int launch_filter(const JobRec& job, Film film, cudaStream_t s) {
   const int n = job.width * job.height;
   if (job.filter == FILTER_BOX) k_filter_box<<<grid_for(n), TB, 0, s>>>(job, film);
-  else k_filter_tent<<<dim3((job.height + kFilterRows - 1) / kFilterRows, job.width), kFilterRows, 0, s>>>(job, film);
+  else {
+    static bool attr = false;  // the tile's shared memory exceeds the 48 KB default
+    if (!attr) {
+      cudaFuncSetAttribute(k_filter_tent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FilterSmem));
+      attr = true;
+    }
+    k_filter_tent<<<dim3((job.height + kFtY - 1) / kFtY, (job.width + kFtX - 1) / kFtX), kFsN, sizeof(FilterSmem),
+                    s>>>(job, film);
+  }
   return 1;
 }
 

@@ -70,6 +70,11 @@ struct SceneRec {        // one resident scene
   const float* tri_uv;   // 6 per original triangle: uv of v0, v1, v2
   float4 key_lo;         // ray sort key: the scene box's low corner
   float4 key_scale;      // and 64 / its extent per axis (0 for a flat axis)
+  // 64-bit hit key scenes: 1 + the rank of each triangle (BVH leaf order) in
+  // the order of the key's (shader id, face id) fields, so that a sort of
+  // shade_rank_bits bits groups hits as the key's top 35 bits do
+  const uint32_t* shade_rank;
+  int shade_rank_bits;
 };
 
 // Texture coordinate of a hit (PolygonObject::texture, src/core/PolygonObject.cpp:45-63).
@@ -215,6 +220,9 @@ int launch_hit_keys(const SceneRec* scenes, const float4* d, const int* slots, c
 // sphere-light hits 0) as low and high words.
 int launch_hit_keys64(const SceneRec* scenes, const float4* hits, int n, uint32_t* lo, uint32_t* hi,
                       cudaStream_t s, const int* n_dev = nullptr);
+// Hit keys from the (shader, face) rank table of a 64-bit-key scene (misses 0).
+int launch_hit_keys_rank(const SceneRec* scenes, const float4* hits, int n, uint32_t* keys, cudaStream_t s,
+                         const int* n_dev = nullptr);
 int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t* dst, cudaStream_t s,
                       const int* n_dev = nullptr);
 // Fills the scene's face texels from their seed (FP16 bits of k / 1024).

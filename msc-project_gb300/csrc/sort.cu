@@ -117,7 +117,8 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
                                                               const int* __restrict__ n_dev, int shift,
                                                               uint32_t mask, int pass,
                                                               const uint32_t* __restrict__ hist, uint32_t* status_cur,
-                                                              uint32_t* status_next, uint32_t* ctl, int* err) {
+                                                              uint32_t* status_next, uint32_t* ctl, int* err,
+                                                              int spin_cap, int withhold_first) {
   using S = SortShape<RB>;
   constexpr int RADIX = S::RADIX, DPT = S::DPT, ITEMS = S::ITEMS, TILE = S::TILE;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -165,7 +166,9 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
 #pragma unroll
     for (int k = 0; k < DPT; ++k) {
       cnt[k] = (uint32_t)sm.rank.tile_count[d0 + k];
-      st_volatile(&status_cur[tile * RADIX + d0 + k], (cnt[k] << 2) | (tile == 0 ? kFlagPrefix : kFlagAggregate));
+      // (withhold_first: a test of the spin cap - the first tile never posts)
+      if (!(withhold_first && tile == 0))
+        st_volatile(&status_cur[tile * RADIX + d0 + k], (cnt[k] << 2) | (tile == 0 ? kFlagPrefix : kFlagAggregate));
     }
 #pragma unroll
     for (int k = 0; k < DPT; ++k) {
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kSortBlock) k_onesweep_pass(const uint32_t* __
           if (done) break;
           t -= used;
           if (used < kLookbackWindow) {  // a predecessor has not posted yet; it is running, so this ends
-            if (++spins > kLookbackSpinCap) {
+            if (++spins > spin_cap) {
               atomicOr(err, kSortErrLookback);
               break;
             }
@@ -336,7 +339,7 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_b
 namespace {
 template <int RB>
 int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n, int bits,
-             SortScratch& s, cudaStream_t stream, int* err, const int* n_dev) {
+             SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, const SortTestHook* hook) {
   using S = SortShape<RB>;
   const int passes = (bits + RB - 1) / RB;
   if (n_dev && (passes == 0 || ((passes % 2) == 1 && (keys_in == keys_out || (vals_in && vals_in == vals_out)))))
@@ -366,7 +369,8 @@ int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_ou
     uint32_t* cur = (p & 1) ? status1 : status0;
     uint32_t* next = (p + 1 < passes) ? ((p & 1) ? status0 : status1) : nullptr;
     k_onesweep_pass<RB><<<tiles, kSortBlock, sizeof(PassSmem<RB>), stream>>>(
-        src_k, src_v, dst_k, dst_v, n, n_dev, shift, mask, p, s.hist, cur, next, s.ctl, errw);
+        src_k, src_v, dst_k, dst_v, n, n_dev, shift, mask, p, s.hist, cur, next, s.ctl, errw,
+        hook ? hook->spin_cap : kLookbackSpinCap, hook ? hook->withhold_first_tile : 0);
     ++launches;
     src_k = dst_k;
     src_v = dst_v;
@@ -385,13 +389,16 @@ void sort_init() {
 }
 
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
-               int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, int digit_bits) {
+               int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, int digit_bits,
+               const SortTestHook* hook) {
   if (n <= 0) return 0;
   sort_init();
   if (digit_bits > s.max_digit_bits) digit_bits = 8;  // scratch sized for narrower digits
-  if (digit_bits == 4) return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
-  if (digit_bits == 11) return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
-  return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev);
+  if (digit_bits == 4)
+    return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
+  if (digit_bits == 11)
+    return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
+  return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
 }
 
 }  // namespace mscg

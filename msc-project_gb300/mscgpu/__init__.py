@@ -33,7 +33,7 @@ class _Stats(C.Structure):
                 ("kernel_launches", C.c_uint64), ("process_ms", C.c_double), ("stage_ms", C.c_double * 12),
                 ("stage_launches", C.c_uint64 * 12), ("width", C.c_int), ("height", C.c_int), ("spp", C.c_int),
                 ("triangles", C.c_int), ("lights", C.c_int), ("iteration", C.c_int), ("load_ms", C.c_double),
-                ("bvh_ms", C.c_double)]
+                ("bvh_ms", C.c_double), ("gpu_busy_ms", C.c_double)]
 
 
 class _JobDesc(C.Structure):
@@ -55,7 +55,8 @@ class _RequestResult(C.Structure):
 class _ServeStats(C.Structure):
     _fields_ = [("completed", C.c_int), ("wall_s", C.c_double), ("p50_s", C.c_double), ("p99_s", C.c_double),
                 ("p999_s", C.c_double), ("mrays_per_s", C.c_double), ("closest_queries", C.c_uint64),
-                ("shadow_queries", C.c_uint64), ("peak_film_samples", C.c_int64)]
+                ("shadow_queries", C.c_uint64), ("peak_film_samples", C.c_int64), ("gpu_busy_s", C.c_double),
+                ("not_admitted", C.c_int)]
 
 
 _lib = None
@@ -99,6 +100,8 @@ def load_library():
         "msc_batch_last_error": (C.c_char_p, [P]),
         "msc_batch_add_scene": (I, [P, C.c_char_p, C.POINTER(I)]),
         "msc_batch_submit": (I, [P, C.POINTER(_JobDesc), C.POINTER(I)]),
+        "msc_batch_set_memory_budget": (I, [P, C.c_int64]),
+        "msc_batch_memory": (I, [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "msc_batch_run": (I, [P]),
         "msc_batch_job_image": (I, [P, I, C.POINTER(F), C.POINTER(I), C.POINTER(I)]),
         "msc_batch_release_job": (I, [P, I]),
@@ -108,6 +111,7 @@ def load_library():
         "msc_stage_sort_keys64": (I, [C.POINTER(C.c_uint64), I, U32]),
         "msc_write_image_file": (I, [C.c_char_p, I, I, F]),
         "msc_stage_sort_pairs_digits": (I, [U32, U32, I, I, I]),
+        "msc_stage_sort_lookback_check": (I, [U32, U32, I, I, I, I]),
         "msc_batch_autotune": (I, [P, I]),
         "msc_get_tuning": (I, [P, C.POINTER(_Tuning)]),
         "msc_set_tuning": (I, [P, C.POINTER(_Tuning)]),
@@ -116,6 +120,8 @@ def load_library():
         "msc_batch_tune_log": (I, [P, C.POINTER(_TuneSample), I, C.POINTER(I)]),
         "msc_batch_scene_info": (I, [P, I, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int64)]),
         "msc_serve": (I, [P, C.POINTER(_Request), I, C.POINTER(_RequestResult), C.POINTER(_ServeStats)]),
+        "msc_serve_window": (I, [P, C.POINTER(_Request), I, C.c_double, C.POINTER(_RequestResult),
+                                 C.POINTER(_ServeStats)]),
         "msc_obj_load": (I, [C.c_char_p, F, F, U32, C.POINTER(C.c_int64)]),
         "msc_scene_load_host": (I, [C.c_char_p, C.POINTER(C.c_int32), F, C.POINTER(C.c_int32)]),
     }
@@ -317,6 +323,17 @@ def sort_pairs_digits(keys, vals, bits=32, digit_bits=8):
     return k, v
 
 
+def sort_lookback_check(keys, vals, bits, spin_cap, withhold_first_tile):
+    """The sort with a given look-back spin cap (and optionally a first tile
+    that never posts): returns (status code, keys, vals); raises nothing."""
+    lib = load_library()
+    k = np.ascontiguousarray(keys, np.uint32).copy()
+    v = np.ascontiguousarray(vals, np.uint32).copy()
+    rc = lib.msc_stage_sort_lookback_check(_ptr(k, C.c_uint32), _ptr(v, C.c_uint32), k.shape[0], bits, spin_cap,
+                                           1 if withhold_first_tile else 0)
+    return rc, k, v
+
+
 def sort_keys64(keys):
     """Stable order of 64-bit keys as the 64-bit hit sort takes it."""
     lib = load_library()
@@ -432,6 +449,16 @@ class Batch:
         self._check(self._lib.msc_batch_scene_info(self._b, scene, lo, hi, C.byref(n)))
         return np.array(lo[:], np.float32), np.array(hi[:], np.float32), n.value
 
+    def set_memory_budget(self, nbytes):
+        """Device-memory budget (bytes, 0: none) for scenes, fixed buffers and job images."""
+        self._check(self._lib.msc_batch_set_memory_budget(self._b, int(nbytes)))
+
+    def memory(self):
+        """(in_use, fixed buffers + scenes, admitted job images) in bytes."""
+        a, f, j = C.c_int64(), C.c_int64(), C.c_int64()
+        self._check(self._lib.msc_batch_memory(self._b, C.byref(a), C.byref(f), C.byref(j)))
+        return a.value, f.value, j.value
+
     def submit(self, scene, **kw):
         """kw: width, height, spp, min_depth, max_depth, camera=(translation, rotation, focal), seed."""
         jid = C.c_int()
@@ -486,8 +513,9 @@ class Batch:
         d["stage_ms"] = {STAGES[i]: s.stage_ms[i] for i in range(len(STAGES))}
         return d
 
-    def serve(self, requests):
-        """requests: list of (arrival_s, job kwargs incl. scene).  Returns (results, stats)."""
+    def serve(self, requests, window_s=None):
+        """requests: list of (arrival_s, job kwargs incl. scene).  Returns (results, stats).
+        window_s: admission closes after that many seconds (msc_serve_window)."""
         n = len(requests)
         reqs = (_Request * max(n, 1))()
         for i, (t, kw) in enumerate(requests):
@@ -496,7 +524,10 @@ class Batch:
             reqs[i].job = _job_desc(kw.pop("scene"), **kw)
         res = (_RequestResult * max(n, 1))()
         st = _ServeStats()
-        self._check(self._lib.msc_serve(self._b, reqs, n, res, C.byref(st)))
+        if window_s is None:
+            self._check(self._lib.msc_serve(self._b, reqs, n, res, C.byref(st)))
+        else:
+            self._check(self._lib.msc_serve_window(self._b, reqs, n, float(window_s), res, C.byref(st)))
         results = [{k: getattr(res[i], k) for k, _ in _RequestResult._fields_} for i in range(n)]
         stats = {k: getattr(st, k) for k, _ in _ServeStats._fields_}
         return results, stats

@@ -18,7 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_LIB = os.path.join(REF_OUT, "libreftinyobj.so")
-REFERENCE = "/root/reference"
+# where the reference's sources lie (read only); MSC_REFERENCE_DIR overrides it
+REFERENCE = os.environ.get("MSC_REFERENCE_DIR", "/root/reference")
 
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-pthread"]
 

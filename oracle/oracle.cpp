@@ -1595,6 +1595,71 @@ void oracle_stable_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits) {
   memcpy(vals, v2.data(), (size_t)n * 4);
 }
 
+// The reference's ray order within a batch, RaySort::operator() of
+// src/core/RaySort.cpp:7-118 after RayBoundingbox (src/core/RayBoundingbox.cpp:5-50):
+// a range of more than 4096 rays is sorted by origin along the widest axis of
+// its box and halved at the middle; a half of more than 4096 rays keeps the box
+// cut at the median origin, a smaller half takes the box of its directions; a
+// range of 65..4096 rays is sorted by direction along the widest axis of its
+// (direction) box and halved, the halves keeping the parent's box except for
+// the first half's bound, as the reference sets it (its second half keeps the
+// parent's box unchanged).  Ranges of 64 rays or fewer stay as they are.  The
+// reference's tbb::parallel_sort is not stable; std::stable_sort here fixes
+// the order among equal coordinates.  Coherence comparisons only.
+namespace orc {
+struct Box3 { float lo[3], hi[3]; };
+int widest(const Box3& b) {
+  int t = (b.hi[0] - b.lo[0]) < (b.hi[1] - b.lo[1]) ? 1 : 0;
+  return (t < (b.hi[2] - b.lo[2])) ? 2 : t;  // the reference compares the index with the extent
+}
+void median_split(const float* org, const float* dir, uint32_t* ix, size_t b, size_t e, Box3 lim) {
+  const size_t size = e - b;
+  if (size > 4096) {
+    const int axis = widest(lim);
+    std::stable_sort(ix + b, ix + e, [&](uint32_t x, uint32_t y) { return org[3 * x + axis] < org[3 * y + axis]; });
+    const size_t mid = b + size / 2;
+    Box3 l, r;
+    auto dir_box = [&](size_t s0, size_t s1, Box3* o) {
+      for (int a = 0; a < 3; ++a) o->lo[a] = o->hi[a] = dir[3 * ix[s0] + a];
+      for (size_t k = s0; k < s1; ++k)
+        for (int a = 0; a < 3; ++a) {
+          const float v = dir[3 * ix[k] + a];
+          if (v < o->lo[a]) o->lo[a] = v;
+          if (v > o->hi[a]) o->hi[a] = v;
+        }
+    };
+    if (mid - b > 4096) { l = lim; l.hi[axis] = org[3 * ix[mid - 1] + axis]; }
+    else dir_box(b, mid, &l);
+    if (e - mid > 4096) { r = lim; r.lo[axis] = org[3 * ix[mid] + axis]; }
+    else dir_box(mid, e, &r);
+    median_split(org, dir, ix, b, mid, l);
+    median_split(org, dir, ix, mid, e, r);
+  } else if (size > 64) {
+    const int axis = widest(lim);
+    std::stable_sort(ix + b, ix + e, [&](uint32_t x, uint32_t y) { return dir[3 * x + axis] < dir[3 * y + axis]; });
+    const size_t mid = b + size / 2;
+    Box3 l = lim, r = lim;
+    l.hi[axis] = dir[3 * ix[mid - 1] + axis];
+    l.lo[axis] = dir[3 * ix[mid] + axis];
+    median_split(org, dir, ix, b, mid, l);
+    median_split(org, dir, ix, mid, e, r);
+  }
+}
+}  // namespace orc
+
+void oracle_median_split_order(const float* org, const float* dir, int n, uint32_t* order) {
+  for (int i = 0; i < n; ++i) order[i] = (uint32_t)i;
+  if (n <= 0) return;
+  orc::Box3 lim;  // RayBoundingbox: the batch's origin box
+  for (int a = 0; a < 3; ++a) lim.lo[a] = lim.hi[a] = org[a];
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      lim.lo[a] = std::min(lim.lo[a], org[3 * i + a]);
+      lim.hi[a] = std::max(lim.hi[a], org[3 * i + a]);
+    }
+  orc::median_split(org, dir, order, 0, (size_t)n, lim);
+}
+
 // 26 / 98 bins (extension, no reference counterpart): the surface cells of
 // an m^3 cube over [-1,1]^3 (m = 3 or 5), the direction scaled so its largest
 // component has magnitude 1; cells in x-major order, interior cells skipped.

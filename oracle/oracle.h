@@ -66,6 +66,9 @@ int oracle_occluded_f32(const oracle_scene* s, const float* org, const float* di
 void oracle_cardinal(const float* dirs, int n, int32_t* bins);
 void oracle_ray_keys(const float* org, const float* dir, int n, uint32_t* keys);
 void oracle_stable_sort_pairs(uint32_t* keys, uint32_t* vals, int n, int bits);
+/* The reference's median-split ray order of a batch (RaySort.cpp:7-118): order[i]
+ * = index of the i-th ray; for coherence comparisons with the project's key. */
+void oracle_median_split_order(const float* org, const float* dir, int n, uint32_t* order);
 void oracle_bin_partition(const float* rays, int n, int cap, float* out, int32_t* counts);
 void oracle_ray_bins(const float* dirs, int n, int nbins, int32_t* bins);
 // Periodic bilinear lookups of a PFM / PPM image at (s[i], t[i]); -1 if unreadable.

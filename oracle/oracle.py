@@ -38,6 +38,7 @@ def lib():
         L.oracle_cardinal.argtypes = [F, I, I32]
         L.oracle_ray_keys.argtypes = [F, F, I, U32]
         L.oracle_stable_sort_pairs.argtypes = [U32, U32, I, I]
+        L.oracle_median_split_order.argtypes = [F, F, I, U32]
         L.oracle_bin_partition.argtypes = [F, I, I, F, I32]
         L.oracle_ray_bins.argtypes = [F, I, I, I32]
         L.oracle_image_lookup.argtypes = [C.c_char_p, I, F, F, F]
@@ -154,6 +155,15 @@ def stable_sort_pairs(keys, vals, bits=32):
     v = np.ascontiguousarray(vals, np.uint32).copy()
     lib().oracle_stable_sort_pairs(_p(k, C.c_uint32), _p(v, C.c_uint32), k.shape[0], bits)
     return k, v
+
+
+def median_split_order(org, dirs):
+    """The reference's ray order (RaySort.cpp:7-118): a permutation of the rays."""
+    org = np.ascontiguousarray(org, np.float32)
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(org.shape[0], np.uint32)
+    lib().oracle_median_split_order(_p(org, C.c_float), _p(dirs, C.c_float), org.shape[0], _p(out, C.c_uint32))
+    return out
 
 
 def image_lookup(path, s, t):

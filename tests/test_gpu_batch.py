@@ -208,3 +208,32 @@ def test_autotuner_books_samples_and_keeps_results(built, scenes):
     with pytest.raises(mscgpu.MscError):
         b.set_tuning(batch_exponent=20)  # above the capacity given at create
     b.close()
+
+
+def test_memory_budget_counts_scenes_and_job_images(built, scenes):
+    """Admission by device memory: fixed buffers and resident scenes count, a job
+    whose image would not fit waits (MSC_ERR_BUSY), a scene that would not fit
+    is refused, and a released job's image returns its bytes."""
+    mscgpu, _ = built
+    b = mscgpu.Batch(batch_exponent=12, film_samples=1 << 22)
+    used0, fixed0, jobs0 = b.memory()
+    assert fixed0 > 0 and jobs0 == 0 and used0 == fixed0
+    b.add_scene(scenes[0])
+    used1, fixed1, _ = b.memory()
+    assert fixed1 > fixed0  # the scene's BVH, triangles and tables
+    small = 3 * 4 * 16 * 16
+    b.set_memory_budget(used1 + small + 1024)
+    with pytest.raises(mscgpu.MscError) as e:
+        b.submit(0, width=64, height=64, spp=1)  # a 49 KB image
+    assert e.value.code == -5 and "budget" in str(e.value)
+    jid = b.submit(0, width=16, height=16, spp=1)
+    assert b.memory()[2] == small
+    with pytest.raises(mscgpu.MscError) as e:
+        b.add_scene(scenes[2])
+    assert e.value.code == -5
+    b.run()
+    b.release(jid)
+    assert b.memory()[2] == 0
+    b.set_memory_budget(0)
+    b.add_scene(scenes[2])
+    b.close()

@@ -246,3 +246,21 @@ def test_radix_digit_widths_are_the_stable_order(built, digit_bits, n, bits):
     wk, wv = oracle.stable_sort_pairs(keys, vals, bits)
     assert np.array_equal(gv, wv)
     assert np.array_equal(gk, wk)
+
+
+def test_lookback_wait_that_runs_out_is_reported(built):
+    """The sort's look-back spins are bounded: with a first tile that never posts
+    its counts, every later tile gives up after the cap, the call returns, and the
+    host reads MSC_ERR_DEVICE; the same sort with nothing withheld is the stable order."""
+    mscgpu, _ = built
+    rng = np.random.default_rng(9)
+    n = 50000
+    keys = rng.integers(0, 1 << 16, size=n, dtype=np.uint32)
+    vals = np.arange(n, dtype=np.uint32)
+    rc, _, _ = mscgpu.sort_lookback_check(keys, vals, 16, 512, True)
+    assert rc == -4  # MSC_ERR_DEVICE
+    assert b"look-back" in mscgpu.load_library().msc_last_error(None)
+    rc, k, v = mscgpu.sort_lookback_check(keys, vals, 16, 512, False)
+    assert rc == 0
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(v, order.astype(np.uint32)) and np.array_equal(k, keys[order])

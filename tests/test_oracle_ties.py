@@ -73,8 +73,10 @@ def test_oracle_settles_exact_ties_by_the_smaller_triangle_index(built, tmp_path
     want, near = _brute_force(tv, org, d)
     sure = ~near
     assert sure.mean() > 0.99
-    # the brute force's float32 rounding differs from the oracle's fused
-    # arithmetic only at edges and grazing hits
+    # the oracle evaluates its dot and cross products with explicit fmaf (the
+    # device's arithmetic order), numpy with separately rounded float32
+    # products; the two disagree only where a ray meets a triangle edge or
+    # grazes a face
     assert (got[sure] == want[sure]).mean() > 0.998
     # the second copies never win: the box faces listed twice (the later half
     # of each box object) and the icosphere placed twice (the later object)

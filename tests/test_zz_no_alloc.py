@@ -38,6 +38,11 @@ def test_noalloc_sort_matches_allocating_sort_twice(built):
         assert rc_a == 0 and rc_b == 0
         assert np.array_equal(ka, kb)
         assert np.array_equal(va, vb)
+        # and directly against a stable CPU sort of the same pairs on the low `bits` bits
+        masked = keys & np.uint32((1 << bits) - 1) if bits < 32 else keys
+        order = np.argsort(masked, kind="stable")
+        assert np.array_equal(va, vals[order])
+        assert np.array_equal(ka, keys[order])
 
 
 def test_noalloc_sort_rejects_more_than_its_maximum(built):
