@@ -384,7 +384,7 @@ def bench_forms(args):
         b.release(i)
     # the per-job loop on the same jobs: one job in flight at a time, with the
     # same tuned settings, so the difference is only the merging of jobs
-    tuned_kw = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")}
+    tuned_kw = {k: tuned[k] for k in TUNE_KEYS}
     b.set_tuning(**tuned_kw)
     b.set_max_active(1)
     _, pst = b.serve([(0.0, j) for j in jobs])
@@ -407,9 +407,12 @@ def bench_forms(args):
         "speedup_e2e_vs_plain_api": ((rays / (wall + load_s) / 1e6) / api["mrays_per_s"]
                                      if api["mrays_per_s"] else None),
         "rel_mse_vs_fp64_oracle": mse,
-        "tuned": {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent", "digit_bits")},
+        "tuned": {k: tuned[k] for k in TUNE_KEYS},
+        "tune_samples_fields": "batch_exponent, bins, trace_block, persistent, digit_bits, ray_sort, hit_sort, "
+                               "ray_key_bits, Mrays/s",
         "tune_samples": [[t["batch_exponent"], t["bins"], t["trace_block"], t["persistent"], t["digit_bits"],
-                          t["ray_sort"], t["hit_sort"], round(t["mrays_per_s"], 1)] for t in tune_log]}
+                          t["ray_sort"], t["hit_sort"], t["ray_key_bits"], round(t["mrays_per_s"], 1)]
+                         for t in tune_log]}
     # served: Poisson arrivals on the first 16 resident scenes, at each rate
     nres = min(16, len(scenes))
     out["served"] = {"workload": "Poisson arrivals on %d resident scenes, 128^2-512^2, 4-64 spp log-uniform, "
@@ -481,8 +484,7 @@ def bench_c4(args):
         if not b.tuning()["tuning"]:
             break
     tuned = b.tuning()
-    tuned_kw = {k: tuned[k] for k in ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "persistent",
-                                       "digit_bits")}
+    tuned_kw = {k: tuned[k] for k in TUNE_KEYS}
     out = {"workload": "16 resident terrain scenes (%d-%d tris, %d total; loaded in %.1f s), Poisson requests, "
                        "256^2-2048^2 (uniform over the four sizes), 4-256 spp log-uniform, depth 4-10, cameras on "
                        "the bounding sphere (fov 30-70); film budget %d samples (%.0f GB); admission closes after "

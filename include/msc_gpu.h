@@ -233,6 +233,7 @@ typedef struct msc_tuning {
 typedef struct msc_tune_sample {
   int batch_exponent, trace_block, ray_sort, hit_sort, bins, persistent, digit_bits;
   double mrays_per_s; /* device-timed rays per second over the candidate's windows */
+  int ray_key_bits;   /* 0: the default width */
 } msc_tune_sample;
 /* Starts the online autotuner: each following msc_batch_run (each pass of
    the plain engine) renders with the next candidate choice (direction bins,

@@ -1106,6 +1106,17 @@ void Core::tune_begin_dim() {
         c.hit_sort = on;
         add(c);
       }
+    } else if (tune_dim_ == 6) {
+      // ray key width: the default and one more byte of the interleaved
+      // origin/direction key (finer order, one more sort pass)
+      if (base.ray_sort) {
+        const int def = scenes_.size() > 1 ? kRayKeyBitsScenes : kRayKeyBits;
+        for (int kb : {def, def + 8}) {
+          TuneChoice c = base;
+          c.ray_key_bits = kb;
+          add(c);
+        }
+      }
     } else {
       tune_active_ = false;
       return;

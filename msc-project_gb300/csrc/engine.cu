@@ -1100,6 +1100,7 @@ int msc_batch_tune_log(msc_batch* b, msc_tune_sample* out, int cap, int* n) {
     out[i].bins = log[i].choice.bins;
     out[i].persistent = log[i].choice.persistent ? 1 : 0;
     out[i].digit_bits = log[i].choice.digit_bits;
+    out[i].ray_key_bits = log[i].choice.ray_key_bits;
     out[i].mrays_per_s = log[i].ms > 0 ? log[i].rays / log[i].ms / 1e3 : 0.0;
   }
   return MSC_OK;

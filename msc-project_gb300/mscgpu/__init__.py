@@ -389,7 +389,8 @@ class _Tuning(C.Structure):
 
 class _TuneSample(C.Structure):
     _fields_ = [("batch_exponent", C.c_int), ("trace_block", C.c_int), ("ray_sort", C.c_int), ("hit_sort", C.c_int),
-                ("bins", C.c_int), ("persistent", C.c_int), ("digit_bits", C.c_int), ("mrays_per_s", C.c_double)]
+                ("bins", C.c_int), ("persistent", C.c_int), ("digit_bits", C.c_int), ("mrays_per_s", C.c_double),
+                ("ray_key_bits", C.c_int)]
 
 
 def _job_desc(scene, width=0, height=0, spp=0, min_depth=-1, max_depth=-1, camera=None, seed=0):
