@@ -299,8 +299,11 @@ def plain_api_jobs(scenes, jobs, max_jobs, limit_s):
 
 def rel_mse_against_fp64(b, scenes, jobs, ids, picks):
     """Relative MSE of batched job images against the FP64 oracle rendering the
-    same jobs (same cameras, sample counts and per-path random sequences)."""
+    same jobs (same cameras, sample counts and per-path random sequences), and
+    the same figure for the plain engine rendering each job from its own scene
+    file: matched error means the two forms' images are the same."""
     import numpy as np
+    import mscgpu
     from oracle import oracle as O
     out = []
     for k in picks:
@@ -310,9 +313,17 @@ def rel_mse_against_fp64(b, scenes, jobs, ids, picks):
         s.set_job(width=j["width"], height=j["height"], spp=j["spp"], min_depth=j["min_depth"],
                   max_depth=j["max_depth"], cam_t=t, cam_r=r, focal=f, seed=j["seed"])
         ref, _, _, _ = s.render(0, double=True)
-        img = b.image(ids[k]).astype(np.float64)
+        img = b.image(ids[k]).astype(np.float32)
+        d = os.path.join(tempfile.gettempdir(), "msc_bench_jobs", "mse%d" % k)
+        os.makedirs(d, exist_ok=True)
+        with mscgpu.Pathtracer(job_yaml(scenes[j["scene"]], j, os.path.join(d, "scene.yaml"))) as pt:
+            pt.process()
+            plain = pt.image()
+        den = max(float(np.mean(ref ** 2)), 1e-30)
         out.append({"job": k, "paths": job_paths(j), "triangles": s.triangles,
-                     "rel_mse": float(np.mean((img - ref) ** 2) / max(np.mean(ref ** 2), 1e-30))})
+                    "rel_mse": float(np.mean((img.astype(np.float64) - ref) ** 2) / den),
+                    "plain_rel_mse": float(np.mean((plain.astype(np.float64) - ref) ** 2) / den),
+                    "plain_image_bit_equal": bool(np.array_equal(img.view(np.uint32), plain.view(np.uint32)))})
     return out
 
 

@@ -439,6 +439,23 @@ int Core::add_scene(const SceneDesc& d_in, int* id) {
     err = "too many triangles across resident scenes";
     return MSC_ERR_ARG;
   }
+  {  // what the scene holds on the device, for the batch's memory budget
+    int64_t b = (int64_t)T * (3 * sizeof(float4) + sizeof(int)) + 8 * sizeof(float);  // triangles, index, box
+    b += sg->bvh.wnodes ? (int64_t)sg->bvh.num_wnodes * 5 * sizeof(uint4)
+                        : (int64_t)std::max(T - 1, 0) * 4 * sizeof(float4);
+    b += (int64_t)std::max<size_t>(1, d.shaders.size()) * sizeof(ShaderRec) +
+         (int64_t)std::max<size_t>(1, geoms.size()) * sizeof(GeomRec) +
+         (int64_t)std::max<size_t>(1, d.lights.size()) * sizeof(LightRec);
+    b += (int64_t)d.sphere_lights.size() * (sizeof(float4) + sizeof(int));
+    if (d.texels.res > 0) b += (int64_t)T * d.texels.res * d.texels.res * 3 * sizeof(unsigned short);
+    if (sg->d_tri_uv) {
+      b += (int64_t)6 * T * sizeof(float) + (int64_t)d.tex_nodes.size() * sizeof(TexNode) +
+           (int64_t)tex_ops.size() * sizeof(int2);
+      for (const auto& im : d.images) b += (int64_t)im.width * im.height * sizeof(float4) + sizeof(int4);
+    }
+    if (sg->d_shade_rank) b += (int64_t)T * sizeof(uint32_t);
+    sg->bytes = b;
+  }
   total_tris_ += (uint32_t)T;
   hit_bits_ = 32 - __builtin_clz(total_tris_);  // keys lie in [0, total_tris_]
   const int sid = (int)scenes_.size();

@@ -45,6 +45,7 @@ struct SceneGPU {
   float* d_tri_uv = nullptr;
   uint32_t* d_shade_rank = nullptr;  // 64-bit hit key scenes: (shader, face) rank + 1 per leaf-order triangle
   std::vector<int> h_tri_orig;  // leaf order -> global triangle index
+  int64_t bytes = 0;            // device bytes the resident scene holds
   SceneRec rec;
   ~SceneGPU();
 };
@@ -154,6 +155,7 @@ class Core {
   size_t sample_capacity() const { return sample_cap_; }
   Film film() const { return film_; }
   int batch_cap() const { return batch_cap_; }
+  int64_t scene_bytes(int id) const { return id >= 0 && id < (int)scenes_.size() ? scenes_[id]->bytes : 0; }
   int ray_key_bits_used() const;
   int batch_size() const { return batch_size_; }
   double now() const;

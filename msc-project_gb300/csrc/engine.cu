@@ -925,13 +925,10 @@ int msc_batch_add_scene(msc_batch* b, const char* yaml_path, int* scene_id) {
       return MSC_ERR_BUSY;
     }
   }
-  size_t free0 = 0, free1 = 0, total = 0;
-  cudaMemGetInfo(&free0, &total);
   int rc = guarded(&b->err, [&] { return b->core.add_scene(d, scene_id); });
   if (rc != MSC_OK && b->err.empty()) b->err = b->core.err;
   if (rc != MSC_OK) b->err = b->core.err;
-  if (rc == MSC_OK && cudaMemGetInfo(&free1, &total) == cudaSuccess && free0 > free1)
-    b->core.mem_fixed += (int64_t)(free0 - free1);  // the scene as built
+  if (rc == MSC_OK) b->core.mem_fixed += b->core.scene_bytes(*scene_id);  // the scene as built
   return rc;
 }
 
