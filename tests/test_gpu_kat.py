@@ -34,6 +34,15 @@ def test_direct_lighting_matches_closed_form(built, tmp_path, light, rr, mis):
     assert (se < 1e-3).all(), se
 
 
+@pytest.mark.parametrize("rr,mis", [(False, "balance"), (True, "balance"), (False, "power")])
+def test_phong_direct_lighting_matches_quadrature(built, tmp_path, rr, mis):
+    mscgpu, _ = built
+    sc = K.phong_over_plane(str(tmp_path), width=128, height=128, base=4, rr=rr, mis=mis)
+    rgb, xy = _render(mscgpu, sc.path)
+    rel, se = K.check_unbiased(rgb, sc.expected(xy), what="GPU phong %s rr=%s" % (mis, rr))
+    assert (se < 4e-3).all(), se
+
+
 @pytest.mark.parametrize("rr", [False, True])
 def test_furnace_matches_closed_form(built, tmp_path, rr):
     mscgpu, _ = built
@@ -45,10 +54,11 @@ def test_furnace_matches_closed_form(built, tmp_path, rr):
     K.check_unbiased(sphere, np.broadcast_to(sc.sphere_expected(), sphere.shape), what="GPU furnace rr=%s" % rr)
 
 
-@pytest.mark.parametrize("which", ["quad", "sphere", "furnace"])
+@pytest.mark.parametrize("which", ["quad", "sphere", "phong", "furnace"])
 def test_known_answer_scenes_match_the_oracle_per_sample(built, tmp_path, which):
     mscgpu, oracle = built
-    make = {"quad": K.quad_over_plane, "sphere": K.sphere_over_plane, "furnace": K.furnace}[which]
+    make = {"quad": K.quad_over_plane, "sphere": K.sphere_over_plane, "phong": K.phong_over_plane,
+            "furnace": K.furnace}[which]
     sc = make(str(tmp_path), width=64, height=64, rr=True)
     rgb, xy = _render(mscgpu, sc.path)
     _, wrgb, wxy, _ = oracle.Scene(sc.path).render(0)

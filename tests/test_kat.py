@@ -31,6 +31,19 @@ def test_oracle_direct_lighting_matches_closed_form(built, tmp_path, light, rr, 
 
 
 @pytest.mark.parametrize("rr", [False, True])
+def test_oracle_phong_direct_lighting_matches_quadrature(built, tmp_path, rr):
+    """The modified Phong lobe (an extension of the reference's shaders) against
+    the direct-lighting integral by Gauss-Legendre quadrature."""
+    _, oracle = built
+    sc = K.phong_over_plane(str(tmp_path), width=64, height=64, rr=rr)
+    s = oracle.Scene(sc.path)
+    for double in (False, True):
+        _, rgb, xy, _ = s.render(0, double=double)
+        rel, se = K.check_unbiased(rgb, sc.expected(xy), what="phong rr=%s fp64=%s" % (rr, double))
+        assert (se < 6e-3).all(), se
+
+
+@pytest.mark.parametrize("rr", [False, True])
 def test_oracle_furnace_matches_closed_form(built, tmp_path, rr):
     _, oracle = built
     sc = K.furnace(str(tmp_path), width=128, height=128, rr=rr)
