@@ -227,7 +227,7 @@ typedef struct msc_tuning {
   int digit_bits;     /* radix sort digit width: 4, 8 or 11 */
   int tuning;         /* read only: 1 while the autotuner is still sampling */
   int samples;        /* read only: candidate samples booked by the autotuner */
-  int ray_key_bits;   /* top bits of the 32-bit ray key that the ray sort orders: 16, 24 or 32;
+  int ray_key_bits;   /* top bits of the 32-bit ray key that the ray sort orders: 8, 16, 24 or 32;
                          0 = 16 for one scene, 24 (scene and bin above the key) for several */
 } msc_tuning;
 typedef struct msc_tune_sample {

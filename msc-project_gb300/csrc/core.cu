@@ -762,7 +762,7 @@ uint64_t Core::graph_key() const {
   const uint64_t bins = bins_.nbins == 6 ? 0 : (bins_.nbins == 26 ? 1 : 2);
   const uint64_t pers = persistent_trace ? 1 : 0;
   const uint64_t dig = sort_digits == 4 ? 0 : (sort_digits == 8 ? 1 : 2);
-  const uint64_t kb = (uint64_t)ray_key_bits_used() / 8;  // 2, 3 or 4
+  const uint64_t kb = (uint64_t)ray_key_bits_used() / 8;  // 1 to 4
   return ns | (k64 << 9) | ((uint64_t)hit_bits_ << 10) | ((uint64_t)ray_sort << 16) | ((uint64_t)hit_sort << 17) |
          ((uint64_t)merge_bins << 18) | ((uint64_t)wide_ << 19) | (bexp << 20) | (block << 25) | (bins << 27) |
          (pers << 29) | (dig << 30) | (kb << 32) | (1ull << 63);
@@ -1041,7 +1041,7 @@ TuneChoice Core::choice() const {
 }
 
 int Core::ray_key_bits_used() const {
-  if (ray_key_bits == 16 || ray_key_bits == 24 || ray_key_bits == 32) return ray_key_bits;
+  if (ray_key_bits == 8 || ray_key_bits == 16 || ray_key_bits == 24 || ray_key_bits == 32) return ray_key_bits;
   return scenes_.size() > 1 ? kRayKeyBitsScenes : kRayKeyBits;
 }
 
@@ -1054,7 +1054,9 @@ void Core::apply(const TuneChoice& c) {
   bins_.nbins = (c.bins == 26 || c.bins == 98) ? c.bins : 6;
   persistent_trace = c.persistent;
   sort_digits = (c.digit_bits == 4 || c.digit_bits == 11) ? c.digit_bits : 8;
-  ray_key_bits = (c.ray_key_bits == 16 || c.ray_key_bits == 24 || c.ray_key_bits == 32) ? c.ray_key_bits : 0;
+  ray_key_bits = (c.ray_key_bits == 8 || c.ray_key_bits == 16 || c.ray_key_bits == 24 || c.ray_key_bits == 32)
+                     ? c.ray_key_bits
+                     : 0;
 }
 
 void Core::start_autotune(int windows) {
@@ -1124,11 +1126,11 @@ void Core::tune_begin_dim() {
         add(c);
       }
     } else if (tune_dim_ == 6) {
-      // ray key width: the default and one more byte of the interleaved
-      // origin/direction key (finer order, one more sort pass)
+      // ray key width: the default, one byte less (a coarser order, one sort
+      // pass fewer) and one byte more (finer, one pass more)
       if (base.ray_sort) {
         const int def = scenes_.size() > 1 ? kRayKeyBitsScenes : kRayKeyBits;
-        for (int kb : {def, def + 8}) {
+        for (int kb : {def - 8, def, def + 8}) {
           TuneChoice c = base;
           c.ray_key_bits = kb;
           add(c);

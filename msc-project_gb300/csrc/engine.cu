@@ -1055,9 +1055,10 @@ static int set_tuning(Core& core, std::string* err, const msc_tuning* in) {
       (in->trace_block != 64 && in->trace_block != 128 && in->trace_block != 256) ||
       (in->bins != 6 && in->bins != 26 && in->bins != 98) ||
       (in->digit_bits != 4 && in->digit_bits != 8 && in->digit_bits != 11) ||
-      (in->ray_key_bits != 0 && in->ray_key_bits != 16 && in->ray_key_bits != 24 && in->ray_key_bits != 32)) {
+      (in->ray_key_bits != 0 && in->ray_key_bits != 8 && in->ray_key_bits != 16 && in->ray_key_bits != 24 &&
+       in->ray_key_bits != 32)) {
     *err = "tuning: batch exponent above the capacity, block size not 64, 128 or 256, bins not 6, 26 or 98, "
-           "digit width not 4, 8 or 11, or ray key bits not 0, 16, 24 or 32";
+           "digit width not 4, 8 or 11, or ray key bits not 0, 8, 16, 24 or 32";
     return MSC_ERR_ARG;
   }
   TuneChoice c;

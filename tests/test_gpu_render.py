@@ -258,3 +258,18 @@ def test_persistent_traversal_gives_the_same_image(built, box_scene, scene_dir, 
             st = pt.stats()
             assert st["closest_queries"] > 0
     assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
+
+
+def test_ray_key_width_does_not_change_the_image(built, box_scene):
+    """8-, 16-, 24- and 32-bit ray sort keys order the batches differently;
+    every path's result, and so the image, stays the same."""
+    mscgpu, _ = built
+    imgs = []
+    for kb in (8, 16, 24, 32):
+        with mscgpu.Pathtracer(box_scene) as pt:
+            pt.set_tuning(batch_exponent=12, ray_sort=True, hit_sort=False, ray_key_bits=kb)
+            assert pt.tuning()["ray_key_bits"] == kb
+            pt.process()
+            imgs.append(pt.image())
+    for im in imgs[1:]:
+        assert np.array_equal(im.view(np.uint32), imgs[0].view(np.uint32))
