@@ -1468,11 +1468,13 @@ int launch_filter(const JobRec& job, Film film, cudaStream_t s) {
   const int n = job.width * job.height;
   if (job.filter == FILTER_BOX) k_filter_box<<<grid_for(n), TB, 0, s>>>(job, film);
   else {
-    static bool attr = false;  // the tile's shared memory exceeds the 48 KB default
-    if (!attr) {
+    // the tile's shared memory exceeds the 48 KB default: opt in once (a
+    // function-local static is initialised once, also across host threads)
+    static const bool attr = [] {
       cudaFuncSetAttribute(k_filter_tent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FilterSmem));
-      attr = true;
-    }
+      return true;
+    }();
+    (void)attr;
     k_filter_tent<<<dim3((job.height + kFtY - 1) / kFtY, (job.width + kFtX - 1) / kFtX), kFsN, sizeof(FilterSmem),
                     s>>>(job, film);
   }

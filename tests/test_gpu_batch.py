@@ -237,3 +237,23 @@ def test_memory_budget_counts_scenes_and_job_images(built, scenes):
     b.set_memory_budget(0)
     b.add_scene(scenes[2])
     b.close()
+
+
+def test_serve_window_closes_admission_and_reports_busy_time(built, scenes):
+    """msc_serve_window: requests that arrive after the window are not served
+    (MSC_ERR_BUSY, counted); the admitted ones complete and match the same job
+    rendered alone; the GPU busy time is positive and below the wall time."""
+    mscgpu, _ = built
+    reqs = [(0.0, JOBS[0]), (0.0, JOBS[1]), (0.0, JOBS[4]), (5.0, JOBS[0]), (6.0, JOBS[1])]
+    b = mscgpu.Batch(batch_exponent=14, film_samples=1 << 20)
+    for s in scenes:
+        b.add_scene(s)
+    results, st = b.serve(reqs, window_s=0.5)
+    assert st["completed"] == 3 and st["not_admitted"] == 2
+    assert [r["status"] for r in results] == [0, 0, 0, -5, -5]
+    assert 0.0 < st["gpu_busy_s"] <= st["wall_s"]
+    assert st["wall_s"] < 5.0  # the late requests were not waited for
+    alone, aid = _batch(mscgpu, scenes, [JOBS[1]])
+    assert np.array_equal(b.image(results[1]["job_id"]).view(np.uint32), alone.image(aid[0]).view(np.uint32))
+    alone.close()
+    b.close()
