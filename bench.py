@@ -676,7 +676,9 @@ def hbm_stages(prof, peak, spp):
     for name, ms, nbytes, what in (
             ("bins", sm["bins"], 112.0 * closest, "112 B per ray entering the bins"),
             ("ray_sort", sm["ray_sort"], 36.0 * closest, "36 B per key: histogram read + two 16 B passes"),
-            ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)")):
+            ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)"),
+            ("shade", sm["shade"], 160.0 * closest, "160 B per closest hit: ray 48 B and hit 16 B read, "
+                                                   "continuation ray 48 B and shadow ray 48 B written")):
         if ms > 0:
             gbs = nbytes / (ms / 1e3) / 1e9
             out[name] = {"ms": round(ms, 3), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4), "alg_bytes": what}
