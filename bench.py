@@ -779,7 +779,7 @@ def run_gpu(args):
     for _ in range(args.steps):
         t = time.time()
         pt.process()
-        img = pt.image()
+        img = pt.image(copy=False)  # msc_image: the host image the pass copied back
         e2e_wall.append(time.time() - t)
         st = pt.stats()
         e2e_rays += st["closest_queries"] + st["shadow_queries"]

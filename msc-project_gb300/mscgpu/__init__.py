@@ -190,12 +190,15 @@ class Pathtracer:
         _check(self._lib.msc_process_device(self._h, C.byref(it)), self._h)
         return it.value
 
-    def image(self):
-        """Accumulated image as an (H, W, 3) float32 copy."""
+    def image(self, copy=True):
+        """Accumulated image as an (H, W, 3) float32 array: a copy, or with
+        copy=False a view of the handle's host buffer (what msc_image returns;
+        valid until the next process / clear / destroy)."""
         p = C.POINTER(C.c_float)()
         w, h = C.c_int(), C.c_int()
         _check(self._lib.msc_image(self._h, C.byref(p), C.byref(w), C.byref(h)), self._h)
-        return np.ctypeslib.as_array(p, shape=(h.value * w.value * 3,)).reshape(h.value, w.value, 3).copy()
+        a = np.ctypeslib.as_array(p, shape=(h.value * w.value * 3,)).reshape(h.value, w.value, 3)
+        return a.copy() if copy else a
 
     def clear(self):
         _check(self._lib.msc_clear(self._h), self._h)
