@@ -1109,6 +1109,7 @@ constexpr int kFtX = 8, kFtY = 30;                   // output tile
 constexpr int kFsX = kFtX + 2, kFsY = kFtY + 2;      // source pixels with their halo
 constexpr int kFsN = kFsX * kFsY;                    // 320 source pixels = block threads
 constexpr int kFtChunk = 4;                          // samples per source in one staging buffer
+constexpr int kFtStages = 2;                         // staging buffers in the ring
 constexpr int kFrgbPitch = kFsN + 1;                 // float4 rows: conflict-free stores and loads
 constexpr int kFposPitch = kFsN + 9;                 // float2 rows
 struct FilterStage {
@@ -1119,7 +1120,7 @@ struct FilterSmemPart {
   float4 part[9][kFrgbPitch];  // (r, g, b, weight) of source q for target slot (1+dx)*3 + (1+dy)
 };
 union FilterSmem {
-  FilterStage st[2];
+  FilterStage st[kFtStages];
   FilterSmemPart pa;
 };
 
@@ -1157,7 +1158,9 @@ __device__ __forceinline__ FilterCopies filter_copies(const JobRec& f, int x0, i
   return fc;
 }
 
-// Issues the copies of samples [s0, s0 + cs) of every source pixel of the tile.
+// Issues the copies of samples [s0, s0 + cs) of every source pixel of the tile
+// as one commit group (an empty group when cs <= 0, which keeps the count of
+// groups behind each chunk fixed).
 __device__ __forceinline__ void filter_stage(FilterStage& st, const FilterCopies& fc, const Film& film, int s0,
                                              int cs) {
 #pragma unroll
@@ -1192,15 +1195,23 @@ __global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
     cys[a] = (float)(qy + a - 1) + 0.5f;
   }
   const int chunks = (spp + kFtChunk - 1) / kFtChunk;
-  filter_stage(sm.st[0], fc, film, 0, min(kFtChunk, spp));
+  // chunks 0 .. kFtStages-2 in flight before the loop
+#pragma unroll
+  for (int c = 0; c < kFtStages - 1; ++c)
+    filter_stage(sm.st[c], fc, film, c * kFtChunk, min(kFtChunk, spp - c * kFtChunk));
   for (int c = 0; c < chunks; ++c) {
     const int s0 = c * kFtChunk, cs = min(kFtChunk, spp - s0);
-    cp_async_wait<0>();  // this thread's copies of chunk c have landed
+    // this thread's copies of chunk c have landed (the kFtStages-2 groups
+    // committed after chunk c's may still be in flight)
+    cp_async_wait<kFtStages - 2>();
     // chunk c is visible to all, and every thread is done with chunk c - 1,
-    // whose buffer the copies of chunk c + 1 now refill
+    // whose buffer the copies of chunk c + kFtStages - 1 now refill
     __syncthreads();
-    if (c + 1 < chunks) filter_stage(sm.st[(c + 1) & 1], fc, film, s0 + kFtChunk, min(kFtChunk, spp - s0 - kFtChunk));
-    const FilterStage& st = sm.st[c & 1];
+    {
+      const int cn = c + kFtStages - 1;
+      filter_stage(sm.st[cn % kFtStages], fc, film, cn * kFtChunk, min(kFtChunk, spp - cn * kFtChunk));
+    }
+    const FilterStage& st = sm.st[c % kFtStages];
     if (qvalid) {
       for (int k = 0; k < cs; ++k) {
         const float2 p = st.pos[k][q];
@@ -1225,7 +1236,8 @@ __global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
       }
     }
   }
-  __syncthreads();  // every thread is done with the staging buffers
+  cp_async_wait<0>();  // only empty groups remain; none may write into the partials
+  __syncthreads();     // every thread is done with the staging buffers
 #pragma unroll
   for (int t = 0; t < 9; ++t) sm.pa.part[t][q] = acc[t];
   __syncthreads();

@@ -180,12 +180,80 @@ __device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, 
   return ((s < 4 ? lo_word : hi_word) >> (8 * (s & 3))) & 0xffu;
 }
 
-// Byte s of the pair as a float, exactly: one byte permute builds the float
-// 2^23 + byte, one subtraction removes 2^23 (integer-to-float conversions run
-// on a slower pipe than these two).
-__device__ __forceinline__ float byte_float(uint32_t lo_word, uint32_t hi_word, int s) {
-  const uint32_t bits = __byte_perm(s < 4 ? lo_word : hi_word, 0x00004B00u, (uint32_t)(s & 3) | 0x5440u);
-  return __uint_as_float(bits) - 8388608.0f;
+// Byte s of the pair as the float 1 + byte * 2^-15, exactly: one byte
+// permute places the byte in the mantissa of 1.0f.  A plane at p + q * step
+// then meets the ray at (1 + q * 2^-15) * A + (b - A) with A = 2^15 * step / d
+// and b = (p - o) / d, so the conversion's subtraction moves out of the
+// per-slot work into one per-axis bias per node.
+__device__ __forceinline__ float byte_unit(uint32_t lo_word, uint32_t hi_word, int s) {
+  return __uint_as_float(__byte_perm(s < 4 ? lo_word : hi_word, 0x3F800000u, 0x7604u | ((uint32_t)(s & 3) << 4)));
+}
+
+// The eight child boxes of wide node `node` against the ray: returns the node
+// group (child base, internal mask, hit internal children in octant order)
+// and the triangle group (base, one bit per triangle of the hit leaf slots).
+// Entry distances are rounded down and exit distances up, bias included
+// (A * f is exact in the fused multiply-add, the bias is the only other
+// rounding), so every distance bounds the one computed from the exact byte
+// value: no true intersection of a box is culled.
+struct Node8Result {
+  uint32_t g_base, g_imask, g_hits, t_base, t_mask;
+};
+
+__device__ __forceinline__ Node8Result node8_test(const uint4* __restrict__ wn, int node, float3 o, float3 id,
+                                                  uint32_t oct, float tmin, float tmax) {
+  const uint4 A = __ldg(&wn[5 * node + 0]);
+  const uint4 B = __ldg(&wn[5 * node + 1]);
+  const uint4 Q0 = __ldg(&wn[5 * node + 2]);
+  const uint4 Q1 = __ldg(&wn[5 * node + 3]);
+  const uint4 Q2 = __ldg(&wn[5 * node + 4]);
+  const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
+  const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
+  const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
+  const uint32_t imask = A.w >> 24;
+  // per axis: the step in ray distance, scaled by 2^15 (exact), and the bias
+  // b - A rounded down for entries and up for exits
+  const float ax = (sx * id.x) * 32768.0f, ay = (sy * id.y) * 32768.0f, az = (sz * id.z) * 32768.0f;
+  const float bx = (__uint_as_float(A.x) - o.x) * id.x;
+  const float by = (__uint_as_float(A.y) - o.y) * id.y;
+  const float bz = (__uint_as_float(A.z) - o.z) * id.z;
+  const float bnx = __fsub_rd(bx, ax), bny = __fsub_rd(by, ay), bnz = __fsub_rd(bz, az);
+  const float bfx = __fsub_ru(bx, ax), bfy = __fsub_ru(by, ay), bfz = __fsub_ru(bz, az);
+  // per axis, the entry plane of a child box is its low plane when the
+  // inverse direction is positive and its high plane otherwise (the step
+  // scale is positive), so the slab min/max reduce to a choice per node
+  const bool nx = id.x < 0.f, ny = id.y < 0.f, nz = id.z < 0.f;
+  // quantised planes: lo x (Q0.x, Q0.y), lo y (Q0.z, Q0.w), lo z (Q1.x, Q1.y),
+  // hi x (Q1.z, Q1.w), hi y (Q2.x, Q2.y), hi z (Q2.z, Q2.w); words for slots 0-3, 4-7
+  const uint32_t enx0 = nx ? Q1.z : Q0.x, enx1 = nx ? Q1.w : Q0.y, exx0 = nx ? Q0.x : Q1.z, exx1 = nx ? Q0.y : Q1.w;
+  const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
+  const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
+  const float widen = 1.0000004f;
+  uint32_t nh = 0u, tm = 0u;
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const uint32_t m = byte_of(B.z, B.w, s);
+    const bool inner = ((imask >> s) & 1u) != 0u;
+    const float tnx = __fmaf_rd(byte_unit(enx0, enx1, s), ax, bnx);
+    const float tny = __fmaf_rd(byte_unit(eny0, eny1, s), ay, bny);
+    const float tnz = __fmaf_rd(byte_unit(enz0, enz1, s), az, bnz);
+    const float tfx = __fmaf_ru(byte_unit(exx0, exx1, s), ax, bfx);
+    const float tfy = __fmaf_ru(byte_unit(exy0, exy1, s), ay, bfy);
+    const float tfz = __fmaf_ru(byte_unit(exz0, exz1, s), az, bfz);
+    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+    const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax)) * widen;
+    if (tn <= tf) {
+      if (inner) nh |= 1u << ((uint32_t)s ^ oct);
+      else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+    }
+  }
+  Node8Result r;
+  r.g_base = B.x;
+  r.g_imask = imask;
+  r.g_hits = nh;
+  r.t_base = B.y;
+  r.t_mask = tm;
+  return r;
 }
 
 // Node and triangle indices are checked against num_nodes / num_tris before
@@ -197,17 +265,12 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
                                            TriHit* hit, int* overflow) {
   const float3 id = f3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
   const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-  // per axis, the entry plane of a child box is its low plane when the
-  // inverse direction is positive and its high plane otherwise (the step
-  // scale is positive), so the slab min/max reduce to a choice per node
-  const bool nx = id.x < 0.f, ny = id.y < 0.f, nz = id.z < 0.f;
   uint2 stack[kWideStack];
   int sp = 0;
   // the root as the only child of a virtual group: base 0, slot 0 internal
   uint32_t g_base = 0, g_imask = 1u, g_hits = 1u << oct;
   uint32_t t_base = 0, t_mask = 0;
   bool found = false;
-  const float widen = 1.0000004f;
   int steps = 0;
   int best_g = -1;
   while (true) {
@@ -228,47 +291,12 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
         *overflow = 3;
         return found;
       }
-      const uint4 A = __ldg(&wn[5 * node + 0]);
-      const uint4 B = __ldg(&wn[5 * node + 1]);
-      const uint4 Q0 = __ldg(&wn[5 * node + 2]);
-      const uint4 Q1 = __ldg(&wn[5 * node + 3]);
-      const uint4 Q2 = __ldg(&wn[5 * node + 4]);
-      const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
-      const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
-      const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
-      const uint32_t imask = A.w >> 24;
-      const float ax = sx * id.x, ay = sy * id.y, az = sz * id.z;
-      const float bx = (__uint_as_float(A.x) - o.x) * id.x;
-      const float by = (__uint_as_float(A.y) - o.y) * id.y;
-      const float bz = (__uint_as_float(A.z) - o.z) * id.z;
-      // quantised planes: lo x (Q0.x, Q0.y), lo y (Q0.z, Q0.w), lo z (Q1.x, Q1.y),
-      // hi x (Q1.z, Q1.w), hi y (Q2.x, Q2.y), hi z (Q2.z, Q2.w); words for slots 0-3, 4-7
-      const uint32_t enx0 = nx ? Q1.z : Q0.x, enx1 = nx ? Q1.w : Q0.y, exx0 = nx ? Q0.x : Q1.z, exx1 = nx ? Q0.y : Q1.w;
-      const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
-      const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
-      uint32_t nh = 0u, tm = 0u;
-#pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        const uint32_t m = byte_of(B.z, B.w, s);
-        const bool inner = ((imask >> s) & 1u) != 0u;
-        const float tnx = fmaf(byte_float(enx0, enx1, s), ax, bx);
-        const float tny = fmaf(byte_float(eny0, eny1, s), ay, by);
-        const float tnz = fmaf(byte_float(enz0, enz1, s), az, bz);
-        const float tfx = fmaf(byte_float(exx0, exx1, s), ax, bx);
-        const float tfy = fmaf(byte_float(exy0, exy1, s), ay, by);
-        const float tfz = fmaf(byte_float(exz0, exz1, s), az, bz);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax)) * widen;
-        if (tn <= tf) {
-          if (inner) nh |= 1u << ((uint32_t)s ^ oct);
-          else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-        }
-      }
-      g_base = B.x;
-      g_imask = imask;
-      g_hits = nh;
-      t_base = B.y;
-      t_mask = tm;
+      const Node8Result r = node8_test(wn, node, o, id, oct, tmin, tmax);
+      g_base = r.g_base;
+      g_imask = r.g_imask;
+      g_hits = r.g_hits;
+      t_base = r.t_base;
+      t_mask = r.t_mask;
     }
     while (t_mask != 0u) {
       const int k = (int)t_base + __ffs(t_mask) - 1;
@@ -393,48 +421,12 @@ __device__ __forceinline__ bool trav8_step(Trav8& s, uint2* stack, const uint4* 
       *overflow = 3;
       return true;
     }
-    const uint4 A = __ldg(&wn[5 * node + 0]);
-    const uint4 B = __ldg(&wn[5 * node + 1]);
-    const uint4 Q0 = __ldg(&wn[5 * node + 2]);
-    const uint4 Q1 = __ldg(&wn[5 * node + 3]);
-    const uint4 Q2 = __ldg(&wn[5 * node + 4]);
-    const float sx = __int_as_float((int)((A.w & 0xffu) << 23));
-    const float sy = __int_as_float((int)(((A.w >> 8) & 0xffu) << 23));
-    const float sz = __int_as_float((int)(((A.w >> 16) & 0xffu) << 23));
-    const uint32_t imask = A.w >> 24;
-    const float3 id = s.id, o = s.o;
-    const float ax = sx * id.x, ay = sy * id.y, az = sz * id.z;
-    const float bx = (__uint_as_float(A.x) - o.x) * id.x;
-    const float by = (__uint_as_float(A.y) - o.y) * id.y;
-    const float bz = (__uint_as_float(A.z) - o.z) * id.z;
-    const bool nx = id.x < 0.f, ny = id.y < 0.f, nz = id.z < 0.f;
-    const uint32_t enx0 = nx ? Q1.z : Q0.x, enx1 = nx ? Q1.w : Q0.y, exx0 = nx ? Q0.x : Q1.z, exx1 = nx ? Q0.y : Q1.w;
-    const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
-    const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
-    const float widen = 1.0000004f;
-    uint32_t nh = 0u, tm = 0u;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint32_t m = byte_of(B.z, B.w, q);
-      const bool inner = ((imask >> q) & 1u) != 0u;
-      const float tnx = fmaf(byte_float(enx0, enx1, q), ax, bx);
-      const float tny = fmaf(byte_float(eny0, eny1, q), ay, by);
-      const float tnz = fmaf(byte_float(enz0, enz1, q), az, bz);
-      const float tfx = fmaf(byte_float(exx0, exx1, q), ax, bx);
-      const float tfy = fmaf(byte_float(exy0, exy1, q), ay, by);
-      const float tfz = fmaf(byte_float(exz0, exz1, q), az, bz);
-      const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, s.tmin));
-      const float tf = fminf(fminf(tfx, tfy), fminf(tfz, s.tmax)) * widen;
-      if (tn <= tf) {
-        if (inner) nh |= 1u << ((uint32_t)q ^ s.oct);
-        else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-      }
-    }
-    s.g_base = B.x;
-    s.g_imask = imask;
-    s.g_hits = nh;
-    s.t_base = B.y;
-    s.t_mask = tm;
+    const Node8Result r = node8_test(wn, node, s.o, s.id, s.oct, s.tmin, s.tmax);
+    s.g_base = r.g_base;
+    s.g_imask = r.g_imask;
+    s.g_hits = r.g_hits;
+    s.t_base = r.t_base;
+    s.t_mask = r.t_mask;
     return false;
   }
   if (s.sp == 0) return true;
