@@ -378,8 +378,9 @@ constexpr int kWideLeafMax = 2;
 // triangle test relative to it (0.6 measured best of 0.15, 0.3 and 0.6).
 constexpr float kCollapseNode = 1.0f;
 constexpr float kCollapseTri = 0.6f;
-// a node's triangle bits (eight slots of at most kWideLeafMax) fit one word
-static_assert(8 * kWideLeafMax <= 32, "triangle bits of a node must fit one word");
+// slot s of a node owns the two triangle bits 2s, 2s + 1 (the traversal
+// spreads its 8-bit leaf-hit mask onto them)
+static_assert(kWideLeafMax <= 2, "a leaf slot owns two triangle bits");
 
 struct WideBuild {
   std::vector<uint32_t> words;  // 20 words per node
@@ -558,17 +559,15 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
     quantise_axis(lo.x, hi.x, &e[0], &s[0]);
     quantise_axis(lo.y, hi.y, &e[1], &s[1]);
     quantise_axis(lo.z, hi.z, &e[2], &s[2]);
-    uint32_t imask = 0, meta[2] = {0, 0}, q[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    uint32_t imask = 0, valid = 0, q[6][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
     const uint32_t child_base = (uint32_t)queue.size();
     const uint32_t tri_base = (uint32_t)out->tri_perm.size();
     for (int i = 0; i < k; ++i) {
       const int c = C[i];
       if (!filled[i]) continue;  // an empty slot
-      uint32_t m = 0;
       if (is_leafish(c)) {
         // the subtree's leaves (restructured treelets need not hold a
         // contiguous leaf range, so they are collected by a walk)
-        const uint32_t off = (uint32_t)out->tri_perm.size() - tri_base;
         int walk[2 * kWideLeafMax], nw = 0, cnt = 0;
         walk[nw++] = c;
         while (nw > 0) {
@@ -581,12 +580,14 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
             walk[nw++] = ch[x].x;
           }
         }
-        m = ((uint32_t)cnt << 5) | off;
+        // slot i owns triangle bits 2i and 2i + 1; the triangles themselves
+        // are stored in slot order, so a bit's triangle is the count of
+        // valid bits below it past the node's triangle base
+        valid |= ((1u << cnt) - 1u) << (2 * i);
       } else {
         imask |= 1u << i;
         queue.push_back(c);
       }
-      meta[i >> 2] |= m << (8 * (i & 3));
       const float4 cl = box_lo(c), chh = box_hi(c);
       const float cll[3] = {cl.x, cl.y, cl.z}, chl[3] = {chh.x, chh.y, chh.z}, pl[3] = {lo.x, lo.y, lo.z};
       for (int a = 0; a < 3; ++a) {
@@ -602,8 +603,8 @@ void collapse_wide(int n, const std::vector<int2>& ch, const std::vector<float4>
     W[3] = (uint32_t)(e[0] + 127) | ((uint32_t)(e[1] + 127) << 8) | ((uint32_t)(e[2] + 127) << 16) | (imask << 24);
     W[4] = child_base;
     W[5] = tri_base;
-    W[6] = meta[0];
-    W[7] = meta[1];
+    W[6] = valid;
+    W[7] = 0;
     // q_lo x, y, z then q_hi x, y, z, two words (slots 0-3, 4-7) each
     for (int a = 0; a < 6; ++a) {
       W[8 + 2 * a] = q[a][0];

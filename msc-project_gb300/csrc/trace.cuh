@@ -164,7 +164,9 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
 //   w3      per-axis step exponents e+127 (bits 0-23) and the internal-child mask (bits 24-31)
 //   w4      index of the first internal child node (internal children are consecutive)
 //   w5      index of the first leaf triangle (leaf triangles of a node are consecutive)
-//   w6, w7  one meta byte per slot: 0 empty or internal, else (count << 5) | triangle offset
+//   w6      valid triangle bits: slot s owns bits 2s, 2s + 1 (one per triangle of a
+//           leaf slot); the triangle of bit b is w5 + popc(w6 & ((1 << b) - 1))
+//   w7      0
 //   w8..w19 quantised child boxes, one byte per slot: lo.x, lo.y, lo.z, hi.x, hi.y, hi.z,
 //           two words each (slots 0-3, 4-7); child box = p + q * 2^e per axis.
 // Traversal keeps node groups, not single children (Ylitie, Karras and Laine,
@@ -172,12 +174,44 @@ __device__ __forceinline__ bool bvh_trace(const float4* __restrict__ nodes, cons
 // children still to visit, as bits in the ray's octant order (bit j = slot
 // j ^ octant).  The slots were assigned by octant at build time, so taking
 // the lowest bit first visits the children roughly front to back.  Each
-// visited node also yields a triangle group (triangle base + one bit per
-// triangle of its hit leaf slots), intersected before the next node.
+// visited node also yields a triangle group (triangle base, the node's valid
+// triangle bits and the bits of its hit leaf slots), intersected before the
+// next node.
 constexpr int kWideStack = 64;
 
-__device__ __forceinline__ uint32_t byte_of(uint32_t lo_word, uint32_t hi_word, int s) {
-  return ((s < 4 ? lo_word : hi_word) >> (8 * (s & 3))) & 0xffu;
+// Three-input minimum and maximum (PTX ISA 8.8, sm_100 and later); like
+// fminf / fmaxf they return the other inputs when one is NaN.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
+// Moves bit s of an 8-bit mask to bit s ^ oct: one masked delta swap per
+// octant bit (adjacent bits, bit pairs, nibbles); m1, m2, m4 are 0x55, 0x33,
+// 0x0f where the ray's octant has that bit, else 0.  t holds bits only where
+// the multiply's shifted copy cannot carry into them.
+__device__ __forceinline__ uint32_t octant_order(uint32_t x, uint32_t m1, uint32_t m2, uint32_t m4) {
+  uint32_t t = (x ^ (x >> 1)) & m1;
+  x ^= t * 3u;
+  t = (x ^ (x >> 2)) & m2;
+  x ^= t * 5u;
+  t = (x ^ (x >> 4)) & m4;
+  x ^= t * 17u;
+  return x;
+}
+
+// Bit s of an 8-bit mask onto bits 2s and 2s + 1.
+__device__ __forceinline__ uint32_t spread_pairs(uint32_t x) {
+  x = (x | (x << 4)) & 0x0f0fu;
+  x = (x | (x << 2)) & 0x3333u;
+  x = (x | (x << 1)) & 0x5555u;
+  return x * 3u;
 }
 
 // Byte s of the pair as the float 1 + byte * 2^-15, exactly: one byte
@@ -191,13 +225,13 @@ __device__ __forceinline__ float byte_unit(uint32_t lo_word, uint32_t hi_word, i
 
 // The eight child boxes of wide node `node` against the ray: returns the node
 // group (child base, internal mask, hit internal children in octant order)
-// and the triangle group (base, one bit per triangle of the hit leaf slots).
-// Entry distances are rounded down and exit distances up, bias included
-// (A * f is exact in the fused multiply-add, the bias is the only other
-// rounding), so every distance bounds the one computed from the exact byte
-// value: no true intersection of a box is culled.
+// and the triangle group (base, the node's valid triangle bits, the bits of
+// the hit leaf slots).  Entry distances are rounded down and exit distances
+// up, bias included (A * f is exact in the fused multiply-add, the bias is
+// the only other rounding), so every distance bounds the one computed from
+// the exact byte value: no true intersection of a box is culled.
 struct Node8Result {
-  uint32_t g_base, g_imask, g_hits, t_base, t_mask;
+  uint32_t g_base, g_imask, g_hits, t_base, t_valid, t_mask;
 };
 
 __device__ __forceinline__ Node8Result node8_test(const uint4* __restrict__ wn, int node, float3 o, float3 id,
@@ -229,31 +263,35 @@ __device__ __forceinline__ Node8Result node8_test(const uint4* __restrict__ wn, 
   const uint32_t eny0 = ny ? Q2.x : Q0.z, eny1 = ny ? Q2.y : Q0.w, exy0 = ny ? Q0.z : Q2.x, exy1 = ny ? Q0.w : Q2.y;
   const uint32_t enz0 = nz ? Q2.z : Q1.x, enz1 = nz ? Q2.w : Q1.y, exz0 = nz ? Q1.x : Q2.z, exz1 = nz ? Q1.y : Q2.w;
   const float widen = 1.0000004f;
-  uint32_t nh = 0u, tm = 0u;
+  uint32_t hm = 0u;  // bit s: the box of slot s is hit
 #pragma unroll
   for (int s = 0; s < 8; ++s) {
-    const uint32_t m = byte_of(B.z, B.w, s);
-    const bool inner = ((imask >> s) & 1u) != 0u;
     const float tnx = __fmaf_rd(byte_unit(enx0, enx1, s), ax, bnx);
     const float tny = __fmaf_rd(byte_unit(eny0, eny1, s), ay, bny);
     const float tnz = __fmaf_rd(byte_unit(enz0, enz1, s), az, bnz);
     const float tfx = __fmaf_ru(byte_unit(exx0, exx1, s), ax, bfx);
     const float tfy = __fmaf_ru(byte_unit(exy0, exy1, s), ay, bfy);
     const float tfz = __fmaf_ru(byte_unit(exz0, exz1, s), az, bfz);
-    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-    const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax)) * widen;
-    if (tn <= tf) {
-      if (inner) nh |= 1u << ((uint32_t)s ^ oct);
-      else if (m != 0u) tm |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-    }
+    const float tn = fmax3(tnx, tny, fmaxf(tnz, tmin));
+    const float tf = fmin3(tfx, tfy, fminf(tfz, tmax)) * widen;
+    if (tn <= tf) hm |= 1u << s;
   }
   Node8Result r;
   r.g_base = B.x;
   r.g_imask = imask;
-  r.g_hits = nh;
+  r.g_hits = octant_order(hm & imask, (oct & 1u) ? 0x55u : 0u, (oct & 2u) ? 0x33u : 0u, (oct & 4u) ? 0x0fu : 0u);
   r.t_base = B.y;
-  r.t_mask = tm;
+  r.t_valid = B.z;
+  // empty slots own no valid bits, so their (degenerate) boxes add nothing
+  r.t_mask = spread_pairs(hm & ~imask) & B.z;
   return r;
+}
+
+// Triangle of the lowest bit of a node's triangle mask, which it clears.
+__device__ __forceinline__ int take_triangle(uint32_t& t_mask, uint32_t t_base, uint32_t t_valid) {
+  const uint32_t lb = t_mask & (0u - t_mask);
+  t_mask ^= lb;
+  return (int)(t_base + (uint32_t)__popc(t_valid & (lb - 1u)));
 }
 
 // Node and triangle indices are checked against num_nodes / num_tris before
@@ -269,7 +307,7 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
   int sp = 0;
   // the root as the only child of a virtual group: base 0, slot 0 internal
   uint32_t g_base = 0, g_imask = 1u, g_hits = 1u << oct;
-  uint32_t t_base = 0, t_mask = 0;
+  uint32_t t_base = 0, t_valid = 0, t_mask = 0;
   bool found = false;
   int steps = 0;
   int best_g = -1;
@@ -296,11 +334,11 @@ __device__ __forceinline__ bool bvh8_trace(const uint4* __restrict__ wn, const f
       g_imask = r.g_imask;
       g_hits = r.g_hits;
       t_base = r.t_base;
+      t_valid = r.t_valid;
       t_mask = r.t_mask;
     }
     while (t_mask != 0u) {
-      const int k = (int)t_base + __ffs(t_mask) - 1;
-      t_mask &= t_mask - 1u;
+      const int k = take_triangle(t_mask, t_base, t_valid);
       if (k >= num_tris) {
         *overflow = 3;
         return found;
@@ -346,7 +384,7 @@ struct Trav8 {
   float3 o, d, id;
   float tmin, tmax;
   uint32_t oct;
-  uint32_t g_base, g_imask, g_hits, t_base, t_mask;
+  uint32_t g_base, g_imask, g_hits, t_base, t_valid, t_mask;
   int sp, steps, best_g;
   bool found;
 };
@@ -362,6 +400,7 @@ __device__ __forceinline__ void trav8_init(Trav8& s, float3 o, float3 d, float t
   s.g_imask = 1u;
   s.g_hits = 1u << s.oct;
   s.t_base = 0;
+  s.t_valid = 0;
   s.t_mask = 0;
   s.sp = 0;
   s.steps = 0;
@@ -375,8 +414,7 @@ __device__ __forceinline__ bool trav8_step(Trav8& s, uint2* stack, const uint4* 
                                            const float4* __restrict__ tris, int num_nodes, int num_tris, TriHit* hit,
                                            int* overflow) {
   if (s.t_mask != 0u) {
-    const int k = (int)s.t_base + __ffs(s.t_mask) - 1;
-    s.t_mask &= s.t_mask - 1u;
+    const int k = take_triangle(s.t_mask, s.t_base, s.t_valid);
     if (k >= num_tris) {
       *overflow = 3;
       return true;
@@ -426,6 +464,7 @@ __device__ __forceinline__ bool trav8_step(Trav8& s, uint2* stack, const uint4* 
     s.g_imask = r.g_imask;
     s.g_hits = r.g_hits;
     s.t_base = r.t_base;
+    s.t_valid = r.t_valid;
     s.t_mask = r.t_mask;
     return false;
   }
