@@ -38,10 +38,10 @@ SEED = 20261203
 ALG_BYTES_TRACE = 52  # per closest-hit query: read ray 32 B (org, dir), write hit 20 B
 # DRAM bytes per closest-hit query of k_trace_closest, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum) of the half-scale terrain:
-# 71.8 MB and 70.4 MB for two launches of 1,048,576 rays (camera rays, first
-# bounces), i.e. ~68 B per ray: the ray and hit records plus node and triangle
-# misses.
-DRAM_BYTES_PER_CLOSEST = (71.77e6 + 70.39e6) / (2 * 1048576)
+# 76.5 MB and 75.1 MB for two launches of 1,048,576 rays (camera rays, first
+# bounces), i.e. ~72 B per ray: the ray and hit records plus node and
+# triangle misses.
+DRAM_BYTES_PER_CLOSEST = (76.48e6 + 75.08e6) / (2 * 1048576)
 
 
 def log(*a):
@@ -663,22 +663,32 @@ TUNE_KEYS = ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "p
              "ray_key_bits")
 
 
-def hbm_stages(prof, peak, spp):
+def hbm_stages(prof, peak, spp, batch_exponent):
     """Achieved HBM bandwidth of the bandwidth-bound stages from one profiled
     pass: algorithmic bytes per ray (or per sample) / the stage's event time."""
     sm = prof["stage_ms"]
     closest = prof["closest_queries"]
     paths = prof["width"] * prof["height"] * spp
     out = {}
-    # bin partition: every ray that leaves shading (and every camera ray) is read
-    # from staging (48 B) and written into its bin (48 B) with its key (4 B),
-    # plus the count, scan and commit passes (~12 B)
+    # batches of 2^13 rays and more bin directly: the shading writes each
+    # continuing ray (48 B) and its sort key (4 B) into its bin, and the bins
+    # stage is the partition of the camera rays plus one small commit per
+    # batch; smaller batches partition every ray through staging (read 48 B,
+    # written 48 B with its 4 B key, plus the count, scan and commit passes)
+    if batch_exponent >= 13:
+        bins_bytes, bins_what = 112.0 * paths, "112 B per camera ray partitioned into the bins"
+        shade_bytes, shade_what = 164.0 * closest, ("164 B per closest hit: ray 48 B and hit 16 B read, continuation "
+                                                     "ray 48 B with its 4 B key into its bin and shadow ray 48 B "
+                                                     "written")
+    else:
+        bins_bytes, bins_what = 112.0 * closest, "112 B per ray entering the bins"
+        shade_bytes, shade_what = 160.0 * closest, ("160 B per closest hit: ray 48 B and hit 16 B read, "
+                                                     "continuation ray 48 B and shadow ray 48 B written")
     for name, ms, nbytes, what in (
-            ("bins", sm["bins"], 112.0 * closest, "112 B per ray entering the bins"),
+            ("bins", sm["bins"], bins_bytes, bins_what),
             ("ray_sort", sm["ray_sort"], 36.0 * closest, "36 B per key: histogram read + two 16 B passes"),
             ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)"),
-            ("shade", sm["shade"], 160.0 * closest, "160 B per closest hit: ray 48 B and hit 16 B read, "
-                                                   "continuation ray 48 B and shadow ray 48 B written")):
+            ("shade", sm["shade"], shade_bytes, shade_what)):
         if ms > 0:
             gbs = nbytes / (ms / 1e3) / 1e9
             out[name] = {"ms": round(ms, 3), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4), "alg_bytes": what}
@@ -805,11 +815,11 @@ def run_gpu(args):
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": DRAM_BYTES_PER_CLOSEST * prof["closest_queries"] / trace_launches,
                 "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of an ncu capture of the half-scale "
-                                "terrain (1,048,576 rays per launch: 71.8 MB and 70.4 MB), scaled by the rays of an "
+                                "terrain (1,048,576 rays per launch: 76.5 MB and 75.1 MB), scaled by the rays of an "
                                 "average full-size launch",
                 "alg_bytes": "52 B per closest-hit query (ray 32 B read, hit 20 B written; BVH bytes excluded)",
                 "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "top_stage": top,
-                "hbm_stages": hbm_stages(prof, peak, info["spp"])}
+                "hbm_stages": hbm_stages(prof, peak, info["spp"], tuned_d["batch_exponent"])}
     lat = sorted(dev_ms)
     out = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

@@ -186,16 +186,19 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   free_ranges_.assign(1, std::make_pair((size_t)0, sample_cap_));
   const int B = batch_cap_, G = generation_, S = staging_cap_;
   const int part_tiles = (std::max(S, B) + kPartTile - 1) / kPartTile;
-  const size_t chunks = bin_pool_chunks((size_t)G);
+  const size_t chunks = bin_pool_chunks((size_t)G, (size_t)B);
   const int max_chunks = (int)(((size_t)G + kChunk - 1) / kChunk) + 1;
   const size_t pool_rays = chunks * (size_t)kChunk;
+  const int pend_cols = B / kChunk + 2;              // new chunks one batch's appends can take per bin
+  const int retire_cap = B / kChunk + kMaxBins + 1;  // chunks one batch can hold back
   size_t bytes = 3 * al256(pool_rays * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
                  2 * al256((size_t)kMaxBins * 4) + al256((size_t)kMaxBins * max_chunks * 4) + al256(chunks * 4) +
                  al256(4) +
                  10 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(pool_rays * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B, 11) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
-                 al256((size_t)(kMaxBins + 1) * part_tiles * 4) + 4096;
+                 al256((size_t)(kMaxBins + 1) * part_tiles * 4) + al256((size_t)kMaxBins * 4) +
+                 al256((size_t)kMaxBins * pend_cols * 4) + al256((size_t)retire_cap * 4) + al256(4) + 4096;
   CK(cudaMalloc(&arena_, bytes));
   Arena A{arena_, 0};
   bins_.rays.o = A.take<float4>(pool_rays);
@@ -234,6 +237,12 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   }
   bins_.tile_counts = A.take<uint32_t>((size_t)(kMaxBins + 1) * part_tiles);
   bins_.max_tiles = part_tiles;
+  bins_.cursor = A.take<int>(kMaxBins);
+  bins_.pend = A.take<int>((size_t)kMaxBins * pend_cols);
+  bins_.pend_cols = pend_cols;
+  bins_.retired = A.take<int>(retire_cap);
+  bins_.retire_cap = retire_cap;
+  bins_.n_retired = A.take<int>(1);
   bins_.count = ctr_->bin_count;
   bins_.in_bins = &ctr_->in_bins;
   bins_.err = &ctr_->err;
@@ -247,6 +256,11 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   sort_init();
   launch_pool_reset(bins_, stream_);
   CK(cudaMemsetAsync(bins_.keys, 0, (size_t)bins_.num_chunks * kChunk * 4, stream_));
+  // every pool record starts as a well-formed ray (job, scene and sample 0),
+  // so that no position ever reads as out-of-range indices
+  CK(cudaMemsetAsync(bins_.rays.o, 0, pool_rays * sizeof(float4), stream_));
+  CK(cudaMemsetAsync(bins_.rays.d, 0, pool_rays * sizeof(float4), stream_));
+  CK(cudaMemsetAsync(bins_.rays.w, 0, pool_rays * sizeof(float4), stream_));
   CK(cudaStreamSynchronize(stream_));
   CK(cudaMallocHost(&h_ctr_, sizeof(Counters)));
   memset(h_ctr_, 0, sizeof(Counters));
@@ -790,9 +804,11 @@ int Core::enqueue_batch(int index, bool overlap) {
   int* shc = &ctr_->shadow_count[q];
   int scene_bits = 0;
   while ((1 << scene_bits) < ns) ++scene_bits;
+  // direct binning: the shading appends the continuing rays into the bins
+  const bool direct = B >= kDirectMin;
   {
     StageClock t(this, MSC_STAGE_OTHER);
-    t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, ctr_, st));
+    t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, ctr_, st, direct));
   }
   const uint32_t* perm = nullptr;
   if (ray_sort) {
@@ -866,7 +882,7 @@ int Core::enqueue_batch(int index, bool overlap) {
     StageClock t(this, MSC_STAGE_SHADE);
     CK(cudaMemsetAsync(shc, 0, sizeof(int), st));
     t.done(launch_shade(d_scenes_, d_jobs_, film_, rays, slots, hits_, order, B, staging_, shadow_[q], shc, d_job_done_,
-                        st, nb));
+                        st, nb, direct ? &bins_ : nullptr, (direct && ray_sort) ? d_scenes_ : nullptr));
   }
   {
     StageClock t(this, MSC_STAGE_SHADOW);
@@ -882,7 +898,8 @@ int Core::enqueue_batch(int index, bool overlap) {
   }
   {
     StageClock t(this, MSC_STAGE_BINS);
-    t.done(launch_bin_partition(staging_, B, bins_, st, nb, ray_sort ? d_scenes_ : nullptr));
+    if (direct) t.done(launch_append_commit(bins_, st));
+    else t.done(launch_bin_partition(staging_, B, bins_, st, nb, ray_sort ? d_scenes_ : nullptr));
   }
   return MSC_OK;
 }
@@ -988,6 +1005,7 @@ int Core::step(bool* idle) {
   if (h_ctr_->err != 0) {
     const int e = h_ctr_->err;
     err = (e & ERR_BIN_OVERFLOW)    ? "a direction bin overflowed"
+          : (e & ERR_APPEND_WAIT)   ? "a bin append waited past its cap for a chunk"
           : (e & ERR_TRAVERSAL_CAP) ? "BVH traversal exceeded its step cap"
           : (e & kSortErrLookback)  ? "radix sort look-back exceeded its spin cap"
           : (e & ERR_BVH_INDEX)     ? "BVH traversal met an out-of-range node or triangle index"

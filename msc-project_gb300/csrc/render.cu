@@ -292,10 +292,13 @@ __global__ void k_pool_reset(BinPool pool) {
   if (i < kMaxBins) {
     pool.count[i] = 0;
     pool.held[i] = 0;
+    if (pool.cursor) pool.cursor[i] = 0;
   }
+  if (pool.pend && i < kMaxBins * pool.pend_cols) pool.pend[i] = -1;
   if (i == 0) {
     *pool.free_top = pool.num_chunks;
     *pool.in_bins = 0;
+    if (pool.n_retired) *pool.n_retired = 0;
   }
 }
 
@@ -318,7 +321,7 @@ __global__ void k_cardinal(const float4* __restrict__ d, int n, int* __restrict_
 // ties to the lower bin), thread 0 then walks the ranks.  Every bin of the
 // pool is a candidate, so rays of a bin function used before a retune drain too.
 __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap, int merge, int scene_bits,
-                                                    BatchPlan* plan, Counters* ctr) {
+                                                    BatchPlan* plan, Counters* ctr, int direct) {
   __shared__ int cnt[kMaxBins];
   __shared__ int by_rank[kMaxBins];
   __shared__ int f_bin[kMaxBins], f_keep[kMaxBins], f_held[kMaxBins], f_ofs[kMaxBins + 1];
@@ -340,7 +343,13 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
       const int c = cnt[b];
       if (c == 0) break;
       if (k > 0 && !merge) break;
-      const int take = min(batch_cap - nb, c);
+      int take = min(batch_cap - nb, c);
+      if (direct && take < c) {
+        // leave the bin chunk-aligned, so that its appends start in a fresh
+        // chunk and never overwrite a ray of this batch
+        take = c - (((c - take) + kChunk - 1) & ~(kChunk - 1));
+        if (take <= 0) continue;  // the room left is below this bin's partial chunk
+      }
       const int left = c - take;
       plan->seg.bin[nsg] = b;
       plan->seg.start[nsg] = left;
@@ -361,7 +370,8 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
     f_ofs[nsg] = freed;
     nsg_s = nsg;
     top_s = *pool.free_top;
-    *pool.free_top = top_s + freed;
+    if (direct) *pool.n_retired = freed;  // held back until the append commit
+    else *pool.free_top = top_s + freed;
     plan->seg.count = nsg;
     plan->seg.prefix[nsg] = nb;
     plan->nb = nb;
@@ -373,10 +383,84 @@ __global__ void __launch_bounds__(kBinRadix) k_plan(BinPool pool, int batch_cap,
     ctr->batches += nb > 0 ? 1ull : 0ull;
   }
   __syncthreads();
+  int* dst = direct ? pool.retired : pool.free_stack + top_s;
   for (int k = 0; k < nsg_s; ++k) {
     const int b = f_bin[k], keep = f_keep[k], nfree = f_held[k] - keep;
-    for (int h = t; h < nfree; h += blockDim.x)
-      pool.free_stack[top_s + f_ofs[k] + h] = pool.table[b * pool.max_chunks + keep + h];
+    // (the entries stay: the batch's ray keys and slots are read through them)
+    for (int h = t; h < nfree; h += blockDim.x) dst[f_ofs[k] + h] = pool.table[b * pool.max_chunks + keep + h];
+  }
+  if (direct && t < kMaxBins) pool.cursor[t] = pool.count[t];
+}
+
+// Direct binning, after the appends: bin b's rays [count, cursor) sit in its
+// held chunks and the chunks taken for it past them (pending), which join its
+// chunk table up to its first failed take (whose rays are dropped, the error
+// already set; chunks taken past it go back to the free stack); the batch's
+// chunks return to the free stack.  One block.
+constexpr int kCommitBlock = 1024;
+
+__device__ __forceinline__ int commit_bin_of(const int* ofs, int e) {
+  int lo = 0, hi = kMaxBins - 1;  // the last bin whose offset is <= e
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ofs[mid] <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kCommitBlock) k_append_commit(BinPool pool) {
+  __shared__ int kb_s[kMaxBins], fail_s[kMaxBins], ofs_s[kMaxBins + 1];
+  const int t = threadIdx.x;
+  if (t < kMaxBins) {
+    const int c0 = pool.count[t], cur = pool.cursor[t], kb = pool.held[t];
+    kb_s[t] = kb;
+    fail_s[t] = cur > c0 ? max(kb, min((cur + kChunk - 1) >> kChunkShift, kb + pool.pend_cols)) : kb;
+  }
+  if (t == 0 && *pool.free_top < 0) *pool.free_top = 0;  // takes from an empty stack took nothing
+  __syncthreads();
+  if (t == 0) {  // the pending entries of all bins, as one index space
+    int o = 0;
+    for (int b = 0; b < kMaxBins; ++b) {
+      ofs_s[b] = o;
+      o += fail_s[b] - kb_s[b];
+    }
+    ofs_s[kMaxBins] = o;
+  }
+  __syncthreads();
+  const int total = ofs_s[kMaxBins];
+  for (int e = t; e < total; e += kCommitBlock) {  // each bin's first failed take
+    const int b = commit_bin_of(ofs_s, e), k = kb_s[b] + (e - ofs_s[b]);
+    if (pool.pend[b * pool.pend_cols + (k - kb_s[b])] < 0 || k >= pool.max_chunks) atomicMin(&fail_s[b], k);
+  }
+  __syncthreads();
+  for (int e = t; e < total; e += kCommitBlock) {
+    const int b = commit_bin_of(ofs_s, e), k = kb_s[b] + (e - ofs_s[b]);
+    int* pe = &pool.pend[b * pool.pend_cols + (k - kb_s[b])];
+    const int x = *pe;
+    *pe = -1;
+    if (k < fail_s[b]) pool.table[b * pool.max_chunks + k] = x;
+    else if (x >= 0) pool.free_stack[atomicAdd(pool.free_top, 1)] = x;
+  }
+  int added = 0;
+  if (t < kMaxBins) {
+    const int c0 = pool.count[t], cur = pool.cursor[t];
+    if (cur > c0) {
+      const int nh = fail_s[t];
+      const int c = min(cur, nh << kChunkShift);
+      pool.count[t] = c;
+      pool.held[t] = nh;
+      added = c - c0;
+    }
+  }
+  if (added > 0) atomicAdd(pool.in_bins, added);
+  __syncthreads();
+  const int top = *pool.free_top, nr = *pool.n_retired;
+  for (int i = t; i < nr; i += kCommitBlock) pool.free_stack[top + i] = pool.retired[i];
+  __syncthreads();
+  if (t == 0) {
+    *pool.free_top = top + nr;
+    *pool.n_retired = 0;
   }
 }
 
@@ -703,12 +787,93 @@ __device__ __forceinline__ float3 frame_dir(float3 a, float x, float y, float z)
 constexpr int kShadowGroups = 64;  // two per lane of one warp in the group scan
 static_assert(kShadowGroups == 64 && TB >= kShadowGroups, "the shadow group scan takes one warp");
 
+constexpr int kAppendSpinCap = 1 << 20;
+
+__device__ __forceinline__ int ld_volatile_i(const int* p) { return *(const volatile int*)p; }
+
+// Direct binning: the continuing ray (dead when b < 0) joins direction bin b
+// at a position from the bin's cursor.  One atomic per bin and block, and the
+// block's rays of one bin keep their block order (warps, then lanes), so runs
+// of rays that were traced next to each other stay together in the bin.
+// Positions past the chunks the bin held at the plan fall in chunks taken
+// from the free stack by the lane that holds the chunk's first position; the
+// others wait for it (bounded).  All threads of the block call this.
+constexpr int kShadeWarps = TB / 32;
+__device__ __forceinline__ void bin_append(const BinPool& pool, int b, float4 no, float4 nd, float4 nw,
+                                           const SceneRec* __restrict__ key_scenes) {
+  __shared__ int wcnt[kShadeWarps][kMaxBins];  // per warp and bin: count, then the warp's offset in the block's run
+  __shared__ int bbase[kMaxBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nbins = pool.nbins;
+  for (int i = threadIdx.x; i < kShadeWarps * nbins; i += TB) wcnt[i / nbins][i % nbins] = 0;
+  __syncthreads();
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  if (b >= 0 && lane == __ffs(peers) - 1) wcnt[warp][b] = __popc(peers);
+  __syncthreads();
+  if (threadIdx.x < nbins) {
+    int run = 0;
+    for (int w = 0; w < kShadeWarps; ++w) {
+      const int c = wcnt[w][threadIdx.x];
+      wcnt[w][threadIdx.x] = run;
+      run += c;
+    }
+    bbase[threadIdx.x] = run > 0 ? atomicAdd(&pool.cursor[threadIdx.x], run) : 0;
+  }
+  __syncthreads();
+  const int pos = b >= 0 ? bbase[b] + wcnt[warp][b] + __popc(peers & ((1u << lane) - 1u)) : 0;
+  int chunk = -1;
+  int* wait_on = nullptr;
+  if (b >= 0) {
+    const int k = pos >> kChunkShift, kb = pool.held[b];
+    if (k < kb) {
+      chunk = pool.table[b * pool.max_chunks + k];  // the bin's partial top chunk
+    } else if (k - kb < pool.pend_cols && k < pool.max_chunks) {
+      int* e = &pool.pend[b * pool.pend_cols + (k - kb)];
+      if ((pos & (kChunk - 1)) == 0) {
+        const int top = atomicSub(pool.free_top, 1) - 1;
+        chunk = top >= 0 ? pool.free_stack[top] : -2;
+        if (chunk < 0) atomicOr(pool.err, ERR_BIN_OVERFLOW);
+        *(volatile int*)e = chunk;
+        __threadfence();
+      } else {
+        wait_on = e;
+      }
+    } else {
+      atomicOr(pool.err, ERR_BIN_OVERFLOW);
+    }
+  }
+  __syncwarp();
+  if (wait_on) {  // a chunk another lane is taking
+    int spins = 0;
+    while ((chunk = ld_volatile_i(wait_on)) == -1) {
+      if (++spins > kAppendSpinCap) {
+        atomicOr(pool.err, ERR_APPEND_WAIT);
+        break;
+      }
+    }
+  }
+  if (chunk >= 0) {
+    const int o = chunk * kChunk + (pos & (kChunk - 1));
+    pool.rays.o[o] = no;
+    pool.rays.d[o] = nd;
+    pool.rays.w[o] = nw;
+    if (key_scenes) {  // the ray sort key, in the ray's scene box
+      const int sc = info_scene(__float_as_int(nd.w));
+      const float4 lo = key_scenes[sc].key_lo, sca = key_scenes[sc].key_scale;
+      const uint32_t key = ray_sort_key(f3(no), f3(nd), f3(lo), f3(sca));
+      pool.keys[o] = (key & ~0xffu) | (uint32_t)sc;
+    }
+  }
+}
+
+template <bool DIRECT>
 __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ scenes, const JobRec* __restrict__ jobs,
                                               Film film, RayBuf batch, const int* __restrict__ slots,
                                               const float4* __restrict__ hits,
                                               const uint32_t* __restrict__ order, int n_max,
                                               const int* __restrict__ n_dev, RayBuf next, ShadowBuf sh,
-                                              int* sh_count, uint32_t* job_done) {
+                                              int* sh_count, uint32_t* job_done, BinPool pool,
+                                              const SceneRec* __restrict__ key_scenes) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = dev_count(n_max, n_dev);
   if (blockIdx.x * blockDim.x >= n) return;  // whole block past the batch
@@ -720,8 +885,8 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   if (live) {
     const int i = order ? (int)order[j] : j;
     const int src = slots ? slots[i] : i;
-    // the batch's rays are only read here (the pool is rewritten by the next
-    // partition, after this kernel): the read-only path serves them
+    // the batch's rays are only read here (their chunks are rewritten only
+    // after this kernel): the read-only path serves them
     const float4 ro = __ldg(&batch.o[src]), rd = __ldg(&batch.d[src]), rw = __ldg(&batch.w[src]), h = hits[i];
     const int k = __float_as_int(h.w);
     const int info = __float_as_int(rd.w);
@@ -926,7 +1091,9 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   const int ended = (live && !cont) ? job : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, ended);
   if (ended >= 0 && lane == __ffs(peers) - 1) atomicAdd(&job_done[ended], (uint32_t)__popc(peers));
-  if (live) {
+  if (DIRECT) {
+    bin_append(pool, cont ? ray_bin(f3(nd), pool.nbins) : -1, no, nd, nw, key_scenes);
+  } else if (live) {
     next.o[j] = no;
     next.d[j] = cont ? nd : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
     next.w[j] = nw;
@@ -1307,7 +1474,7 @@ int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s
 }
 
 int launch_pool_reset(BinPool& pool, cudaStream_t s) {
-  const int n = std::max(pool.num_chunks, kMaxBins);
+  const int n = std::max(std::max(pool.num_chunks, kMaxBins), pool.pend ? kMaxBins * pool.pend_cols : 0);
   k_pool_reset<<<grid_for(n), TB, 0, s>>>(pool);
   return 1;
 }
@@ -1325,8 +1492,13 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s) {
 }
 
 int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, Counters* ctr,
-                cudaStream_t s) {
-  k_plan<<<1, kBinRadix, 0, s>>>(pool, batch_cap, merge, scene_bits, plan, ctr);
+                cudaStream_t s, bool direct) {
+  k_plan<<<1, kBinRadix, 0, s>>>(pool, batch_cap, merge, scene_bits, plan, ctr, direct ? 1 : 0);
+  return 1;
+}
+
+int launch_append_commit(BinPool& pool, cudaStream_t s) {
+  k_append_commit<<<1, kCommitBlock, 0, s>>>(pool);
   return 1;
 }
 
@@ -1439,10 +1611,15 @@ int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t 
 
 int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const int* slots,
                  const float4* hits, const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count,
-                 uint32_t* job_done, cudaStream_t s, const int* n_dev) {
+                 uint32_t* job_done, cudaStream_t s, const int* n_dev, const BinPool* direct,
+                 const SceneRec* key_scenes) {
   if (n <= 0) return 0;
-  k_shade<<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, slots, hits, order, n, n_dev, next, sh, sh_count,
-                                     job_done);
+  if (direct)
+    k_shade<true><<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, slots, hits, order, n, n_dev, next, sh,
+                                             sh_count, job_done, *direct, key_scenes);
+  else
+    k_shade<false><<<grid_for(n), TB, 0, s>>>(scenes, jobs, film, batch, slots, hits, order, n, n_dev, next, sh,
+                                              sh_count, job_done, BinPool(), nullptr);
   return 1;
 }
 

@@ -106,7 +106,13 @@ struct Film {            // per-sample radiance and film position, all jobs (Ima
 };
 
 // Error bits reported through the engine's device flag word.
-enum : int { ERR_BIN_OVERFLOW = 1, ERR_STACK_OVERFLOW = 2, ERR_TRAVERSAL_CAP = 4, ERR_BVH_INDEX = 8 };
+enum : int {
+  ERR_BIN_OVERFLOW = 1,
+  ERR_STACK_OVERFLOW = 2,
+  ERR_TRAVERSAL_CAP = 4,
+  ERR_BVH_INDEX = 8,
+  ERR_APPEND_WAIT = 16  // a bin append waited past its cap for a chunk another lane was taking
+};
 
 // Direction bins: the reference's 6 cardinal bins (dominant axis and sign),
 // or the 26 / 98 surface cells of a 3^3 / 5^3 direction cube (extension).
@@ -168,14 +174,29 @@ struct BinPool {
   uint32_t* tile_counts = nullptr;  // partition scratch ((kMaxBins + 1) * tiles)
   int max_tiles = 0;
   int* err = nullptr;
+  // Direct binning (shading appends continuing rays into the bins; batches of
+  // at least kDirectMin rays): each bin's append cursor, the chunks taken for
+  // the appends past the bin's held chunks (pend_cols per bin; -1 not taken
+  // yet, -2 a failed take; the chunk table itself still maps the batch's own
+  // rays while they are read) and the chunks of the batch in flight, returned
+  // to the free stack after its shading.
+  int* cursor = nullptr;     // device [kMaxBins]
+  int* pend = nullptr;       // device [kMaxBins * pend_cols]
+  int pend_cols = 0;
+  int* retired = nullptr;    // device [retire_cap]
+  int* n_retired = nullptr;  // device
+  int retire_cap = 0;
 };
+// Smallest batch whose plan keeps each touched bin chunk-aligned (direct binning).
+constexpr int kDirectMin = 2 * kChunk;
 __host__ __device__ __forceinline__ int pool_index(const int* table, int max_chunks, int bin, int pos) {
   return table[bin * max_chunks + (pos >> kChunkShift)] * kChunk + (pos & (kChunk - 1));
 }
 // Chunks a pool needs so that `rays_in_flight` rays fit in any split over
-// the bins (each bin holds at most one partial chunk).
-inline size_t bin_pool_chunks(size_t rays_in_flight) {
-  return (rays_in_flight + kChunk - 1) / kChunk + 2 * (size_t)kMaxBins;
+// the bins (each bin holds at most one partial chunk), with room for the
+// chunks of one batch of `batch` rays held back while its shading appends.
+inline size_t bin_pool_chunks(size_t rays_in_flight, size_t batch = 0) {
+  return (rays_in_flight + kChunk - 1) / kChunk + (batch + kChunk - 1) / kChunk + 3 * (size_t)kMaxBins;
 }
 // Empties the pool: every chunk free (stream-ordered).
 int launch_pool_reset(BinPool& pool, cudaStream_t s);
@@ -189,9 +210,15 @@ int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s
 
 // The next batch from the bins: the fullest bin's top, topped up from the
 // next fullest while merge is set (the order of the host's choice before).
-// Also opens the batch: shadow count zeroed, counters.
+// Also opens the batch: shadow count zeroed, counters.  direct: the batch's
+// shading appends into the bins (launch_shade with the pool), so each bin the
+// batch takes from is left chunk-aligned, the batch's chunks are held back
+// until launch_append_commit and the append cursors are set.
 int launch_plan(BinPool& pool, int batch_cap, int merge, int scene_bits, BatchPlan* plan, Counters* ctr,
-                cudaStream_t s);
+                cudaStream_t s, bool direct = false);
+// After a direct-binning shade: the appended rays join their bins and the
+// batch's chunks return to the free stack.
+int launch_append_commit(BinPool& pool, cudaStream_t s);
 // Direction bin of each direction (6, 26 or 98 bins).
 int launch_ray_bins(const float4* d, int n, int nbins, int* out, cudaStream_t s);
 
@@ -227,9 +254,13 @@ int launch_gather_u32(const uint32_t* src, const uint32_t* idx, int n, uint32_t*
                       const int* n_dev = nullptr);
 // Fills the scene's face texels from their seed (FP16 bits of k / 1024).
 int launch_face_texels(unsigned short* texels, int64_t faces, int res, uint32_t seed, cudaStream_t s);
+// Continuing rays go to `next` (one record per hit, ended paths dead), or
+// with `direct` straight into the pool's bins (plan made with direct set);
+// key_scenes (direct only, optional): also store each ray's sort key.
 int launch_shade(const SceneRec* scenes, const JobRec* jobs, Film film, const RayBuf& batch, const int* slots,
                  const float4* hits, const uint32_t* order, int n, RayBuf next, ShadowBuf sh, int* sh_count,
-                 uint32_t* job_done, cudaStream_t s, const int* n_dev = nullptr);
+                 uint32_t* job_done, cudaStream_t s, const int* n_dev = nullptr, const BinPool* direct = nullptr,
+                 const SceneRec* key_scenes = nullptr);
 // shadow_total (optional): the batch's shadow count is added to it.
 int launch_trace_shadow(const SceneRec* scenes, int num_scenes, const SceneRec& scene0, const ShadowBuf& sh,
                         const int* sh_count, int max_n, float4* sample_rgb, int* err, cudaStream_t s,
