@@ -810,28 +810,26 @@ int Core::enqueue_batch(int index, bool overlap) {
     StageClock t(this, MSC_STAGE_OTHER);
     t.done(launch_plan(bins_, B, merge_bins ? 1 : 0, scene_bits, plan_, ctr_, st, direct));
   }
-  const uint32_t* perm = nullptr;
+  // traversal and shading read the batch's rays where the bins hold them
+  // (RayDecompress, RayDecompress.cpp:5-29, needs no copy here), through the
+  // pool index of each ray in sorted order: sorted as the values beside the
+  // keys, or listed in batch order without the ray sort
   if (ray_sort) {
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      t.done(launch_ray_keys(bins_, plan_, B, ray_key_bits_used(), keys_, st));
+      t.done(launch_ray_keys(bins_, plan_, B, ray_key_bits_used(), keys_, st, perm_));
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
-    const int l = sort_pairs(keys_, nullptr, keys_sorted_, perm_, B, ray_key_bits_used(), ss_, st, errw, nb,
-                             sort_digits);
+    const int l = sort_pairs(keys_, perm_, keys_sorted_, reinterpret_cast<uint32_t*>(slots_), B, ray_key_bits_used(),
+                             ss_, st, errw, nb, sort_digits);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;
     }
     t.done(l);
-    perm = perm_;
-  }
-  {
+  } else {
     StageClock t(this, MSC_STAGE_GATHER);
-    // traversal and shading read the batch's rays where the bins hold them
-    // (RayDecompress, RayDecompress.cpp:5-29, needs no copy here), through
-    // the pool index of each ray in sorted order
-    t.done(launch_batch_slots(bins_, plan_, B, perm, slots_, st));
+    t.done(launch_batch_slots(bins_, plan_, B, nullptr, slots_, st));
   }
   const RayBuf& rays = bins_.rays;
   const int* slots = slots_;

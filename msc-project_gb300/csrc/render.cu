@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kCommitBlock) k_append_commit(BinPool pool) {
 // spans several; the bin is the run's, the scene sits in the key's low byte.
 __global__ void __launch_bounds__(TB) k_ray_keys(const uint32_t* __restrict__ pool_keys, const int* __restrict__ table,
                                                  int max_chunks, const BatchPlan* __restrict__ plan, int key_bits,
-                                                 uint32_t* __restrict__ keys) {
+                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ where) {
   __shared__ Segments seg;
   const int n = plan->nb;
   if ((int)(blockIdx.x * blockDim.x) >= n) return;  // the whole block
@@ -485,7 +485,9 @@ __global__ void __launch_bounds__(TB) k_ray_keys(const uint32_t* __restrict__ po
     else hi = mid - 1;
   }
   const int bin = seg.bin[lo];
-  const uint32_t pk = pool_keys[pool_index(table, max_chunks, bin, seg.start[lo] + (i - seg.prefix[lo]))];
+  const int at = pool_index(table, max_chunks, bin, seg.start[lo] + (i - seg.prefix[lo]));
+  if (where) where[i] = (uint32_t)at;
+  const uint32_t pk = pool_keys[at];
   uint32_t key = pk & ~0xffu;
   const int prefix_bits = plan->prefix_bits;
   if (prefix_bits > 0) {
@@ -1503,9 +1505,9 @@ int launch_append_commit(BinPool& pool, cudaStream_t s) {
 }
 
 int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
-                    cudaStream_t s) {
+                    cudaStream_t s, uint32_t* where) {
   if (n_max <= 0) return 0;
-  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.keys, pool.table, pool.max_chunks, plan, key_bits, keys);
+  k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.keys, pool.table, pool.max_chunks, plan, key_bits, keys, where);
   return 1;
 }
 

@@ -227,8 +227,10 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 
 // Sort keys of the batch rays from pool.keys: (scene, direction bin) above the
 // key when prefix_bits > 0; only the top key_bits bits are kept (shifted down).
+// where (optional): each batch ray's pool index, which sorted beside the keys
+// gives the rays' slots in sorted order.
 int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
-                    cudaStream_t s);
+                    cudaStream_t s, uint32_t* where = nullptr);
 // ray_sort_key of n rays (o, d as float4) in the origin box lo + [0, 64 / scale).
 int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, float3 scale, uint32_t* keys,
                            cudaStream_t s);
