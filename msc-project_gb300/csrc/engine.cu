@@ -137,10 +137,12 @@ int plain_setup(msc_handle* h) {
     return MSC_ERR_ARG;
   }
   const int e = std::min(d.settings.bin_exponent, 24);
-  uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(32ull << e, 1ull << 22);
+  // paths in flight: 64 times the scene's batch (fuller bins, so the batches
+  // stay full for more of the pass)
+  uint64_t gen = d.ext.generation > 0 ? (uint64_t)d.ext.generation : std::max<uint64_t>(64ull << e, 1ull << 22);
   gen = std::max<uint64_t>(std::min<uint64_t>(gen, paths), 1);
-  // capacity for eight times the scene's batch so the autotuner can also try larger ones
-  int rc = h->core.init(std::min(e + 3, 23), (int)gen, paths, d.ext.wide_bvh != 0);
+  // capacity for sixteen times the scene's batch so the autotuner can also try larger ones
+  int rc = h->core.init(std::min(e + 4, 24), (int)gen, paths, d.ext.wide_bvh != 0);
   if (rc != MSC_OK) {
     h->err = h->core.err;
     return rc;
@@ -149,9 +151,10 @@ int plain_setup(msc_handle* h) {
   h->core.hit_sort = d.ext.hit_sort != 0;
   {
     TuneChoice c = h->core.choice();
-    // eight times the scene's bin exponent (Settings.h:16-24): larger
-    // traversal grids amortise the kernels' tails
-    c.batch_exp = std::min(e + 3, 23);
+    // sixteen times the scene's batch (2^bin exponent, Settings.h:16-24):
+    // larger traversal grids amortise the kernels' tails and larger sorted
+    // batches trace more coherently
+    c.batch_exp = std::min(e + 4, 24);
     c.bins = d.ext.bins;
     h->core.apply(c);
   }
