@@ -161,6 +161,9 @@ def test_scene_info_is_the_triangle_box(built, scenes):
 
 
 def test_results_do_not_depend_on_the_tuning_choice(built, scenes):
+    """Every tuning gives the same images bit for bit: batch sizes below 2^13
+    partition the continuing rays through staging, larger ones append them
+    straight into their bins from the shading kernel."""
     mscgpu, _ = built
     ref, rids = _batch(mscgpu, scenes, JOBS)
     want = [ref.image(i) for i in rids]
@@ -170,7 +173,10 @@ def test_results_do_not_depend_on_the_tuning_choice(built, scenes):
                 dict(batch_exponent=14, trace_block=128, ray_sort=False, hit_sort=False),
                 dict(batch_exponent=13, trace_block=128, ray_sort=True, hit_sort=False, persistent=True, bins=26),
                 dict(batch_exponent=12, trace_block=64, ray_sort=True, hit_sort=True, bins=98, digit_bits=11),
-                dict(batch_exponent=14, trace_block=256, ray_sort=True, hit_sort=True, digit_bits=4)):
+                dict(batch_exponent=14, trace_block=256, ray_sort=True, hit_sort=True, digit_bits=4),
+                # direct binning (batches of 2^13 rays and more) into 98 bins, and with 24-bit ray keys
+                dict(batch_exponent=13, trace_block=64, ray_sort=True, hit_sort=False, bins=98),
+                dict(batch_exponent=14, trace_block=128, ray_sort=True, hit_sort=False, bins=26, ray_key_bits=24)):
         b = mscgpu.Batch(batch_exponent=14, film_samples=1 << 22)
         for s in scenes:
             b.add_scene(s)
