@@ -107,6 +107,38 @@ JobSpec spec_of(const msc_job_desc& d) {
 
 // ================================================================ plain form
 
+// The host image of a plain handle: allocated page-locked by the driver
+// (cudaMallocHost), so the copy after every pass runs at the host link's
+// speed; an ordinary allocation when that fails (pageable copies still work).
+struct HostImage {
+  float* p = nullptr;
+  size_t n = 0;
+  bool pinned = false;
+  std::vector<float> fallback;
+  float* data() { return p; }
+  size_t size() const { return n; }
+  float* begin() { return p; }
+  float* end() { return p + n; }
+  void assign(size_t count, float v) {
+    release();
+    n = count;
+    pinned = cudaMallocHost(reinterpret_cast<void**>(&p), std::max<size_t>(n, 1) * sizeof(float)) == cudaSuccess;
+    if (!pinned) {
+      cudaGetLastError();
+      fallback.assign(std::max<size_t>(n, 1), v);
+      p = fallback.data();
+    }
+    std::fill(p, p + n, v);
+  }
+  void release() {
+    if (pinned && p) cudaFreeHost(p);
+    p = nullptr;
+    pinned = false;
+    fallback.clear();
+  }
+  ~HostImage() { release(); }
+};
+
 struct msc_handle {
   Core core;
   SceneDesc desc;
@@ -117,14 +149,10 @@ struct msc_handle {
   int job = -1;
   int iteration = 0;
   bool host_stale = false;
-  std::vector<float> h_pixels;  // page-locked once sized (pixels_pinned), for fast image copies
-  bool pixels_pinned = false;
+  HostImage h_pixels;
   msc_stats stats;
   double load_ms = 0, bvh_ms = 0;  // msc_create's scene parse and device BVH build, wall clock
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
-  ~msc_handle() {
-    if (pixels_pinned) cudaHostUnregister(h_pixels.data());
-  }
 };
 
 namespace {
@@ -179,11 +207,6 @@ int plain_setup(msc_handle* h) {
     return rc;
   }
   h->h_pixels.assign((size_t)3 * d.width * d.height, 0.f);
-  // the image is copied to the host every pass: page-locked memory takes the
-  // copy at full link speed (the vector keeps its size, so its memory stays put)
-  h->pixels_pinned = cudaHostRegister(h->h_pixels.data(), h->h_pixels.size() * sizeof(float),
-                                      cudaHostRegisterDefault) == cudaSuccess;
-  if (!h->pixels_pinned) cudaGetLastError();  // pageable copies still work
   if (cudaEventCreate(&h->ev_begin) != cudaSuccess || cudaEventCreate(&h->ev_end) != cudaSuccess) {
     h->err = "cannot create CUDA events";
     return MSC_ERR_CUDA;
