@@ -1293,55 +1293,84 @@ union FilterSmem {
   FilterSmemPart pa;
 };
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// This thread's share of the staging: element j of a chunk is sample k of
-// source pixel src; gbase is that source's first sample (-1: outside the image).
+// This thread's share of the staging: as kFsN is a multiple of kFtChunk, all
+// its copies of a chunk are the same sample slot k = thread % kFtChunk, of
+// source pixels thread / kFtChunk + j * kFsN / kFtChunk.  gbase is that
+// source's sample k (-1: outside the image); srgb / spos are the shared-memory
+// byte offsets of the copies within a staging buffer.
+static_assert(kFsN % kFtChunk == 0, "each thread stages one sample slot");
 struct FilterCopies {  // the film pool indexes samples with 31 bits
   int gbase[kFtChunk];
-  int dst[kFtChunk];  // src | k << 16
+  uint32_t srgb[kFtChunk], spos[kFtChunk];
+  int k;
 };
 
 __device__ __forceinline__ FilterCopies filter_copies(const JobRec& f, int x0, int y0) {
   FilterCopies fc;
   const int W = f.width, H = f.height;
+  fc.k = (int)threadIdx.x % kFtChunk;
 #pragma unroll
   for (int j = 0; j < kFtChunk; ++j) {
-    const int e = threadIdx.x + j * kFsN;
-    const int src = e / kFtChunk, k = e - src * kFtChunk;
+    const int src = (int)threadIdx.x / kFtChunk + j * (kFsN / kFtChunk);
     const int sx = x0 - 1 + src / kFsY, sy = y0 - 1 + src % kFsY;
     const bool ok = sx >= 0 && sx < W && sy >= 0 && sy < H;
-    fc.gbase[j] = ok ? (int)((int64_t)f.sample_base + ((int64_t)sx * H + sy) * f.spp + k) : -1;
-    fc.dst[j] = src | (k << 16);
+    fc.gbase[j] = ok ? (int)((int64_t)f.sample_base + ((int64_t)sx * H + sy) * f.spp + fc.k) : -1;
+    fc.srgb[j] = (uint32_t)(offsetof(FilterStage, rgb) + ((size_t)fc.k * kFrgbPitch + src) * sizeof(float4));
+    fc.spos[j] = (uint32_t)(offsetof(FilterStage, pos) + ((size_t)fc.k * kFposPitch + src) * sizeof(float2));
   }
   return fc;
 }
 
+__device__ __forceinline__ void cp_async16_s(uint32_t s, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8_s(uint32_t s, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
 // Issues the copies of samples [s0, s0 + cs) of every source pixel of the tile
-// as one commit group (an empty group when cs <= 0, which keeps the count of
-// groups behind each chunk fixed).
-__device__ __forceinline__ void filter_stage(FilterStage& st, const FilterCopies& fc, const Film& film, int s0,
-                                             int cs) {
+// into the staging buffer at shared address st, as one commit group (an empty
+// group when cs <= 0, which keeps the count of groups behind each chunk fixed).
+__device__ __forceinline__ void filter_stage(uint32_t st, const FilterCopies& fc, const Film& film, int s0, int cs) {
+  if (fc.k < cs) {
 #pragma unroll
-  for (int j = 0; j < kFtChunk; ++j) {
-    const int src = fc.dst[j] & 0xffff, k = fc.dst[j] >> 16;
-    if (k < cs && fc.gbase[j] >= 0) {
-      const size_t g = (size_t)fc.gbase[j] + (size_t)s0;
-      cp_async16(&st.rgb[k][src], &film.rgb[g]);
-      cp_async8(&st.pos[k][src], &film.pos[g]);
+    for (int j = 0; j < kFtChunk; ++j) {
+      if (fc.gbase[j] >= 0) {
+        const size_t g = (size_t)(fc.gbase[j] + s0);
+        cp_async16_s(st + fc.srgb[j], &film.rgb[g]);
+        cp_async8_s(st + fc.spos[j], &film.pos[g]);
+      }
     }
   }
   cp_async_commit();
+}
+
+// One sample of this thread's source pixel into its nine partial sums.
+__device__ __forceinline__ void filter_fold(const FilterStage& st, int k, int q, const float* cxs, const float* cys,
+                                            float4* acc) {
+  const float2 p = st.pos[k][q];
+  const float4 cc = st.rgb[k][q];
+  float wx[3], wy[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    wx[a] = fmaxf(0.f, 1.f - fabsf(p.x - cxs[a]));
+    wy[a] = fmaxf(0.f, 1.f - fabsf(p.y - cys[a]));
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const float m = wx[a] * wy[b];
+      float4& r = acc[a * 3 + b];
+      r.w = r.w + m;
+      r.x = fmaf(cc.x, m, r.x);
+      r.y = fmaf(cc.y, m, r.y);
+      r.z = fmaf(cc.z, m, r.z);
+    }
 }
 
 __global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
@@ -1364,10 +1393,11 @@ __global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
     cys[a] = (float)(qy + a - 1) + 0.5f;
   }
   const int chunks = (spp + kFtChunk - 1) / kFtChunk;
+  const uint32_t st0 = (uint32_t)__cvta_generic_to_shared(&sm.st[0]);
   // chunks 0 .. kFtStages-2 in flight before the loop
 #pragma unroll
   for (int c = 0; c < kFtStages - 1; ++c)
-    filter_stage(sm.st[c], fc, film, c * kFtChunk, min(kFtChunk, spp - c * kFtChunk));
+    filter_stage(st0 + c * (uint32_t)sizeof(FilterStage), fc, film, c * kFtChunk, min(kFtChunk, spp - c * kFtChunk));
   for (int c = 0; c < chunks; ++c) {
     const int s0 = c * kFtChunk, cs = min(kFtChunk, spp - s0);
     // this thread's copies of chunk c have landed (the kFtStages-2 groups
@@ -1378,30 +1408,16 @@ __global__ void __launch_bounds__(kFsN, 3) k_filter_tent(JobRec f, Film film) {
     __syncthreads();
     {
       const int cn = c + kFtStages - 1;
-      filter_stage(sm.st[cn % kFtStages], fc, film, cn * kFtChunk, min(kFtChunk, spp - cn * kFtChunk));
+      filter_stage(st0 + (uint32_t)(cn % kFtStages) * (uint32_t)sizeof(FilterStage), fc, film, cn * kFtChunk,
+                   min(kFtChunk, spp - cn * kFtChunk));
     }
     const FilterStage& st = sm.st[c % kFtStages];
     if (qvalid) {
-      for (int k = 0; k < cs; ++k) {
-        const float2 p = st.pos[k][q];
-        const float4 cc = st.rgb[k][q];
-        float wx[3], wy[3];
+      if (cs == kFtChunk) {  // a full chunk: the folds unrolled
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          wx[a] = fmaxf(0.f, 1.f - fabsf(p.x - cxs[a]));
-          wy[a] = fmaxf(0.f, 1.f - fabsf(p.y - cys[a]));
-        }
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            const float m = wx[a] * wy[b];
-            float4& r = acc[a * 3 + b];
-            r.w = r.w + m;
-            r.x = fmaf(cc.x, m, r.x);
-            r.y = fmaf(cc.y, m, r.y);
-            r.z = fmaf(cc.z, m, r.z);
-          }
+        for (int k = 0; k < kFtChunk; ++k) filter_fold(st, k, q, cxs, cys, acc);
+      } else {
+        for (int k = 0; k < cs; ++k) filter_fold(st, k, q, cxs, cys, acc);
       }
     }
   }
