@@ -796,33 +796,47 @@ __device__ __forceinline__ int ld_volatile_i(const int* p) { return *(const vola
 // Direct binning: the continuing ray (dead when b < 0) joins direction bin b
 // at a position from the bin's cursor.  One atomic per bin and block, and the
 // block's rays of one bin keep their block order (warps, then lanes), so runs
-// of rays that were traced next to each other stay together in the bin.
-// Positions past the chunks the bin held at the plan fall in chunks taken
-// from the free stack by the lane that holds the chunk's first position; the
-// others wait for it (bounded).  All threads of the block call this.
+// of rays that were traced next to each other stay together in the bin: the
+// block counts its rays per warp and bin (bin_count), one thread per bin
+// scans the warps' counts and takes the block's run from the cursor
+// (bin_scan), and each ray then has its position (bin_place).  Positions past
+// the chunks the bin held at the plan fall in chunks taken from the free
+// stack by the lane that holds the chunk's first position; the others wait
+// for it (bounded).
 constexpr int kShadeWarps = TB / 32;
-__device__ __forceinline__ void bin_append(const BinPool& pool, int b, float4 no, float4 nd, float4 nw,
-                                           const SceneRec* __restrict__ key_scenes) {
-  __shared__ int wcnt[kShadeWarps][kMaxBins];  // per warp and bin: count, then the warp's offset in the block's run
-  __shared__ int bbase[kMaxBins];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nbins = pool.nbins;
-  for (int i = threadIdx.x; i < kShadeWarps * nbins; i += TB) wcnt[i / nbins][i % nbins] = 0;
-  __syncthreads();
+struct BinBlock {
+  int wcnt[kShadeWarps][kMaxBins];  // per warp and bin: count, then the warp's offset in the block's run
+  int bbase[kMaxBins];              // the block's first position in each bin
+};
+
+__device__ __forceinline__ void bin_zero(BinBlock& bb, int nbins) {
+  for (int i = threadIdx.x; i < kShadeWarps * nbins; i += TB) bb.wcnt[i / nbins][i % nbins] = 0;
+}
+
+// All lanes of the warp call this; returns the lanes of the warp in the same bin.
+__device__ __forceinline__ unsigned bin_count(BinBlock& bb, int b) {
+  const int lane = threadIdx.x & 31;
   const unsigned peers = __match_any_sync(0xffffffffu, b);
-  if (b >= 0 && lane == __ffs(peers) - 1) wcnt[warp][b] = __popc(peers);
-  __syncthreads();
-  if (threadIdx.x < nbins) {
-    int run = 0;
-    for (int w = 0; w < kShadeWarps; ++w) {
-      const int c = wcnt[w][threadIdx.x];
-      wcnt[w][threadIdx.x] = run;
-      run += c;
-    }
-    bbase[threadIdx.x] = run > 0 ? atomicAdd(&pool.cursor[threadIdx.x], run) : 0;
+  if (b >= 0 && lane == __ffs(peers) - 1) bb.wcnt[threadIdx.x >> 5][b] = __popc(peers);
+  return peers;
+}
+
+// Thread t of [0, nbins) of the calling threads: bin t's run for the block.
+__device__ __forceinline__ void bin_scan(BinBlock& bb, const BinPool& pool, int t) {
+  int run = 0;
+  for (int w = 0; w < kShadeWarps; ++w) {
+    const int c = bb.wcnt[w][t];
+    bb.wcnt[w][t] = run;
+    run += c;
   }
-  __syncthreads();
-  const int pos = b >= 0 ? bbase[b] + wcnt[warp][b] + __popc(peers & ((1u << lane) - 1u)) : 0;
+  bb.bbase[t] = run > 0 ? atomicAdd(&pool.cursor[t], run) : 0;
+}
+
+// All lanes of the warp call this (after bin_scan, behind a block barrier).
+__device__ __forceinline__ void bin_place(const BinBlock& bb, const BinPool& pool, int b, unsigned peers, float4 no,
+                                          float4 nd, float4 nw, const SceneRec* __restrict__ key_scenes) {
+  const int lane = threadIdx.x & 31;
+  const int pos = b >= 0 ? bb.bbase[b] + bb.wcnt[threadIdx.x >> 5][b] + __popc(peers & ((1u << lane) - 1u)) : 0;
   int chunk = -1;
   int* wait_on = nullptr;
   if (b >= 0) {
@@ -1058,14 +1072,21 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   // the block's shadow rays are appended grouped by light (a block-wide
   // counting sort on the light index modulo kShadowGroups; the order inside a
   // group does not matter), so the occlusion kernel's warps trace rays from
-  // one neighbourhood toward one light
+  // one neighbourhood toward one light; with direct binning the continuing
+  // rays are counted per bin under the same block barriers
+  __shared__ BinBlock bb;
+  const int bin = (DIRECT && cont) ? ray_bin(f3(nd), pool.nbins) : -1;
+  unsigned bin_peers = 0u;
   {
     __shared__ int grp[kShadowGroups];
     if (threadIdx.x < kShadowGroups) grp[threadIdx.x] = 0;
+    if (DIRECT) bin_zero(bb, pool.nbins);
     __syncthreads();
     const int g = light & (kShadowGroups - 1);
     const int rank = emit ? atomicAdd(&grp[g], 1) : 0;
+    if (DIRECT) bin_peers = bin_count(bb, bin);
     __syncthreads();
+    if (DIRECT && threadIdx.x >= 32 && threadIdx.x < 32 + pool.nbins) bin_scan(bb, pool, threadIdx.x - 32);
     if (threadIdx.x < 32) {  // exclusive scan of the group counts, two per lane
       const int a = grp[2 * lane], b = grp[2 * lane + 1];
       int incl = a + b;
@@ -1094,7 +1115,7 @@ __global__ void __launch_bounds__(TB, 4) k_shade(const SceneRec* __restrict__ sc
   const unsigned peers = __match_any_sync(0xffffffffu, ended);
   if (ended >= 0 && lane == __ffs(peers) - 1) atomicAdd(&job_done[ended], (uint32_t)__popc(peers));
   if (DIRECT) {
-    bin_append(pool, cont ? ray_bin(f3(nd), pool.nbins) : -1, no, nd, nw, key_scenes);
+    bin_place(bb, pool, bin, bin_peers, no, nd, nw, key_scenes);
   } else if (live) {
     next.o[j] = no;
     next.d[j] = cont ? nd : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
