@@ -663,7 +663,7 @@ TUNE_KEYS = ("batch_exponent", "trace_block", "ray_sort", "hit_sort", "bins", "p
              "ray_key_bits")
 
 
-def hbm_stages(prof, peak, spp, batch_exponent):
+def hbm_stages(prof, peak, spp, batch_exponent, digit_bits=8):
     """Achieved HBM bandwidth of the bandwidth-bound stages from one profiled
     pass: algorithmic bytes per ray (or per sample) / the stage's event time."""
     sm = prof["stage_ms"]
@@ -686,7 +686,9 @@ def hbm_stages(prof, peak, spp, batch_exponent):
                                                      "continuation ray 48 B and shadow ray 48 B written")
     for name, ms, nbytes, what in (
             ("bins", sm["bins"], bins_bytes, bins_what),
-            ("ray_sort", sm["ray_sort"], 36.0 * closest, "36 B per key: histogram read + two 16 B passes"),
+            ("ray_sort", sm["ray_sort"], (32.0 if digit_bits == 8 else 36.0) * closest,
+             "32 B per key: two 16 B passes (the ray-key kernel counts the digits)" if digit_bits == 8 else
+             "36 B per key: histogram read + two 16 B passes"),
             ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)"),
             ("shade", sm["shade"], shade_bytes, shade_what)):
         if ms > 0:
@@ -819,7 +821,7 @@ def run_gpu(args):
                                 "average full-size launch",
                 "alg_bytes": "52 B per closest-hit query (ray 32 B read, hit 20 B written; BVH bytes excluded)",
                 "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()}, "top_stage": top,
-                "hbm_stages": hbm_stages(prof, peak, info["spp"], tuned_d["batch_exponent"])}
+                "hbm_stages": hbm_stages(prof, peak, info["spp"], tuned_d["batch_exponent"], tuned_d["digit_bits"])}
     lat = sorted(dev_ms)
     out = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

@@ -815,13 +815,17 @@ int Core::enqueue_batch(int index, bool overlap) {
   // pool index of each ray in sorted order: sorted as the values beside the
   // keys, or listed in batch order without the ray sort
   if (ray_sort) {
+    // with 8-bit digits (and a key of whole digits) the key kernel also
+    // counts the sort's digits
+    const bool fused = sort_digits == 8 && ray_key_bits_used() % 8 == 0;
     {
       StageClock t(this, MSC_STAGE_RAYKEYS);
-      t.done(launch_ray_keys(bins_, plan_, B, ray_key_bits_used(), keys_, st, perm_));
+      if (fused) CK(cudaMemsetAsync(ss_.hist, 0, (size_t)kSortHistWords * 4 + 64, st));
+      t.done(launch_ray_keys(bins_, plan_, B, ray_key_bits_used(), keys_, st, perm_, fused ? ss_.hist : nullptr));
     }
     StageClock t(this, MSC_STAGE_RAYSORT);
     const int l = sort_pairs(keys_, perm_, keys_sorted_, reinterpret_cast<uint32_t*>(slots_), B, ray_key_bits_used(),
-                             ss_, st, errw, nb, sort_digits);
+                             ss_, st, errw, nb, sort_digits, nullptr, fused);
     if (l < 0) {
       err = "internal: ray sort without distinct outputs";
       return MSC_ERR_CUDA;

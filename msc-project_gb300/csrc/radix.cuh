@@ -164,9 +164,13 @@ struct SortTestHook {
 // the pass count is odd, and returns -1 otherwise.
 // digit_bits: 4, 8 or 11 (an 11-bit sort needs scratch bound for 11 bits,
 // else it falls back to 8).  hook (tests only): see SortTestHook.
+// hist_ready (8-bit digits only): the caller zeroed s.hist and s.ctl (one
+// memset of kSortHistWords * 4 + 64 bytes from s.hist) and then counted the
+// keys' digits into s.hist (pass p's digit d at p * 256 + d) while it made
+// them, so the sort skips its own counting pass.
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
                int bits, SortScratch& s, cudaStream_t stream, int* err = nullptr, const int* n_dev = nullptr,
-               int digit_bits = 8, const SortTestHook* hook = nullptr);
+               int digit_bits = 8, const SortTestHook* hook = nullptr, bool hist_ready = false);
 
 constexpr int kSortErrLookback = 256;
 

@@ -469,6 +469,30 @@ __global__ void __launch_bounds__(kCommitBlock) k_append_commit(BinPool pool) {
 // scene's box in place of the reference's per-batch origin box,
 // RayBoundingbox.cpp:5-50), under (scene, direction bin) when the batch
 // spans several; the bin is the run's, the scene sits in the key's low byte.
+// The sort key and pool index of batch ray i (the segments in shared memory).
+__device__ __forceinline__ uint32_t batch_ray_key(const uint32_t* __restrict__ pool_keys,
+                                                  const int* __restrict__ table, int max_chunks,
+                                                  const BatchPlan* __restrict__ plan, const Segments& seg,
+                                                  int key_bits, int i, int* where) {
+  int lo = 0, hi = seg.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg.prefix[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  const int bin = seg.bin[lo];
+  const int at = pool_index(table, max_chunks, bin, seg.start[lo] + (i - seg.prefix[lo]));
+  *where = at;
+  const uint32_t pk = pool_keys[at];
+  uint32_t key = pk & ~0xffu;
+  const int prefix_bits = plan->prefix_bits;
+  if (prefix_bits > 0) {
+    const uint32_t prefix = ((pk & 0xffu) << plan->bin_bits) | (uint32_t)bin;
+    key = (prefix << (32 - prefix_bits)) | (key >> prefix_bits);
+  }
+  return key >> (32 - key_bits);
+}
+
 __global__ void __launch_bounds__(TB) k_ray_keys(const uint32_t* __restrict__ pool_keys, const int* __restrict__ table,
                                                  int max_chunks, const BatchPlan* __restrict__ plan, int key_bits,
                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ where) {
@@ -478,23 +502,36 @@ __global__ void __launch_bounds__(TB) k_ray_keys(const uint32_t* __restrict__ po
   load_segments(plan, seg);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int lo = 0, hi = seg.count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (seg.prefix[mid] <= i) lo = mid;
-    else hi = mid - 1;
-  }
-  const int bin = seg.bin[lo];
-  const int at = pool_index(table, max_chunks, bin, seg.start[lo] + (i - seg.prefix[lo]));
+  int at;
+  keys[i] = batch_ray_key(pool_keys, table, max_chunks, plan, seg, key_bits, i, &at);
   if (where) where[i] = (uint32_t)at;
-  const uint32_t pk = pool_keys[at];
-  uint32_t key = pk & ~0xffu;
-  const int prefix_bits = plan->prefix_bits;
-  if (prefix_bits > 0) {
-    const uint32_t prefix = ((pk & 0xffu) << plan->bin_bits) | (uint32_t)bin;
-    key = (prefix << (32 - prefix_bits)) | (key >> prefix_bits);
+}
+
+// The same, with the sort's 8-bit digit counts of every pass taken on the way
+// (hist zeroed beforehand; pass p's digit d at p * 256 + d): a grid-stride
+// loop over the batch, counts gathered in shared memory per block.
+constexpr int kKeyHistBlocks = 4 * 152;
+__global__ void __launch_bounds__(TB) k_ray_keys_hist(const uint32_t* __restrict__ pool_keys,
+                                                      const int* __restrict__ table, int max_chunks,
+                                                      const BatchPlan* __restrict__ plan, int key_bits,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ where,
+                                                      uint32_t* __restrict__ hist) {
+  __shared__ Segments seg;
+  __shared__ uint32_t cnt[4 * 256];
+  const int n = plan->nb;
+  const int passes = key_bits / 8;
+  for (int k = threadIdx.x; k < passes * 256; k += TB) cnt[k] = 0u;
+  load_segments(plan, seg);  // (syncs)
+  for (int i = blockIdx.x * TB + threadIdx.x; i < n; i += gridDim.x * TB) {
+    int at;
+    const uint32_t key = batch_ray_key(pool_keys, table, max_chunks, plan, seg, key_bits, i, &at);
+    keys[i] = key;
+    where[i] = (uint32_t)at;
+    for (int p = 0; p < passes; ++p) atomicAdd(&cnt[p * 256 + ((key >> (8 * p)) & 0xffu)], 1u);
   }
-  keys[i] = key >> (32 - key_bits);
+  __syncthreads();
+  for (int k = threadIdx.x; k < passes * 256; k += TB)
+    if (cnt[k]) atomicAdd(&hist[k], cnt[k]);
 }
 
 __global__ void __launch_bounds__(TB) k_ray_keys_direct(const float4* __restrict__ o, const float4* __restrict__ d,
@@ -1542,8 +1579,13 @@ int launch_append_commit(BinPool& pool, cudaStream_t s) {
 }
 
 int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
-                    cudaStream_t s, uint32_t* where) {
+                    cudaStream_t s, uint32_t* where, uint32_t* hist) {
   if (n_max <= 0) return 0;
+  if (hist && where && key_bits % 8 == 0 && key_bits <= 32) {
+    const int blocks = std::min((n_max + TB - 1) / TB, kKeyHistBlocks);
+    k_ray_keys_hist<<<blocks, TB, 0, s>>>(pool.keys, pool.table, pool.max_chunks, plan, key_bits, keys, where, hist);
+    return 1;
+  }
   k_ray_keys<<<grid_for(n_max), TB, 0, s>>>(pool.keys, pool.table, pool.max_chunks, plan, key_bits, keys, where);
   return 1;
 }

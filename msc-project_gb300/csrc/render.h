@@ -228,9 +228,12 @@ int launch_cardinal(const float4* d, int n, int* out, cudaStream_t s);
 // Sort keys of the batch rays from pool.keys: (scene, direction bin) above the
 // key when prefix_bits > 0; only the top key_bits bits are kept (shifted down).
 // where (optional): each batch ray's pool index, which sorted beside the keys
-// gives the rays' slots in sorted order.
+// gives the rays' slots in sorted order.  hist (optional, with where; key_bits
+// a multiple of 8): the 8-bit digit counts of every pass of the keys are
+// added into it (zeroed beforehand), as an 8-bit-digit sort with hist_ready
+// takes them.
 int launch_ray_keys(const BinPool& pool, const BatchPlan* plan, int n_max, int key_bits, uint32_t* keys,
-                    cudaStream_t s, uint32_t* where = nullptr);
+                    cudaStream_t s, uint32_t* where = nullptr, uint32_t* hist = nullptr);
 // ray_sort_key of n rays (o, d as float4) in the origin box lo + [0, 64 / scale).
 int launch_ray_keys_direct(const float4* o, const float4* d, int n, float3 lo, float3 scale, uint32_t* keys,
                            cudaStream_t s);

@@ -339,7 +339,8 @@ void sort_scratch_bind(SortScratch* s, void* base, int capacity, int max_digit_b
 namespace {
 template <int RB>
 int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n, int bits,
-             SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, const SortTestHook* hook) {
+             SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, const SortTestHook* hook,
+             bool hist_ready) {
   using S = SortShape<RB>;
   const int passes = (bits + RB - 1) / RB;
   if (n_dev && (passes == 0 || ((passes % 2) == 1 && (keys_in == keys_out || (vals_in && vals_in == vals_out)))))
@@ -354,11 +355,13 @@ int onesweep(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_ou
   uint32_t* status1 = s.status + (size_t)tiles * S::RADIX;
   // zero the first look-back array, the histograms, the tile counters and the error word
   cudaMemsetAsync(status0, 0, (size_t)tiles * S::RADIX * 4, stream);
-  cudaMemsetAsync(s.hist, 0, (size_t)kSortHistWords * 4 + 64, stream);
   int* errw = err ? err : (int*)(s.ctl + kSortMaxPassesAny);
-  const int hist_blocks = std::min(std::max(1, (n + S::TILE - 1) / S::TILE), 4 * 152);
-  k_onesweep_hist<RB><<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
-  ++launches;
+  if (!hist_ready || RB != 8 || src_k != keys_in) {
+    cudaMemsetAsync(s.hist, 0, (size_t)kSortHistWords * 4 + 64, stream);
+    const int hist_blocks = std::min(std::max(1, (n + S::TILE - 1) / S::TILE), 4 * 152);
+    k_onesweep_hist<RB><<<hist_blocks, kSortBlock, 0, stream>>>(src_k, n, n_dev, passes, bits, s.hist);
+    ++launches;
+  }
   for (int p = 0; p < passes; ++p) {
     const bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t* dst_k = to_out ? keys_out : s.keys_alt;
@@ -390,15 +393,15 @@ void sort_init() {
 
 int sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, int n,
                int bits, SortScratch& s, cudaStream_t stream, int* err, const int* n_dev, int digit_bits,
-               const SortTestHook* hook) {
+               const SortTestHook* hook, bool hist_ready) {
   if (n <= 0) return 0;
   sort_init();
   if (digit_bits > s.max_digit_bits) digit_bits = 8;  // scratch sized for narrower digits
   if (digit_bits == 4)
-    return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
+    return onesweep<4>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook, false);
   if (digit_bits == 11)
-    return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
-  return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook);
+    return onesweep<11>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook, false);
+  return onesweep<8>(keys_in, vals_in, keys_out, vals_out, n, bits, s, stream, err, n_dev, hook, hist_ready);
 }
 
 }  // namespace mscg
