@@ -670,27 +670,29 @@ def hbm_stages(prof, peak, spp, batch_exponent, digit_bits=8):
     closest = prof["closest_queries"]
     paths = prof["width"] * prof["height"] * spp
     out = {}
-    # batches of 2^13 rays and more bin directly: the shading writes each
-    # continuing ray (48 B) and its sort key (4 B) into its bin, and the bins
-    # stage is the partition of the camera rays plus one small commit per
-    # batch; smaller batches partition every ray through staging (read 48 B,
-    # written 48 B with its 4 B key, plus the count, scan and commit passes)
+    # the camera rays are made straight into their bins (film sample 24 B and
+    # the ray with its key 52 B written, its bin byte written and read); batches
+    # of 2^13 rays and more bin directly: the shading writes each continuing
+    # ray (48 B) and its sort key (4 B) into its bin, and the bins stage is one
+    # small commit per batch; smaller batches partition the continuing rays
+    # through staging (read 48 B, written 48 B with its 4 B key, plus the
+    # count, scan and commit passes)
+    stages = [("raygen", sm["raygen"], 78.0 * paths, "78 B per camera ray: film sample 24 B, ray and key 52 B "
+                                                     "into its bin, its bin byte 2 B")]
     if batch_exponent >= 13:
-        bins_bytes, bins_what = 112.0 * paths, "112 B per camera ray partitioned into the bins"
         shade_bytes, shade_what = 164.0 * closest, ("164 B per closest hit: ray 48 B and hit 16 B read, continuation "
                                                      "ray 48 B with its 4 B key into its bin and shadow ray 48 B "
                                                      "written")
     else:
-        bins_bytes, bins_what = 112.0 * closest, "112 B per ray entering the bins"
+        stages.append(("bins", sm["bins"], 112.0 * max(0, closest - paths), "112 B per continuing ray partitioned"))
         shade_bytes, shade_what = 160.0 * closest, ("160 B per closest hit: ray 48 B and hit 16 B read, "
                                                      "continuation ray 48 B and shadow ray 48 B written")
-    for name, ms, nbytes, what in (
-            ("bins", sm["bins"], bins_bytes, bins_what),
+    for name, ms, nbytes, what in stages + [
             ("ray_sort", sm["ray_sort"], (32.0 if digit_bits == 8 else 36.0) * closest,
              "32 B per key: two 16 B passes (the ray-key kernel counts the digits)" if digit_bits == 8 else
              "36 B per key: histogram read + two 16 B passes"),
             ("filter", sm["filter"], 24.0 * paths, "24 B per film sample (radiance 16 B + position 8 B)"),
-            ("shade", sm["shade"], shade_bytes, shade_what)):
+            ("shade", sm["shade"], shade_bytes, shade_what)]:
         if ms > 0:
             gbs = nbytes / (ms / 1e3) / 1e9
             out[name] = {"ms": round(ms, 3), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4), "alg_bytes": what}

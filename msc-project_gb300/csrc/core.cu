@@ -191,14 +191,15 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   const size_t pool_rays = chunks * (size_t)kChunk;
   const int pend_cols = B / kChunk + 2;              // new chunks one batch's appends can take per bin
   const int retire_cap = B / kChunk + kMaxBins + 1;  // chunks one batch can hold back
-  size_t bytes = 3 * al256(pool_rays * sizeof(float4)) + 3 * al256((size_t)S * sizeof(float4)) +
+  size_t bytes = 3 * al256(pool_rays * sizeof(float4)) + 3 * al256((size_t)B * sizeof(float4)) +
                  2 * al256((size_t)kMaxBins * 4) + al256((size_t)kMaxBins * max_chunks * 4) + al256(chunks * 4) +
                  al256(4) +
                  10 * al256((size_t)B * 4) + al256(sizeof(Counters)) +
                  al256(pool_rays * 4) + al256(sizeof(BatchPlan)) +
                  sort_scratch_bytes(B, 11) + al256((size_t)B * sizeof(float4)) + 6 * al256((size_t)B * sizeof(float4)) +
                  al256((size_t)(kMaxBins + 1) * part_tiles * 4) + al256((size_t)kMaxBins * 4) +
-                 al256((size_t)kMaxBins * pend_cols * 4) + al256((size_t)retire_cap * 4) + al256(4) + 4096;
+                 al256((size_t)kMaxBins * pend_cols * 4) + al256((size_t)retire_cap * 4) + al256(4) + al256((size_t)S) +
+                 4096;
   CK(cudaMalloc(&arena_, bytes));
   Arena A{arena_, 0};
   bins_.rays.o = A.take<float4>(pool_rays);
@@ -212,9 +213,10 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   bins_.free_stack = A.take<int>(chunks);
   bins_.free_top = A.take<int>(1);
   A.take<int>(kMaxBins);  // spare
-  staging_.o = A.take<float4>(S);
-  staging_.d = A.take<float4>(S);
-  staging_.w = A.take<float4>(S);
+  // continuing rays of batches too small for direct binning
+  staging_.o = A.take<float4>(B);
+  staging_.d = A.take<float4>(B);
+  staging_.w = A.take<float4>(B);
   slots_ = A.take<int>(B);
   keys_ = A.take<uint32_t>(B);
   keys_sorted_ = A.take<uint32_t>(B);
@@ -243,6 +245,7 @@ int Core::init(int batch_exponent, int generation, size_t sample_capacity, bool 
   bins_.retired = A.take<int>(retire_cap);
   bins_.retire_cap = retire_cap;
   bins_.n_retired = A.take<int>(1);
+  cam_digits_ = A.take<uint8_t>(S);
   bins_.count = ctr_->bin_count;
   bins_.in_bins = &ctr_->in_bins;
   bins_.err = &ctr_->err;
@@ -751,16 +754,16 @@ int Core::generate(bool* did) {
     if (j.slot < 0 || j.complete || j.generated >= j.paths) continue;
     const uint64_t n = std::min<uint64_t>(want - filled, j.paths - j.generated);
     if (n == 0) break;
-    RayBuf out{staging_.o + filled, staging_.d + filled, staging_.w + filled};
-    launches += launch_raygen(j.rec, j.slot, (uint32_t)j.generated, (int)n, out, film_, stream_);
+    // the camera rays go straight into their bins, in sample order
+    // (Camera.cpp:42-44, DirectionalBins::add), made twice instead of staged
+    launches += launch_camera_rays(j.rec, j.slot, (uint32_t)j.generated, (int)n, film_, bins_,
+                                   ray_sort ? d_scenes_ : nullptr, cam_digits_, stream_);
     j.generated += n;
     filled += n;
     if (filled >= want) break;
   }
   t.done(launches);
   if (filled > 0) {
-    StageClock tb(this, MSC_STAGE_BINS);
-    tb.done(launch_bin_partition(staging_, (int)filled, bins_, stream_, nullptr, ray_sort ? d_scenes_ : nullptr));
     stats.generations += 1;
     *did = true;
   }

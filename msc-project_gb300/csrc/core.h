@@ -228,6 +228,7 @@ class Core {
   SortScratch ss_;
   float4* hits_ = nullptr;
   int* slots_ = nullptr;  // pool index of each batch ray (sorted order)
+  uint8_t* cam_digits_ = nullptr;  // direction bin of each camera ray of a top-up
   ShadowBuf shadow_[2];          // shadow queues, alternating between batches
   cudaStream_t side_ = nullptr;  // occlusion of batch k runs here beside batch k+1's front part
   static constexpr int kGraphBodies = 4;

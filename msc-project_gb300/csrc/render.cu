@@ -66,10 +66,9 @@ __device__ __forceinline__ int seg_source(const Segments& seg, const int* table,
 // PinHoleCamera::sample (src/core/PinHoleCamera.cpp:16-32) /
 // ThinLensCamera::sample (src/core/ThinLensCamera.cpp:16-56).
 // sampleID = x*H*spp + y*spp + i (Camera.cpp:28), local to the job.
-__global__ void __launch_bounds__(TB) k_raygen(JobRec f, int job_index, uint32_t first, int n, RayBuf out, Film film) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const uint32_t sid = first + (uint32_t)t;
+// The camera ray of sample sid and its film position.
+__device__ __forceinline__ void camera_ray(const JobRec& f, int job_index, uint32_t sid, float4* ro, float4* rd,
+                                           float4* rw, float2* fpos) {
   const uint32_t col = (uint32_t)f.height * (uint32_t)f.spp;
   const uint32_t x = sid / col;
   const uint32_t rem = sid - x * col;
@@ -90,8 +89,7 @@ __global__ void __launch_bounds__(TB) k_raygen(JobRec f, int job_index, uint32_t
     sy = (float)iy * celly + u01(r.y) * celly;
   }
   const float px = (float)x + sx, py = (float)y + sy;
-  film.rgb[f.sample_base + sid] = make_float4(0.f, 0.f, 0.f, 0.f);
-  film.pos[f.sample_base + sid] = make_float2(px, py);
+  *fpos = make_float2(px, py);
   const float W = (float)f.width, H = (float)f.height;
   const float fx = ((px * 2.f - W) / W) * 36.f;
   const float fy = ((py * 2.f - H) / W) * 36.f;
@@ -130,9 +128,9 @@ __global__ void __launch_bounds__(TB) k_raygen(JobRec f, int job_index, uint32_t
     org = nodal;
     dir = v_normalize(v_sub(nodal, fp));
   }
-  out.o[t] = make_float4(org.x, org.y, org.z, 1.f);
-  out.d[t] = make_float4(dir.x, dir.y, dir.z, __int_as_float(ray_info(job_index, f.scene, 0)));
-  out.w[t] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)sid));
+  *ro = make_float4(org.x, org.y, org.z, 1.f);
+  *rd = make_float4(dir.x, dir.y, dir.z, __int_as_float(ray_info(job_index, f.scene, 0)));
+  *rw = make_float4(1.f, 1.f, 1.f, __int_as_float((int)sid));
 }
 
 // -------------------------------------------------------- bin partition
@@ -284,6 +282,88 @@ __global__ void k_part_commit(const uint32_t* __restrict__ scanned, int tiles, B
   const int c = min(pool.count[b] + added, pool.held[b] << kChunkShift);
   atomicAdd(pool.in_bins, c - pool.count[b]);
   pool.count[b] = c;
+}
+
+// ------------------------------------------------- camera rays into the bins
+// The camera rays of samples [first, first + n) of a job go into the bins in
+// the same stable counting partition as the continuing rays (sample order
+// inside each bin), without a staging copy: a counting kernel makes each
+// tile's rays for their direction bins (kept, one byte per ray, and the film
+// samples written), the partition's scan and reserve hand out the positions,
+// and a scatter kernel ranks the kept bins and makes each ray again - the
+// same arithmetic, so the same bits - to write it into its position.  Sample
+// t of the range is tile t / kPartTile's item.
+__global__ void __launch_bounds__(PB) k_cam_count(JobRec f, int job_index, uint32_t first, int n, Film film,
+                                                  int nbins, uint32_t* __restrict__ counts, int tiles,
+                                                  uint8_t* __restrict__ digits) {
+  __shared__ int hist[PRADIX];
+  for (int i = threadIdx.x; i < PRADIX; i += PB) hist[i] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kPartTile;
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < PITEMS; ++k) {
+    const int idx = base + k * PB + threadIdx.x;
+    int dg = -1;
+    if (idx < n) {
+      const uint32_t sid = first + (uint32_t)idx;
+      float4 ro, rd, rw;
+      float2 fp;
+      camera_ray(f, job_index, sid, &ro, &rd, &rw, &fp);
+      film.rgb[f.sample_base + sid] = make_float4(0.f, 0.f, 0.f, 0.f);
+      film.pos[f.sample_base + sid] = fp;
+      dg = ray_bin(f3(rd), nbins);
+      digits[idx] = (uint8_t)dg;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, dg);
+    if (dg >= 0 && lane == __ffs(peers) - 1) atomicAdd(&hist[dg], __popc(peers));
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g <= nbins; g += PB) counts[g * tiles + blockIdx.x] = (uint32_t)hist[g];
+}
+
+__global__ void __launch_bounds__(PB) k_cam_scatter(JobRec f, int job_index, uint32_t first, int n,
+                                                    const uint32_t* __restrict__ scanned, int tiles, BinPool pool,
+                                                    const SceneRec* __restrict__ key_scenes,
+                                                    const uint8_t* __restrict__ digits) {
+  __shared__ RankSmem<PB, PRADIX> sm;
+  __shared__ uint32_t sidx[kPartTile];
+  __shared__ int gofs[PRADIX];
+  const int tile = blockIdx.x, base = tile * kPartTile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nbins = pool.nbins;
+  for (int b = threadIdx.x; b < PRADIX; b += PB)
+    gofs[b] = (b < nbins) ? pool.count[b] + (int)(scanned[b * tiles + tile] - scanned[b * tiles]) : 0;
+  int dig[PITEMS], pos[PITEMS];
+#pragma unroll
+  for (int k = 0; k < PITEMS; ++k) {
+    const int idx = base + warp * 32 * PITEMS + k * 32 + lane;
+    dig[k] = idx < n ? (int)digits[idx] : -1;
+  }
+  tile_rank<PB, PITEMS, PRADIX>(dig, pos, sm);
+#pragma unroll
+  for (int k = 0; k < PITEMS; ++k)
+    if (pos[k] >= 0) sidx[pos[k]] = (uint32_t)((warp * 32 * PITEMS + k * 32 + lane) | (dig[k] << 16));
+  __syncthreads();
+  const int count = min(kPartTile, n - base);
+  for (int p = threadIdx.x; p < count; p += PB) {
+    const uint32_t e = sidx[p];
+    const int b = (int)(e >> 16);
+    const int at = gofs[b] + (p - sm.tile_start[b]);
+    if ((at >> kChunkShift) >= pool.held[b]) continue;  // no chunk reserved: reported by k_part_reserve
+    const int o = pool_index(pool.table, pool.max_chunks, b, at);
+    float4 ro, rd, rw;
+    float2 fp;
+    camera_ray(f, job_index, first + (uint32_t)(base + (int)(e & 0xffffu)), &ro, &rd, &rw, &fp);
+    pool.rays.o[o] = ro;
+    pool.rays.d[o] = rd;
+    pool.rays.w[o] = rw;
+    if (key_scenes) {  // the ray sort key, in the ray's scene box
+      const int sc = f.scene;
+      const float4 lo = key_scenes[sc].key_lo, sca = key_scenes[sc].key_scale;
+      const uint32_t key = ray_sort_key(f3(ro), f3(rd), f3(lo), f3(sca));
+      pool.keys[o] = (key & ~0xffu) | (uint32_t)sc;
+    }
+  }
 }
 
 __global__ void k_pool_reset(BinPool pool) {
@@ -1529,10 +1609,17 @@ __global__ void __launch_bounds__(TB) k_filter_box(JobRec f, Film film) {
 
 }  // namespace
 
-int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s) {
+int launch_camera_rays(const JobRec& job, int job_index, uint32_t first, int n, Film film, BinPool& pool,
+                       const SceneRec* key_scenes, uint8_t* digits, cudaStream_t s) {
   if (n <= 0) return 0;
-  k_raygen<<<grid_for(n), TB, 0, s>>>(job, job_index, first, n, out, film);
-  return 1;
+  const int tiles = (n + kPartTile - 1) / kPartTile;
+  k_cam_count<<<tiles, PB, 0, s>>>(job, job_index, first, n, film, pool.nbins, pool.tile_counts, tiles, digits);
+  k_scan_exclusive<<<1, 1024, 0, s>>>(pool.tile_counts, tiles * (pool.nbins + 1), nullptr);
+  k_part_reserve<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
+  k_cam_scatter<<<tiles, PB, 0, s>>>(job, job_index, first, n, pool.tile_counts, tiles, pool,
+                                     pool.keys ? key_scenes : nullptr, digits);
+  k_part_commit<<<1, kBinRadix, 0, s>>>(pool.tile_counts, tiles, pool);
+  return 5;
 }
 
 int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev,

@@ -156,7 +156,6 @@ struct Counters {
 };
 
 // Each launcher returns the number of kernels it enqueued.
-int launch_raygen(const JobRec& job, int job_index, uint32_t first, int n, RayBuf out, Film film, cudaStream_t s);
 
 struct BinPool {
   RayBuf rays;               // num_chunks * kChunk rays
@@ -207,6 +206,13 @@ constexpr int kPartTile = 2048;
 // scenes (optional): also store each ray's sort key (pool.keys) for the ray sort.
 int launch_bin_partition(const RayBuf& src, int n, BinPool& pool, cudaStream_t s, const int* n_dev = nullptr,
                          const SceneRec* scenes = nullptr);
+// Camera rays of samples [first, first + n) of a job straight into their
+// direction bins in sample order (a stable partition whose rays are made
+// twice instead of staged), their film samples zeroed and positioned;
+// key_scenes (optional): also store each ray's sort key; digits: scratch of
+// n bytes (each ray's bin between the two kernels).
+int launch_camera_rays(const JobRec& job, int job_index, uint32_t first, int n, Film film, BinPool& pool,
+                       const SceneRec* key_scenes, uint8_t* digits, cudaStream_t s);
 
 // The next batch from the bins: the fullest bin's top, topped up from the
 // next fullest while merge is set (the order of the host's choice before).
